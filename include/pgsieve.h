@@ -1,0 +1,170 @@
+/*
+ * libpgsieve -- GB300 (sm_103a) method2 combined sieve, C ABI.
+ *
+ * The reference (sethtroisi/prime-gap) has no library interface for this
+ * path: its boundary is the combined_sieve process, whose entry point is
+ * prime_gap_parallel(Config&) (combined_sieve.cpp:2014) writing the unknowns
+ * file through save_unknowns_method2 (combined_sieve.cpp:1261).  This header
+ * is the C boundary a host program (the bundled combined_sieve CLI, or a
+ * ctypes/cgo/JNI binding) calls instead.  Plain pointers and sizes only.
+ *
+ * Errors are returned as negative status codes; the library never exits,
+ * aborts or traps.  One context per device; calls on one context are
+ * serialised internally.
+ */
+#ifndef PGSIEVE_H
+#define PGSIEVE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PGS_OK 0
+#define PGS_EINVAL (-1)   /* job rejected by the reference's validation (exit(1) there) */
+#define PGS_ENOMEM (-2)   /* device or host allocation failed */
+#define PGS_ECUDA (-3)    /* CUDA runtime error (message in pgs_last_error) */
+#define PGS_EABORT (-4)   /* a job the reference itself aborts on with an assert */
+#define PGS_ENODEV (-5)   /* no usable CUDA device */
+#define PGS_ETIMEOUT (-6) /* a bounded device-side wait gave up */
+
+typedef struct pgs_ctx pgs_ctx;
+
+/*
+ * One method2 job: the Config fields combined_sieve reads
+ * (gap_common.h:39-89).  max_prime is absolute (the CLI's --max-prime is in
+ * millions, gap_common.cpp:937-939).  compression: 0 plain text (default),
+ * 1 --rle, 2 --bitcompressed (Config::compression, gap_common.h:57-62).
+ */
+typedef struct {
+    uint32_t p;
+    uint32_t d;
+    uint64_t mstart;
+    uint64_t minc;
+    uint32_t sieve_length;
+    uint64_t max_prime;
+    int32_t compression;
+    int32_t reserved;
+} pgs_job;
+
+/* Stage indexes of pgs_result.ms_stage (device time from CUDA events). */
+enum {
+    PGS_STAGE_SETUP = 0,  /* host tables -> device */
+    PGS_STAGE_PRIMES = 1, /* segmented sieve */
+    PGS_STAGE_KMOD = 2,   /* K mod p */
+    PGS_STAGE_LARGE = 3,  /* large-prime marks */
+    PGS_STAGE_ROWS = 4,   /* small primes + merge + compaction */
+    PGS_STAGE_TEXT = 5,   /* scan + formatting */
+    PGS_STAGE_D2H = 6,    /* text -> host */
+    PGS_NSTAGES = 8
+};
+
+typedef struct {
+    char *text;            /* unknowns file contents; owned by the library */
+    uint64_t text_len;
+    uint64_t rows;         /* valid m = rows of the file */
+    uint64_t primes;       /* sieving primes: primes <= prime_limit */
+    uint64_t prime_limit;  /* largest number whose prime factors are sieved */
+    uint64_t unknowns;     /* total unknown offsets */
+    double ms_total;       /* device time from setup to the last stage */
+    double ms_stage[PGS_NSTAGES];
+    uint64_t launches;     /* kernels launched for this job */
+    void *internal;        /* owner of `text`; do not touch */
+} pgs_result;
+
+/* Create a context on CUDA device `device`. */
+int pgs_create(int device, pgs_ctx **out);
+void pgs_destroy(pgs_ctx *ctx);
+/* Human-readable description of the last error on this context. */
+const char *pgs_last_error(pgs_ctx *ctx);
+/* Use an external CUDA stream (cudaStream_t as void*); NULL restores the
+ * context's own stream. */
+int pgs_set_stream(pgs_ctx *ctx, void *stream);
+/* The stream the context launches on (cudaStream_t as void*). */
+void *pgs_get_stream(pgs_ctx *ctx);
+
+/*
+ * Run one job end to end and return the unknowns file bytes (replaces
+ * prime_gap_parallel + save_unknowns_method2, combined_sieve.cpp:2014-2447,
+ * 1261-1445).  Output is byte-identical to the reference's file for the same
+ * parameters.  Free with pgs_result_free.
+ */
+int pgs_method2(pgs_ctx *ctx, const pgs_job *job, pgs_result *out);
+void pgs_result_free(pgs_result *r);
+
+/*
+ * Split form for callers that keep the job resident: pgs_prepare uploads the
+ * job's tables, pgs_run runs every sieve stage on the device (no host
+ * transfer) and leaves the text on the device; pgs_fetch copies it out.
+ */
+typedef struct pgs_prepared pgs_prepared;
+int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out);
+int pgs_run(pgs_ctx *ctx, pgs_prepared *prep, int record_stages);
+int pgs_fetch(pgs_ctx *ctx, pgs_prepared *prep, pgs_result *out);
+void pgs_prepared_free(pgs_prepared *prep);
+
+/* Device time of each stage of the last pgs_run on `prep` (waits for it);
+ * out has PGS_NSTAGES entries, *total the whole run. */
+int pgs_stage_ms(pgs_ctx *ctx, pgs_prepared *prep, double *out, double *total);
+
+/*
+ * Measured integer multiply-add issue rate of this device (32-bit IMAD per
+ * second), from a microbenchmark kernel of independent mad.lo.u32 chains.
+ * The integer-pipe roofline denominator of the sieve kernels.
+ */
+int pgs_int_peak(pgs_ctx *ctx, double *imad_per_s);
+
+/*
+ * Derived job parameters, as the reference computes them: valid m count,
+ * offsets coprime to K, SMALL/MEDIUM thresholds of
+ * calculate_thresholds_method2 (gap_common.cpp:345-375), and the unknowns
+ * file name of Args::gen_unknown_fn (gap_common.cpp:732-749).
+ */
+typedef struct {
+    uint64_t valid_ms;
+    uint64_t coprime_x;
+    uint64_t small_threshold;
+    uint64_t medium_threshold;
+    uint64_t prime_limit;
+    uint32_t k_bits;
+    char filename[256];
+} pgs_plan;
+int pgs_plan_job(const pgs_job *job, pgs_plan *out);
+
+/* ---- the reference's number-theory kernels, batched on the device ---- */
+
+/*
+ * Primes in [lo, hi], ascending (replaces primesieve::iterator walks,
+ * combined_sieve.cpp:1475-1502).  Writes min(count, cap) primes.
+ */
+int pgs_primes(pgs_ctx *ctx, uint64_t lo, uint64_t hi, uint64_t *out, size_t cap, size_t *count);
+
+/* K mod q for each q (replaces mpz_fdiv_ui, combined_sieve.cpp:1497, 1856);
+ * K given as little-endian 32-bit limbs; odd q < 2^46. */
+int pgs_k_mod_p(pgs_ctx *ctx, const uint32_t *k_limbs, int n_limbs, const uint64_t *q, size_t n,
+                uint64_t *out);
+
+/* Smallest k >= 1 with l <= k*a mod p <= r, for each i (replaces
+ * _modulo_search_euclid, modulo_search.cpp:101-129); p < 2^46. */
+int pgs_modulo_search(pgs_ctx *ctx, const uint64_t *p, const uint64_t *a, const uint64_t *l,
+                      const uint64_t *r, uint64_t *k_out, size_t n);
+
+/*
+ * Every mi < max_mi with (base_r*(M+mi) + SL) mod prime <= 2*SL, ascending,
+ * with that residue (replaces modulo_search_euclid_all_large,
+ * modulo_search.cpp:339-376).  Needs prime > 4*SL + 2.  Writes up to cap
+ * pairs and the total count.
+ */
+int pgs_large_hits(pgs_ctx *ctx, uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t prime,
+                   uint64_t base_r, uint32_t *mi_out, uint64_t *mod_out, size_t cap,
+                   size_t *count);
+
+/* Library version string. */
+const char *pgs_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,160 @@
+"""ORACLE -- test infrastructure only.
+
+ctypes binding of the C restatement of the reference's method2 sieve
+(oracle/m2_oracle.c).  Only tests, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg use it, and only as the checker.
+"""
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "_build" / "libm2oracle.so"
+BIN_PATH = HERE / "_build" / "m2_oracle"
+
+
+class OJob(ctypes.Structure):
+    _fields_ = [
+        ("p", ctypes.c_uint32),
+        ("d", ctypes.c_uint32),
+        ("mstart", ctypes.c_uint64),
+        ("minc", ctypes.c_uint64),
+        ("sieve_length", ctypes.c_uint32),
+        ("max_prime", ctypes.c_uint64),
+        ("compression", ctypes.c_int32),
+        ("threads", ctypes.c_int32),
+    ]
+
+
+class OPlan(ctypes.Structure):
+    _fields_ = [
+        ("small_threshold", ctypes.c_uint64),
+        ("medium_threshold", ctypes.c_uint64),
+        ("last_prime", ctypes.c_uint64),
+        ("valid_ms", ctypes.c_uint64),
+        ("coprime_x", ctypes.c_uint64),
+        ("prime_limit", ctypes.c_uint64),
+    ]
+
+
+_lib = None
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+
+
+def load() -> ctypes.CDLL:
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise FileNotFoundError(f"oracle not built: {LIB_PATH}")
+        lib = ctypes.CDLL(str(LIB_PATH))
+        lib.pgo_method2.argtypes = [ctypes.POINTER(OJob), ctypes.POINTER(ctypes.c_void_p),
+                                    ctypes.POINTER(ctypes.c_size_t)]
+        lib.pgo_method2.restype = ctypes.c_int
+        lib.pgo_free.argtypes = [ctypes.c_void_p]
+        lib.pgo_modulo_search_euclid_small.restype = ctypes.c_uint32
+        lib.pgo_modulo_search_euclid_small.argtypes = [ctypes.c_uint32] * 4
+        lib.pgo_modulo_search_euclid.restype = ctypes.c_uint64
+        lib.pgo_modulo_search_euclid.argtypes = [ctypes.c_uint64] * 4
+        lib.pgo_modulo_search_euclid_stack.restype = ctypes.c_uint64
+        lib.pgo_modulo_search_euclid_stack.argtypes = [ctypes.c_uint64] * 4
+        lib.pgo_modulo_search_all_large.restype = ctypes.c_size_t
+        lib.pgo_modulo_search_all_large.argtypes = [
+            ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, ctypes.c_uint64,
+            ctypes.POINTER(ctypes.c_uint32), _u64p, ctypes.c_size_t]
+        lib.pgo_build_k.restype = ctypes.c_int
+        lib.pgo_build_k.argtypes = [ctypes.c_uint32, ctypes.c_uint32,
+                                    ctypes.POINTER(ctypes.c_uint32), ctypes.c_int]
+        lib.pgo_k_mod.restype = ctypes.c_uint64
+        lib.pgo_k_mod.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int, ctypes.c_uint64]
+        lib.pgo_primes.restype = ctypes.c_size_t
+        lib.pgo_primes.argtypes = [ctypes.c_uint64, ctypes.c_uint64, _u64p, ctypes.c_size_t]
+        lib.pgo_plan_job.restype = ctypes.c_int
+        lib.pgo_plan_job.argtypes = [ctypes.POINTER(OJob), ctypes.POINTER(OPlan)]
+        lib.pgo_trial_division.restype = ctypes.c_int
+        lib.pgo_trial_division.argtypes = [ctypes.POINTER(OJob), _u64p,
+                                           ctypes.POINTER(ctypes.c_int64), ctypes.c_size_t, _u64p]
+        _lib = lib
+    return _lib
+
+
+def _job(p, d, mstart, minc, sieve_length, max_prime, compression=0, threads=1) -> OJob:
+    return OJob(p, d, mstart, minc, sieve_length, max_prime, compression, threads)
+
+
+def method2(p, d, mstart, minc, sieve_length, max_prime, compression=0, threads=1) -> bytes:
+    """Unknowns file bytes from the CPU restatement (max_prime absolute)."""
+    lib = load()
+    buf = ctypes.c_void_p()
+    n = ctypes.c_size_t()
+    rc = lib.pgo_method2(ctypes.byref(_job(p, d, mstart, minc, sieve_length, max_prime,
+                                           compression, threads)), ctypes.byref(buf), ctypes.byref(n))
+    if rc != 0:
+        raise RuntimeError(f"oracle failed with {rc}")
+    try:
+        return ctypes.string_at(buf, n.value)
+    finally:
+        lib.pgo_free(buf)
+
+
+def plan(p, d, mstart, minc, sieve_length, max_prime) -> dict:
+    lib = load()
+    pl = OPlan()
+    rc = lib.pgo_plan_job(ctypes.byref(_job(p, d, mstart, minc, sieve_length, max_prime)),
+                          ctypes.byref(pl))
+    return {"rc": rc, "small_threshold": pl.small_threshold, "medium_threshold": pl.medium_threshold,
+            "last_prime": pl.last_prime, "valid_ms": pl.valid_ms, "coprime_x": pl.coprime_x,
+            "prime_limit": pl.prime_limit}
+
+
+def build_k(p: int, d: int) -> list[int]:
+    lib = load()
+    buf = (ctypes.c_uint32 * 8192)()
+    n = lib.pgo_build_k(p, d, buf, 8192)
+    if n < 0:
+        raise ValueError(f"bad K ({n})")
+    return list(buf[:n])
+
+
+def k_mod(limbs: list[int], q: int) -> int:
+    lib = load()
+    arr = (ctypes.c_uint32 * len(limbs))(*limbs)
+    return lib.pgo_k_mod(arr, len(limbs), q)
+
+
+def primes(lo: int, hi: int) -> list[int]:
+    lib = load()
+    n = lib.pgo_primes(lo, hi, None, 0)
+    out = (ctypes.c_uint64 * max(1, n))()
+    lib.pgo_primes(lo, hi, out, n)
+    return list(out[:n])
+
+
+def modulo_search(p, a, l, r) -> int:
+    return load().pgo_modulo_search_euclid(p, a, l, r)
+
+
+def modulo_search_stack(p, a, l, r) -> int:
+    return load().pgo_modulo_search_euclid_stack(p, a, l, r)
+
+
+def all_large(M, max_mi, SL, prime, base_r, cap=1 << 20) -> list[tuple[int, int]]:
+    lib = load()
+    mi = (ctypes.c_uint32 * cap)()
+    md = (ctypes.c_uint64 * cap)()
+    n = lib.pgo_modulo_search_all_large(M, max_mi, SL, prime, base_r, mi, md, cap)
+    k = min(n, cap)
+    return list(zip(mi[:k], md[:k]))
+
+
+def trial_division(job: dict, ms: list[int], xs: list[int], threads=8) -> list[int]:
+    """Smallest prime <= the sieve limit dividing m*K + X, or 0."""
+    lib = load()
+    n = len(ms)
+    out = (ctypes.c_uint64 * max(1, n))()
+    m_arr = (ctypes.c_uint64 * max(1, n))(*ms)
+    x_arr = (ctypes.c_int64 * max(1, n))(*xs)
+    rc = lib.pgo_trial_division(ctypes.byref(_job(threads=threads, **job)), m_arr, x_arr, n, out)
+    if rc != 0:
+        raise RuntimeError(f"trial division failed {rc}")
+    return list(out[:n])

@@ -1,0 +1,408 @@
+// Integer arithmetic shared by the sieve kernels and by the host-side unit
+// tests (the same source compiles for sm_103a and for the CPU).
+//
+// Contents
+//   * modular helpers for 32-bit and 64-bit primes (p < 2^46);
+//   * Montgomery reduction used by the K mod p kernel;
+//   * pg_modsearch*: smallest k >= 1 with l <= k*a mod p <= r, the problem
+//     solved by _modulo_search_euclid / _modulo_search_euclid_stack
+//     (modulo_search.cpp:71-193), here as an iterative descent with an
+//     explicit stack whose unwinding also returns the residue k*a mod p;
+//   * pg_three_gap: the two "record" multiples of a modulo p that decide every
+//     return of the orbit y -> y + a (mod p) to the window [0, w) (Slater's
+//     three-gap theorem), computed by a subtractive continued fraction;
+//   * pg_hits_*: all mi in [mi_lo, mi_hi) with (r*(M+mi) + SL) mod p <= 2*SL,
+//     i.e. the enumeration of modulo_search_euclid_all_large
+//     (modulo_search.cpp:339-376), at O(1) per hit after one search.
+#pragma once
+#include <stdint.h>
+
+#if defined(__CUDACC__)
+#define PG_HD __host__ __device__ __forceinline__
+#else
+#define PG_HD inline
+#endif
+
+namespace pg {
+
+PG_HD uint64_t umulhi64(uint64_t a, uint64_t b) {
+#if defined(__CUDA_ARCH__)
+    return __umul64hi(a, b);
+#else
+    return (uint64_t)(((unsigned __int128)a * b) >> 64);
+#endif
+}
+
+// x mod p for p < 2^46 and x < 2^64, from a double-precision quotient
+// estimate corrected with exact 64-bit wrap-around arithmetic.
+PG_HD uint64_t mod_u64(uint64_t x, uint64_t p, double inv_p) {
+    uint64_t q = (uint64_t)((double)x * inv_p);
+    int64_t r = (int64_t)(x - q * p);
+    while (r < 0) r += (int64_t)p;
+    while (r >= (int64_t)p) r -= (int64_t)p;
+    return (uint64_t)r;
+}
+
+// a*b mod p for a, b < p < 2^46 (the product fits in 92 bits; the quotient
+// estimate a*b/p < 2^46 is within 1 of the truth).
+PG_HD uint64_t mulmod_u64(uint64_t a, uint64_t b, uint64_t p, double inv_p) {
+    uint64_t q = (uint64_t)((double)a * (double)b * inv_p);
+    int64_t r = (int64_t)(a * b - q * p);
+    while (r < 0) r += (int64_t)p;
+    while (r >= (int64_t)p) r -= (int64_t)p;
+    return (uint64_t)r;
+}
+
+// -p^{-1} mod 2^32 for odd p (Newton iteration on the 2-adic inverse).
+PG_HD uint32_t neg_inv32(uint32_t p) {
+    uint32_t x = p;  // correct to 3 bits
+    for (int i = 0; i < 4; i++) x *= 2u - p * x;
+    return 0u - x;
+}
+
+// -p^{-1} mod 2^64 for odd p.
+PG_HD uint64_t neg_inv64(uint64_t p) {
+    uint64_t x = p;
+    for (int i = 0; i < 5; i++) x *= 2ull - p * x;
+    return 0ull - x;
+}
+
+// Montgomery reduction, R = 2^32: t * 2^-32 mod p (result < 2p) for t < p*2^32.
+PG_HD uint32_t redc32_lazy(uint64_t t, uint32_t p, uint32_t pinv) {
+    uint32_t m = (uint32_t)t * pinv;
+    uint64_t s = (uint64_t)m * p;
+    // (t + s) is divisible by 2^32; add the high halves and the carry of the low ones.
+    uint64_t hi = (t >> 32) + (s >> 32) + ((uint32_t)t != 0u);
+    return (uint32_t)hi;
+}
+
+PG_HD uint32_t redc32(uint64_t t, uint32_t p, uint32_t pinv) {
+    uint64_t m = (uint32_t)((uint32_t)t * pinv);
+    uint64_t s = m * p;
+    uint64_t hi = (t >> 32) + (s >> 32) + ((uint32_t)t != 0u);
+    return (uint32_t)(hi >= p ? hi - p : hi);
+}
+
+// Montgomery reduction, R = 2^64, of the 128-bit value (hi:lo) < p*2^64;
+// p < 2^63.  Result in [0, p).
+PG_HD uint64_t redc64(uint64_t hi, uint64_t lo, uint64_t p, uint64_t pinv) {
+    uint64_t m = lo * pinv;
+    uint64_t s_hi = umulhi64(m, p);
+    // lo + m*p_lo == 0 mod 2^64, carry out iff lo != 0
+    uint64_t r = hi + s_hi + (lo != 0);
+    return r >= p ? r - p : r;
+}
+
+// ---------------------------------------------------------------------------
+// K mod p by Montgomery multiplication over the limbs of K, most significant
+// first: u <- REDC(u * R^2 + limb) gives u = K * R^-1 after the last limb, and
+// REDC(u * R^2) = K mod p.
+
+// 32-bit odd primes; lazy reduction keeps u < 2p while p < 2^31.
+PG_HD uint32_t kmod32(const uint32_t *limbs, int n, uint32_t p, uint32_t &pinv_out,
+                      uint32_t &r2_out) {
+    const uint32_t pinv = neg_inv32(p);
+    const uint32_t r1 = (0u - p) % p;                          // 2^32 mod p
+    const uint32_t r2 = (uint32_t)(((uint64_t)r1 * r1) % p);  // 2^64 mod p
+    uint32_t u = 0;
+    if (p < 0x80000000u) {
+        for (int i = n - 1; i >= 0; i--) u = redc32_lazy((uint64_t)u * r2 + limbs[i], p, pinv);
+        if (u >= p) u -= p;
+    } else {
+        for (int i = n - 1; i >= 0; i--) u = redc32((uint64_t)u * r2 + limbs[i], p, pinv);
+    }
+    pinv_out = pinv;
+    r2_out = r2;
+    return redc32((uint64_t)u * r2, p, pinv);
+}
+
+// (r * M + sl) mod p with the Montgomery constants of p (M < 3 * 2^32, sl < p).
+PG_HD uint32_t start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p, uint32_t pinv,
+                       uint32_t r2) {
+    uint32_t a = redc32(M, p, pinv);                  // M R^-1
+    uint32_t mm = redc32((uint64_t)a * r2, p, pinv);  // M mod p
+    uint32_t b = redc32((uint64_t)r * mm, p, pinv);   // r M R^-1
+    uint32_t rm = redc32((uint64_t)b * r2, p, pinv);  // r M mod p
+    uint64_t t = (uint64_t)rm + sl;
+    return (uint32_t)(t >= p ? t - p : t);
+}
+
+// Odd primes 2^31 <= p < 2^46 (and any odd p >= 3 below that): R = 2^64.
+PG_HD uint64_t kmod64(const uint32_t *limbs, int n, uint64_t p) {
+    const uint64_t pinv = neg_inv64(p);
+    const uint64_t r1 = (0ull - p) % p;                             // 2^64 mod p
+    const uint64_t r2 = mulmod_u64(r1, r1, p, 1.0 / (double)p);  // 2^128 mod p
+    uint64_t u = 0;
+    const int nw = (n + 1) / 2;
+    for (int i = nw - 1; i >= 0; i--) {
+        uint64_t w = limbs[2 * i];
+        if (2 * i + 1 < n) w |= (uint64_t)limbs[2 * i + 1] << 32;
+        uint64_t lo = u * r2;
+        uint64_t hi = umulhi64(u, r2);
+        uint64_t lo2 = lo + w;
+        hi += lo2 < lo;
+        u = redc64(hi, lo2, p, pinv);
+    }
+    return redc64(umulhi64(u, r2), u * r2, p, pinv);
+}
+
+// ---------------------------------------------------------------------------
+// modulo search
+//
+// Smallest k >= 1 with l <= (k*a mod p) <= r, for 0 < a < p, 1 <= l <= r < p.
+// Follows the reduction of modulo_search.cpp:131-193: mirror when a > p/2,
+// answer directly when a multiple of a falls in [l, r], otherwise recurse on
+// (a, a - p mod a, l mod a, r mod a).  Also returns the residue k*a mod p.
+//
+// Unwinding uses k_i = (k_{i+1} p_i + v_{i+1}) / a_i + floor((l_i - 1)/a_i),
+// an exact division, where v is the residue of the deeper level; the residue
+// of each level is v_i = floor((l_i-1)/a_i)*a_i + v_{i+1} (no reduction
+// needed since it lies in [l_i, r_i]), then un-mirrored.
+
+struct ModSearch32 {
+    uint32_t k;  // smallest k >= 1
+    uint32_t v;  // k*a mod p, in [l, r]
+};
+
+// 32-bit primes: every level has p_i < 2^32, depth <= 32 (p halves per level).
+PG_HD ModSearch32 modsearch32(uint32_t p, uint32_t a, uint32_t l, uint32_t r) {
+    uint32_t st_p[32], st_a[32], st_ldiv[32];
+    uint8_t st_mirror[32];
+    int depth = 0;
+    const uint32_t delta = r - l;
+    uint32_t k, v;
+    for (;;) {
+        bool mirror = a > (p >> 1);
+        if (mirror) {
+            // k*a in [l, r]  <=>  k*(p-a) in [p-r, p-l]
+            a = p - a;
+            l = p - (l + delta);
+        }
+        uint32_t l_div = (l - 1) / a;
+        uint32_t l_mod = l - l_div * a;  // in [1, a]
+        if (l_mod + delta >= a) {
+            // (l_div + 1) * a lies in [l, r]
+            k = l_div + 1;
+            v = k * a;
+            if (mirror) v = p - v;
+            break;
+        }
+        if (depth >= 31) {
+            // unreachable for 0 < a < p < 2^32 (p halves per level); bail out
+            // with "no solution below p" rather than overflow the stack
+            k = 0xFFFFFFFFu;
+            v = l;
+            depth = 0;
+            break;
+        }
+        st_p[depth] = p;
+        st_a[depth] = a;
+        st_ldiv[depth] = l_div;
+        st_mirror[depth] = mirror;
+        depth++;
+        uint32_t new_a = a - (p % a);
+        p = a;
+        a = new_a;
+        l = l_mod;
+    }
+    while (depth > 0) {
+        depth--;
+        uint32_t pi = st_p[depth], ai = st_a[depth], ldiv = st_ldiv[depth];
+        // v is the pre-mirror residue of the deeper level: k*(a_i - p_i mod a_i) mod a_i
+        uint64_t num = (uint64_t)k * pi + v;
+        uint32_t q = (uint32_t)(num / ai);
+        k = q + ldiv;
+        v = ldiv * ai + v;  // post-mirror residue at this level, in [l_i, r_i]
+        if (st_mirror[depth]) v = pi - v;
+    }
+    return {k, v};
+}
+
+struct ModSearch64 {
+    uint64_t k;
+    uint64_t v;
+};
+
+// Primes up to 2^46.  Levels whose modulus is below 2^32 continue in 32-bit.
+PG_HD ModSearch64 modsearch64(uint64_t p, uint64_t a, uint64_t l, uint64_t r) {
+    if (p < 0xFFFFFFFFull) {
+        ModSearch32 s = modsearch32((uint32_t)p, (uint32_t)a, (uint32_t)l, (uint32_t)r);
+        return {s.k, s.v};
+    }
+    uint64_t st_p[24], st_a[24], st_ldiv[24];
+    uint8_t st_mirror[24];
+    int depth = 0;
+    const uint64_t delta = r - l;
+    uint64_t k, v;
+    for (;;) {
+        if (p < 0xFFFFFFFFull) {
+            ModSearch32 s = modsearch32((uint32_t)p, (uint32_t)a, (uint32_t)l,
+                                        (uint32_t)(l + delta));
+            k = s.k;
+            v = s.v;
+            break;
+        }
+        bool mirror = a > (p >> 1);
+        if (mirror) {
+            a = p - a;
+            l = p - (l + delta);
+        }
+        uint64_t l_div = (l - 1) / a;
+        uint64_t l_mod = l - l_div * a;
+        if (l_mod + delta >= a) {
+            k = l_div + 1;
+            v = k * a;
+            if (mirror) v = p - v;
+            break;
+        }
+        if (depth >= 23) {
+            k = ~0ull >> 1;  // unreachable for p < 2^46; see modsearch32
+            v = l;
+            depth = 0;
+            break;
+        }
+        st_p[depth] = p;
+        st_a[depth] = a;
+        st_ldiv[depth] = l_div;
+        st_mirror[depth] = mirror;
+        depth++;
+        uint64_t new_a = a - (p % a);
+        p = a;
+        a = new_a;
+        l = l_mod;
+    }
+    while (depth > 0) {
+        depth--;
+        uint64_t pi = st_p[depth], ai = st_a[depth], ldiv = st_ldiv[depth];
+        // num = k*p_i + v < 2^(46+46); quotient < p_i < 2^46
+        uint64_t lo = k * pi;
+        uint64_t hi = umulhi64(k, pi);
+        uint64_t lo2 = lo + v;
+        hi += (lo2 < lo);
+        // exact division of (hi:lo2) by ai with quotient < 2^46
+        double est = ((double)hi * 18446744073709551616.0 + (double)lo2) / (double)ai;
+        uint64_t q = (uint64_t)est;
+        // correct: rem = num - q*ai in signed 64-bit (|rem| small)
+        int64_t rem = (int64_t)(lo2 - q * ai);
+        while (rem < 0) {
+            q--;
+            rem += (int64_t)ai;
+        }
+        while (rem >= (int64_t)ai) {
+            q++;
+            rem -= (int64_t)ai;
+        }
+        k = q + ldiv;
+        v = ldiv * ai + v;
+        if (st_mirror[depth]) v = pi - v;
+    }
+    return {k, v};
+}
+
+// ---------------------------------------------------------------------------
+// three-gap structure of the rotation y -> y + a (mod p) on the window [0, w)
+//
+// kp = smallest k >= 1 with (k*a mod p) in (0, w),      up  = that residue
+// kn = smallest k >= 1 with (-(k*a) mod p) in (0, w),   dn  = that residue
+// For p > 2w, the first return time from y in [0, w) is
+//   kp       if y + up < w           (landing at y + up)
+//   kn       else if y >= dn         (landing at y - dn)
+//   kp + kn  otherwise               (landing at y + up - dn).
+// (up + dn >= w always holds, so the first two cases are exclusive.)
+// Computed by the subtractive continued fraction that keeps the lattice basis
+// (kp, up), (kn, -dn) with kp*dn + kn*up = p, reducing the larger residue by
+// the smaller until both are below w.
+template <typename T>
+struct ThreeGap {
+    T kp, up, kn, dn;
+};
+
+template <typename T>
+PG_HD ThreeGap<T> three_gap(T p, T a, T w) {
+    T kp = 1, up = a, kn = 1, dn = p - a;
+    // Each pass lowers up or dn by at least one; the pass limit only guards
+    // against non-prime moduli (for prime p, up == dn forces up == dn == 1).
+    for (int pass = 0; pass < 256 && (up >= w || dn >= w); pass++) {
+        if (up > dn) {
+            T q1 = (up - w) / dn + 1;  // first multiple that brings up below w
+            T q2 = (up - 1) / dn;      // multiples that keep up > 0 and stop at up <= dn
+            T q = q1 < q2 ? q1 : q2;
+            if (q == 0) break;
+            up -= q * dn;
+            kp += q * kn;
+        } else {
+            T q1 = (dn - w) / up + 1;
+            T q2 = (dn - 1) / up;
+            T q = q1 < q2 ? q1 : q2;
+            if (q == 0) break;
+            dn -= q * up;
+            kn += q * kp;
+        }
+    }
+    return {kp, up, kn, dn};
+}
+
+// ---------------------------------------------------------------------------
+// hit enumeration
+
+PG_HD void modsearch_any(uint32_t p, uint32_t a, uint32_t l, uint32_t r, uint64_t &k, uint32_t &v) {
+    ModSearch32 s = modsearch32(p, a, l, r);
+    k = s.k;
+    v = s.v;
+}
+PG_HD void modsearch_any(uint64_t p, uint64_t a, uint64_t l, uint64_t r, uint64_t &k, uint64_t &v) {
+    ModSearch64 s = modsearch64(p, a, l, r);
+    k = s.k;
+    v = s.v;
+}
+
+// y(mi_lo) = (t0 + mi_lo * r) mod p from y(0) = t0.
+PG_HD uint32_t advance_residue(uint32_t t0, uint64_t mi_lo, uint32_t r, uint32_t p) {
+    if (mi_lo == 0) return t0;
+    uint32_t m = (uint32_t)(mi_lo % p);
+    uint32_t s = (uint32_t)(((uint64_t)m * r) % p);
+    uint32_t y = t0 + s;
+    if (y >= p || y < t0) y -= p;
+    return y;
+}
+PG_HD uint64_t advance_residue(uint64_t t0, uint64_t mi_lo, uint64_t r, uint64_t p) {
+    if (mi_lo == 0) return t0;
+    uint64_t s = mulmod_u64(mi_lo % p, r, p, 1.0 / (double)p);
+    uint64_t y = t0 + s;
+    return y >= p ? y - p : y;
+}
+
+// Calls emit(mi, y) for every mi in [mi_lo, mi_hi), ascending, with
+// y = (y0 + (mi - mi_lo) * a) mod p <= two_sl, where y0 = y(mi_lo).
+// Needs p > 2 * (two_sl + 1) and 0 < a < p.
+template <typename T, typename Emit>
+PG_HD void enumerate_hits(T p, T a, T y, uint64_t mi_lo, uint64_t mi_hi, T two_sl, Emit &emit) {
+    uint64_t mi = mi_lo;
+    if (mi >= mi_hi) return;
+    if (y > two_sl) {
+        uint64_t k;
+        T v;
+        modsearch_any(p, a, p - y, p - y + two_sl, k, v);
+        mi += k;
+        if (mi >= mi_hi) return;
+        y = y - (p - v);  // (y + v) mod p with v in [p - y, p - y + two_sl]
+    }
+    const ThreeGap<T> g = three_gap<T>(p, a, two_sl + 1);
+    if (g.up > two_sl || g.dn > two_sl) return;  // unreachable for prime p > 2(two_sl+1)
+    for (;;) {
+        emit(mi, y);
+        if (y + g.up <= two_sl) {
+            mi += g.kp;
+            y += g.up;
+        } else if (y >= g.dn) {
+            mi += g.kn;
+            y -= g.dn;
+        } else {
+            mi += (uint64_t)g.kp + g.kn;
+            y = (y + g.up) - g.dn;
+        }
+        if (mi >= mi_hi) return;
+    }
+}
+
+}  // namespace pg

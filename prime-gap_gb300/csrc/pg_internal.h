@@ -1,0 +1,120 @@
+// Internal declarations shared by the CUDA translation units of libpgsieve.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+namespace pg {
+
+// ---- prime sieve (pg_primes.cu) -------------------------------------------
+
+// Odd numbers per sieve segment (one CTA): a 32 KiB shared bitmap.
+constexpr uint32_t kSegBits = 32768u * 8u;
+// Number line covered by one segment.
+constexpr uint64_t kSegSpan = 2ull * kSegBits;
+
+// Base primes for sieving windows up to `limit`: all odd primes <= sqrt(limit).
+struct BasePrimes {
+    uint32_t *d_primes = nullptr;  // device, ascending
+    uint32_t count = 0;
+    uint64_t covers = 0;  // windows up to covers are sievable
+};
+
+// Host-side: build base primes on the device for windows up to `limit`.
+cudaError_t base_primes_build(BasePrimes &bp, uint64_t limit, cudaStream_t stream);
+void base_primes_free(BasePrimes &bp);
+
+// Upper bound on the number of primes in [lo, hi] (Brun-Titchmarsh,
+// Montgomery-Vaughan form), plus slack; used to size output buffers.
+uint64_t prime_count_bound(uint64_t lo, uint64_t hi);
+
+// Sieve the odd primes in [lo, hi] (lo >= 3, hi - lo < 2^32) and append their
+// offsets from `lo` (unordered) to d_out, counting into *d_count (device).
+// cap = capacity of d_out.
+cudaError_t sieve_window(const BasePrimes &bp, uint64_t lo, uint64_t hi, uint32_t *d_out,
+                         uint64_t cap, unsigned long long *d_count, cudaStream_t stream);
+
+// ---- K mod p (pg_kmod.cu) ---------------------------------------------------
+
+// For primes base + off[i] (i < *d_count), write r[i] = K mod p and
+// t0[i] = (r * mstart + SL) mod p.  Primes below 2^32 use 32-bit words
+// (d_r32/d_t032), others 64-bit (d_r64/d_t064).  K limbs on the device.
+cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
+                        const unsigned long long *d_count, uint64_t max_count, uint64_t mstart,
+                        uint32_t sl, void *d_r, void *d_t0, bool wide, cudaStream_t stream);
+
+// K mod q for an explicit list of 32-bit primes (d-primes, tests).
+cudaError_t kmod_list32(const uint32_t *d_klimbs, int nlimbs, const uint32_t *d_q, uint32_t n,
+                        uint32_t *d_r, cudaStream_t stream);
+
+// ---- large primes (pg_large.cu) -----------------------------------------------
+
+struct JobDev {
+    uint64_t mstart;
+    uint32_t minc;
+    uint32_t sl;        // sieve length
+    uint32_t two_sl;    // 2*SL
+    uint32_t rows;      // valid m count
+    uint32_t half_cols; // H: live columns per side
+    uint32_t side_pad;  // Hp: H rounded up to 32, start of the high side
+    uint32_t pitch;     // 32-bit words per composite row
+    const int32_t *row_of_mi;  // minc entries, -1 if gcd(m, d) > 1
+    const int32_t *col_of_x;   // 2*SL+1 entries, -1 if not a live offset
+    uint32_t *comp;            // rows * pitch words
+};
+
+cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
+                         const unsigned long long *d_count, uint64_t max_count, const void *d_r,
+                         const void *d_t0, bool wide, uint32_t hits_per_item, cudaStream_t stream);
+
+// ---- rows: small primes, merge, extract, format (pg_rows.cu) -----------------
+
+struct RowsDev {
+    JobDev job;
+    uint32_t x_par;            // parity of the live offsets' index x = X + SL
+    uint32_t nb;               // positions x in [0, 2SL] with x % 2 == x_par
+    const uint32_t *valid_mi;  // rows entries
+    const uint32_t *dist;      // H live distances, ascending
+    // odd primes dividing d (patterns) and their K mod q
+    uint32_t nd;
+    const uint32_t *dq;
+    const uint32_t *dr;
+    // odd primes in (P, S1] as offsets from sp_base, and K mod p
+    uint32_t sp_base;
+    const uint32_t *sp;
+    const uint32_t *sr;
+    const unsigned long long *sp_count;
+    uint64_t sp_cap;           // capacity of sp / sr
+    uint64_t text_cap;         // capacity of the text buffer
+    // outputs
+    uint32_t *lists;       // rows * 2H distances (low side then high side)
+    uint32_t *counts;      // rows * 2
+    uint64_t *row_bytes;   // rows
+    int compression;       // 0 plain, 1 RLE
+};
+
+cudaError_t rows_extract(const RowsDev &rd, uint32_t rows_per_block, cudaStream_t stream);
+
+// Exclusive scan of n 64-bit values; total written to *d_total.
+cudaError_t scan_u64(const uint64_t *d_in, uint64_t *d_out, uint64_t *d_total, uint64_t n,
+                     uint64_t *d_tmp, cudaStream_t stream);
+uint64_t scan_tmp_words(uint64_t n);
+
+cudaError_t format_rows(const RowsDev &rd, const uint64_t *d_offsets, char *d_text,
+                        cudaStream_t stream);
+
+// ---- C-ABI helpers (pg_tools.cu) -----------------------------------------------
+
+cudaError_t tools_kmod_list64(const uint32_t *d_limbs, int n, const uint64_t *d_q, size_t count,
+                              uint64_t *d_out, cudaStream_t stream);
+cudaError_t tools_modsearch(const uint64_t *p, const uint64_t *a, const uint64_t *l,
+                            const uint64_t *r, uint64_t *k, size_t n, cudaStream_t stream);
+cudaError_t tools_large_hits(uint64_t M, uint32_t max_mi, uint32_t sl, uint64_t p, uint64_t r,
+                             uint32_t *mi_out, uint64_t *mod_out, size_t cap,
+                             unsigned long long *count, cudaStream_t stream);
+
+cudaError_t tools_imad_peak(double *imad_per_s, cudaStream_t stream);
+
+}  // namespace pg

@@ -1,0 +1,87 @@
+// K mod p for every sieving prime: a batched multi-limb reduction of
+// K = P#/d against 32-bit and 64-bit primes by Montgomery multiplication.
+//
+// Replaces mpz_fdiv_ui(K, prime) at combined_sieve.cpp:1497 and 1856 (and the
+// mpz_mod_ui of 1674).  One thread per prime walks the limbs of K from the
+// most significant end: u <- REDC(u * R^2 + limb), so after the last limb
+// u = K * R^-1 and REDC(u * R^2) = K mod p.  K's limbs sit in shared memory
+// and are read as warp-wide broadcasts.
+//
+// Each prime also gets t0 = (r * mstart + SL) mod p, the starting residue of
+// the large-prime walk ((base_r * M + SL) % prime, modulo_search.cpp:345).
+#include "pg_arith.cuh"
+#include "pg_internal.h"
+
+namespace pg {
+
+namespace {
+
+constexpr int kKmodThreads = 256;
+constexpr int kMaxSharedLimbs = 12288;  // 48 KiB
+
+template <bool kWide>
+__global__ void __launch_bounds__(kKmodThreads)
+    kmod_kernel(const uint32_t *__restrict__ klimbs, int nlimbs, uint64_t base,
+                const uint32_t *__restrict__ off, const unsigned long long *count,
+                uint64_t max_count, uint64_t mstart, uint32_t sl, void *r_out, void *t0_out) {
+    extern __shared__ uint32_t s_limbs[];
+    const bool in_shared = nlimbs <= kMaxSharedLimbs;
+    if (in_shared)
+        for (int i = threadIdx.x; i < nlimbs; i += blockDim.x) s_limbs[i] = klimbs[i];
+    __syncthreads();
+    const uint32_t *limbs = in_shared ? s_limbs : klimbs;
+    const uint64_t n = min((uint64_t)*count, max_count);  // never past the list's capacity
+    const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= n) return;
+    const uint64_t p = base + off[idx];
+    if (!kWide) {
+        uint32_t pinv, r2;
+        uint32_t r = kmod32(limbs, nlimbs, (uint32_t)p, pinv, r2);
+        ((uint32_t *)r_out)[idx] = r;
+        ((uint32_t *)t0_out)[idx] = start32(r, mstart, sl, (uint32_t)p, pinv, r2);
+    } else {
+        const uint64_t r = kmod64(limbs, nlimbs, p);
+        const double inv_p = 1.0 / (double)p;
+        uint64_t mm = mstart % p;
+        uint64_t t = mulmod_u64(r, mm, p, inv_p) + sl;
+        if (t >= p) t -= p;
+        ((uint64_t *)r_out)[idx] = r;
+        ((uint64_t *)t0_out)[idx] = t;
+    }
+}
+
+__global__ void __launch_bounds__(kKmodThreads)
+    kmod_list_kernel(const uint32_t *__restrict__ klimbs, int nlimbs, const uint32_t *q, uint32_t n,
+                     uint32_t *r) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    uint32_t pinv, r2;
+    r[i] = kmod32(klimbs, nlimbs, q[i], pinv, r2);
+}
+
+}  // namespace
+
+cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
+                        const unsigned long long *d_count, uint64_t max_count, uint64_t mstart,
+                        uint32_t sl, void *d_r, void *d_t0, bool wide, cudaStream_t stream) {
+    if (max_count == 0) return cudaSuccess;
+    uint64_t blocks = (max_count + kKmodThreads - 1) / kKmodThreads;
+    size_t smem = nlimbs <= kMaxSharedLimbs ? (size_t)nlimbs * sizeof(uint32_t) : 0;
+    if (wide)
+        kmod_kernel<true><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(
+            d_klimbs, nlimbs, base, d_off, d_count, max_count, mstart, sl, d_r, d_t0);
+    else
+        kmod_kernel<false><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(
+            d_klimbs, nlimbs, base, d_off, d_count, max_count, mstart, sl, d_r, d_t0);
+    return cudaGetLastError();
+}
+
+cudaError_t kmod_list32(const uint32_t *d_klimbs, int nlimbs, const uint32_t *d_q, uint32_t n,
+                        uint32_t *d_r, cudaStream_t stream) {
+    if (n == 0) return cudaSuccess;
+    kmod_list_kernel<<<(n + kKmodThreads - 1) / kKmodThreads, kKmodThreads, 0, stream>>>(
+        d_klimbs, nlimbs, d_q, n, d_r);
+    return cudaGetLastError();
+}
+
+}  // namespace pg

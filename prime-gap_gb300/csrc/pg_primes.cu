@@ -1,0 +1,348 @@
+// Prime generation: a segmented sieve of Eratosthenes over odd numbers.
+//
+// Replaces the reference's primesieve::iterator loops
+// (combined_sieve.cpp:1475-1502, 1662-1668, 1851-1852): every prime below
+// the sieve limit is produced on the device and stays resident in HBM.
+//
+// One CTA sieves one segment of kSegBits odd numbers in a 32 KiB shared
+// bitmap (bit set = composite):
+//   * base primes below 64 stamp a precomputed 32-bit pattern into every word;
+//   * base primes in [64, 2048) are marked warp-cooperatively;
+//   * larger base primes are marked one per thread;
+// then the block compacts its primes (offsets from the window start) into a
+// global list with one atomicAdd per block.  The list is unordered: every
+// consumer treats primes independently.
+#include "pg_internal.h"
+
+#include <cmath>
+
+namespace pg {
+
+namespace {
+
+constexpr int kSieveThreads = 512;
+constexpr uint32_t kSegWords = kSegBits / 32;
+__constant__ uint32_t c_tiny[17] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61};
+
+// bits at multiples of q inside a 32-bit word (q >= 32 -> bit 0 only)
+__device__ __forceinline__ uint32_t tiny_pattern(uint32_t q) {
+    uint32_t m = 0;
+    for (uint32_t b = 0; b < 32; b += q) m |= 1u << b;
+    return m;
+}
+
+// number of base primes q with q*q <= hi (base ascending)
+__device__ uint32_t base_bound(const uint32_t *base, uint32_t nbase, uint64_t hi) {
+    uint32_t lo = 0, up = nbase;
+    while (lo < up) {
+        uint32_t mid = (lo + up) >> 1;
+        uint64_t q = base[mid];
+        if (q * q <= hi) lo = mid + 1;
+        else up = mid;
+    }
+    return lo;
+}
+
+// Marks composites of the segment [seg_lo, seg_hi] (seg_lo odd) in `bits`.
+// Primes themselves stay clear; 1 is marked.
+__device__ void sieve_segment(uint32_t *bits, uint64_t seg_lo, uint64_t seg_hi,
+                              const uint32_t *base, uint32_t nbase) {
+    const uint32_t nbits = (uint32_t)((seg_hi - seg_lo) / 2 + 1);
+    __shared__ uint32_t s_nq;
+    __shared__ uint32_t s_j0[17];
+    if (threadIdx.x == 0) s_nq = base_bound(base, nbase, seg_hi);
+    if (threadIdx.x < 17) {
+        uint32_t q = c_tiny[threadIdx.x];
+        // index j with seg_lo + 2j == 0 (mod q): j = -seg_lo * (q+1)/2 mod q
+        uint32_t lm = (uint32_t)(seg_lo % q);
+        uint32_t neg = (q - lm) % q;
+        s_j0[threadIdx.x] = (uint32_t)((neg * ((q + 1) / 2)) % q);
+    }
+    __syncthreads();
+
+    // tiny primes: per-word patterns; this also initialises every word
+    for (uint32_t w = threadIdx.x; w < kSegWords; w += blockDim.x) {
+        uint32_t word = 0;
+#pragma unroll
+        for (int t = 0; t < 17; t++) {
+            uint32_t q = c_tiny[t];
+            uint32_t o = (s_j0[t] + q - (32u * w) % q) % q;
+            if (o < 32) word |= tiny_pattern(q) << o;
+        }
+        bits[w] = word;
+    }
+    __syncthreads();
+    if (threadIdx.x < 17) {
+        // the tiny primes themselves are prime
+        uint64_t q = c_tiny[threadIdx.x];
+        if (q >= seg_lo && q <= seg_hi) {
+            uint32_t j = (uint32_t)((q - seg_lo) / 2);
+            atomicAnd(&bits[j >> 5], ~(1u << (j & 31)));
+        }
+    }
+    if (threadIdx.x == 0 && seg_lo == 1) atomicOr(&bits[0], 1u);  // 1 is not prime
+    __syncthreads();
+
+    const uint32_t nq = s_nq;
+    // base primes are odd primes starting at 3; skip those below 64 (index of
+    // first prime >= 64 is 17, since 3..61 are the 17 odd primes below 64)
+    const uint32_t first_mid = 17;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    // medium primes: one warp per prime
+    for (uint32_t i = first_mid + warp; i < nq; i += nwarps) {
+        uint64_t q = base[i];
+        if (q >= 2048) break;
+        uint64_t start = q * q;
+        if (start < seg_lo) {
+            start = (seg_lo + q - 1) / q * q;
+            if ((start & 1) == 0) start += q;
+        }
+        if (start > seg_hi) continue;
+        for (uint64_t j = (start - seg_lo) / 2 + (uint64_t)lane * q; j < nbits; j += 32 * q)
+            atomicOr(&bits[j >> 5], 1u << (j & 31));
+    }
+    // large primes: one thread per prime
+    uint32_t first_large = first_mid;
+    {
+        // index of first base prime >= 2048 (binary search, cheap)
+        uint32_t lo = first_mid, up = nq;
+        while (lo < up) {
+            uint32_t mid = (lo + up) >> 1;
+            if (base[mid] < 2048) lo = mid + 1;
+            else up = mid;
+        }
+        first_large = lo;
+    }
+    for (uint32_t i = first_large + threadIdx.x; i < nq; i += blockDim.x) {
+        uint64_t q = base[i];
+        uint64_t start = q * q;
+        if (start < seg_lo) {
+            start = (seg_lo + q - 1) / q * q;
+            if ((start & 1) == 0) start += q;
+        }
+        for (uint64_t j = (start - seg_lo) / 2; j < nbits; j += q)
+            atomicOr(&bits[j >> 5], 1u << (j & 31));
+    }
+    __syncthreads();
+}
+
+// Unordered compaction of a window's primes (offsets from win_lo).
+__global__ void __launch_bounds__(kSieveThreads)
+    sieve_window_kernel(uint64_t win_lo, uint64_t win_hi, uint64_t first_odd, const uint32_t *base,
+                        uint32_t nbase, uint32_t *out, uint64_t cap,
+                        unsigned long long *count) {
+    __shared__ uint32_t bits[kSegWords];
+    __shared__ uint32_t s_scan[kSieveThreads];
+    __shared__ unsigned long long s_base;
+    const uint64_t seg_lo = first_odd + (uint64_t)blockIdx.x * kSegSpan;
+    if (seg_lo > win_hi) return;
+    uint64_t seg_hi = seg_lo + kSegSpan - 2;
+    if (seg_hi > win_hi) seg_hi = win_hi;
+    sieve_segment(bits, seg_lo, seg_hi, base, nbase);
+
+    const uint32_t nbits = (uint32_t)((seg_hi - seg_lo) / 2 + 1);
+    // each thread owns a contiguous range of words
+    const uint32_t per = kSegWords / kSieveThreads;
+    const uint32_t w0 = threadIdx.x * per;
+    uint32_t cnt = 0;
+    for (uint32_t w = w0; w < w0 + per; w++) {
+        uint32_t valid = 0;
+        uint32_t b0 = w * 32;
+        if (b0 < nbits) valid = (nbits - b0 >= 32) ? 0xFFFFFFFFu : ((1u << (nbits - b0)) - 1);
+        // exclude values below the window start (first segment of a window at 1)
+        uint32_t primes = ~bits[w] & valid;
+        cnt += __popc(primes);
+    }
+    s_scan[threadIdx.x] = cnt;
+    __syncthreads();
+    // block exclusive scan (Hillis-Steele on 512 entries)
+    for (int off = 1; off < kSieveThreads; off <<= 1) {
+        uint32_t v = threadIdx.x >= (uint32_t)off ? s_scan[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_scan[threadIdx.x] += v;
+        __syncthreads();
+    }
+    if (threadIdx.x == kSieveThreads - 1) s_base = atomicAdd(count, (unsigned long long)s_scan[kSieveThreads - 1]);
+    __syncthreads();
+    uint64_t pos = s_base + s_scan[threadIdx.x] - cnt;
+    for (uint32_t w = w0; w < w0 + per; w++) {
+        uint32_t b0 = w * 32;
+        if (b0 >= nbits) break;
+        uint32_t valid = (nbits - b0 >= 32) ? 0xFFFFFFFFu : ((1u << (nbits - b0)) - 1);
+        uint32_t primes = ~bits[w] & valid;
+        while (primes) {
+            uint32_t b = __ffs(primes) - 1;
+            primes &= primes - 1;
+            uint64_t v = seg_lo + 2ull * (b0 + b);
+            if (pos < cap) out[pos] = (uint32_t)(v - win_lo);
+            pos++;
+        }
+    }
+}
+
+// Ordered sieve of [3, hi] for base primes: bitmaps + per-segment counts.
+__global__ void __launch_bounds__(kSieveThreads)
+    sieve_bitmap_kernel(uint64_t hi, const uint32_t *base, uint32_t nbase, uint32_t *gbits,
+                        uint32_t *seg_counts) {
+    __shared__ uint32_t bits[kSegWords];
+    const uint64_t seg_lo = 1 + (uint64_t)blockIdx.x * kSegSpan;
+    uint64_t seg_hi = seg_lo + kSegSpan - 2;
+    if (seg_hi > hi) seg_hi = hi;
+    sieve_segment(bits, seg_lo, seg_hi, base, nbase);
+    const uint32_t nbits = (uint32_t)((seg_hi - seg_lo) / 2 + 1);
+    uint32_t cnt = 0;
+    for (uint32_t w = threadIdx.x; w < kSegWords; w += blockDim.x) {
+        uint32_t b0 = w * 32;
+        uint32_t valid = 0;
+        if (b0 < nbits) valid = (nbits - b0 >= 32) ? 0xFFFFFFFFu : ((1u << (nbits - b0)) - 1);
+        uint32_t primes = ~bits[w] & valid;
+        gbits[(uint64_t)blockIdx.x * kSegWords + w] = primes;
+        cnt += __popc(primes);
+    }
+    cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&seg_counts[blockIdx.x], cnt);
+}
+
+// Single CTA: ordered extraction of primes from bitmaps (values 1 + 2j).
+__global__ void __launch_bounds__(1024) ordered_extract_kernel(const uint32_t *gbits, uint64_t nwords,
+                                                               uint32_t *out, uint32_t *count) {
+    __shared__ uint32_t s_scan[1024];
+    __shared__ uint32_t s_total;
+    if (threadIdx.x == 0) s_total = 0;
+    __syncthreads();
+    for (uint64_t w0 = 0; w0 < nwords; w0 += 1024) {
+        uint64_t w = w0 + threadIdx.x;
+        uint32_t word = w < nwords ? gbits[w] : 0;
+        uint32_t c = __popc(word);
+        s_scan[threadIdx.x] = c;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {
+            uint32_t v = threadIdx.x >= (uint32_t)off ? s_scan[threadIdx.x - off] : 0;
+            __syncthreads();
+            s_scan[threadIdx.x] += v;
+            __syncthreads();
+        }
+        uint32_t pos = s_total + s_scan[threadIdx.x] - c;
+        // segment s, word k: values 1 + 2*(s*kSegBits + 32k + b) = 1 + 2*(32w + b)
+        while (word) {
+            uint32_t b = __ffs(word) - 1;
+            word &= word - 1;
+            out[pos++] = (uint32_t)(1 + 2 * (32 * w + b));
+        }
+        __syncthreads();
+        if (threadIdx.x == 1023) s_total += s_scan[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count = s_total;
+}
+
+// Odd primes below 2^16 by trial division against odd primes below 256.
+__global__ void __launch_bounds__(1024) small_primes_kernel(uint32_t *out, uint32_t *count) {
+    __shared__ uint32_t s_scan[1024];
+    __shared__ uint32_t s_total;
+    if (threadIdx.x == 0) s_total = 0;
+    __syncthreads();
+    for (uint32_t v0 = 3; v0 < 65536; v0 += 2048) {
+        uint32_t v = v0 + 2 * threadIdx.x;
+        bool prime = v < 65536;
+        for (uint32_t d = 3; prime && d * d <= v; d += 2)
+            if (v % d == 0) prime = false;
+        s_scan[threadIdx.x] = prime;
+        __syncthreads();
+        for (int off = 1; off < 1024; off <<= 1) {
+            uint32_t x = threadIdx.x >= (uint32_t)off ? s_scan[threadIdx.x - off] : 0;
+            __syncthreads();
+            s_scan[threadIdx.x] += x;
+            __syncthreads();
+        }
+        if (prime) out[s_total + s_scan[threadIdx.x] - 1] = v;
+        __syncthreads();
+        if (threadIdx.x == 1023) s_total += s_scan[1023];
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) *count = s_total;
+}
+
+uint64_t isqrt64(uint64_t n) {
+    uint64_t r = (uint64_t)std::sqrt((double)n);
+    while (r * r > n) r--;
+    while ((r + 1) * (r + 1) <= n) r++;
+    return r;
+}
+
+}  // namespace
+
+uint64_t prime_count_bound(uint64_t lo, uint64_t hi) {
+    if (hi < lo) return 0;
+    double y = (double)(hi - lo + 1);
+    if (y < 1e4) return (uint64_t)y / 2 + 64;
+    // pi(x + y) - pi(x) <= 2y / ln y  (Montgomery & Vaughan, 1973)
+    return (uint64_t)(2.0 * y / std::log(y)) + 1024;
+}
+
+cudaError_t base_primes_build(BasePrimes &bp, uint64_t limit, cudaStream_t stream) {
+    uint64_t need = isqrt64(limit) + 1;
+    if (bp.d_primes && bp.covers >= limit) return cudaSuccess;
+    base_primes_free(bp);
+    cudaError_t e;
+    // level 0: odd primes < 2^16
+    uint32_t *d_small = nullptr, *d_cnt = nullptr;
+    const uint32_t small_cap = 6600;
+    if ((e = cudaMalloc(&d_small, small_cap * sizeof(uint32_t)))) return e;
+    if ((e = cudaMalloc(&d_cnt, 2 * sizeof(uint32_t)))) return e;
+    small_primes_kernel<<<1, 1024, 0, stream>>>(d_small, d_cnt);
+    uint32_t nsmall = 0;
+    if ((e = cudaMemcpyAsync(&nsmall, d_cnt, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream))) return e;
+    if ((e = cudaStreamSynchronize(stream))) return e;
+    if (need < 65536) {
+        bp.d_primes = d_small;
+        bp.count = nsmall;
+        bp.covers = 65535ull * 65535ull;
+        cudaFree(d_cnt);
+        return cudaSuccess;
+    }
+    // level 1: odd primes in [3, need] from bitmaps sieved by level 0
+    uint64_t nseg = (need - 1) / kSegSpan + 1;
+    uint32_t *d_bits = nullptr, *d_segc = nullptr, *d_out = nullptr;
+    uint64_t cap = prime_count_bound(1, need) + 16;
+    if ((e = cudaMalloc(&d_bits, nseg * kSegWords * sizeof(uint32_t)))) return e;
+    if ((e = cudaMalloc(&d_segc, nseg * sizeof(uint32_t)))) return e;
+    if ((e = cudaMalloc(&d_out, cap * sizeof(uint32_t)))) return e;
+    cudaMemsetAsync(d_segc, 0, nseg * sizeof(uint32_t), stream);
+    sieve_bitmap_kernel<<<(unsigned)nseg, kSieveThreads, 0, stream>>>(need, d_small, nsmall, d_bits,
+                                                                      d_segc);
+    ordered_extract_kernel<<<1, 1024, 0, stream>>>(d_bits, nseg * kSegWords, d_out, d_cnt + 1);
+    uint32_t nout = 0;
+    if ((e = cudaMemcpyAsync(&nout, d_cnt + 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, stream))) return e;
+    if ((e = cudaStreamSynchronize(stream))) return e;
+    if ((e = cudaGetLastError())) return e;
+    cudaFree(d_bits);
+    cudaFree(d_segc);
+    cudaFree(d_small);
+    cudaFree(d_cnt);
+    bp.d_primes = d_out;
+    bp.count = nout;
+    bp.covers = need * need - 1;
+    return cudaSuccess;
+}
+
+void base_primes_free(BasePrimes &bp) {
+    if (bp.d_primes) cudaFree(bp.d_primes);
+    bp = BasePrimes{};
+}
+
+cudaError_t sieve_window(const BasePrimes &bp, uint64_t lo, uint64_t hi, uint32_t *d_out,
+                         uint64_t cap, unsigned long long *d_count, cudaStream_t stream) {
+    if (hi < lo) return cudaSuccess;
+    if (hi > bp.covers) return cudaErrorInvalidValue;
+    if (hi - lo >= (1ull << 32)) return cudaErrorInvalidValue;
+    uint64_t first_odd = lo | 1;
+    if (first_odd < 3) first_odd = 3;
+    if (first_odd > hi) return cudaSuccess;
+    uint64_t nseg = (hi - first_odd) / kSegSpan + 1;
+    sieve_window_kernel<<<(unsigned)nseg, kSieveThreads, 0, stream>>>(
+        lo, hi, first_odd, bp.d_primes, bp.count, d_out, cap, d_count);
+    return cudaGetLastError();
+}
+
+}  // namespace pg

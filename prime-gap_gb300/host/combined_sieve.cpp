@@ -1,0 +1,384 @@
+// combined_sieve -- drop-in replacement for the reference's combined_sieve
+// process (method2 path) running on one GB300 through libpgsieve.
+//
+// Same flags and unknowns-file name as the reference: Args::argparse
+// (gap_common.cpp:805-1099), Args::gen_unknown_fn (gap_common.cpp:732-749) and
+// main()'s validation (combined_sieve.cpp:74-157).  Writes the same bytes to
+// unknowns/<P>_<d>_<mstart>_<minc>_s<SL>_l<MP>M.txt and records the run in the
+// search database's `range` table like insert_range_db
+// (combined_sieve.cpp:347-380).  Exit codes: 0 ok, 1 invalid arguments or
+// failed run (the reference's exit(1)).
+//
+// --method1 produces the same bytes (the reference checks the two methods
+// against each other, misc/tests.sh:62-67) under the .m1.txt name.
+// Not carried over: the d optimizer for d % 4 == 0 and the automatic
+// sieve-length choice of set_defaults (combined_sieve.cpp:160-300).
+#include <dlfcn.h>
+#include <getopt.h>
+#include <libgen.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <string>
+
+#include "pgsieve.h"
+
+namespace {
+
+struct Config {
+    int valid = 1;
+    uint32_t p = 0, d = 0;
+    uint64_t mstart = 0, minc = 0, mskip = 0;
+    float min_merit = 18;
+    uint32_t sieve_length = 0;
+    uint64_t max_prime = 0;
+    bool save_unknowns = false, method1 = false, show_timing = true, testing = false;
+    int compression = 0, threads = 1, max_mem = 10, verbose = 2;
+    std::string unknown_filename;
+    std::string search_db = "prime-gap-search.db";
+    std::string gaps_db = "gaps.db";
+};
+
+bool file_exists(const std::string &path) {
+    std::ifstream f(path);
+    return f.good();
+}
+
+void require_file(const char *path) {
+    if (!file_exists(path)) {
+        printf("'%s' doesn't exist\n", path);
+        exit(1);
+    }
+}
+
+bool is_prime_brute(uint64_t n) {
+    if (n < 2) return false;
+    if (n % 2 == 0) return n == 2;
+    for (uint64_t t = 3; t * t <= n; t += 2)
+        if (n % t == 0) return false;
+    return true;
+}
+
+void show_usage(const char *name) {
+    printf("Usage: %s\n", name);
+    printf("[REQUIRED]\n  -p <p>\n  -d <p>\n  --mstart <start>\n  --minc   <int>\nOR\n");
+    printf("  -u, --unknown-filename <filename>\n");
+    printf("    parse p, d, mstart, minc, sieve-length, max-prime from filename\n\n");
+    printf("[OPTIONALLY]\n  -t, --threads N\n  --min-merit <min_merit>\n");
+    printf("  --sieve-length\n    how large the positive/negative sieve arrays should be\n");
+    printf("  --max-prime\n    use primes <= max-prime (in millions) for checking composite\n\n");
+    printf("  --save-unknowns\n  --rle\n  --bitcompress\n  --maxmem <max memory in GB>\n\n");
+    printf("[OPTIONAL]\n  --search-db\n  --prime-gaps-db\n\n  -q, --quiet\n  -h, --help\n\n");
+    printf("calculates prime_gaps for (mstart + mi) * p#/d, mi <= minc \n");
+}
+
+std::string gen_unknown_fn(const Config &c) {
+    if (!c.unknown_filename.empty()) return c.unknown_filename;
+    return "unknowns/" + std::to_string(c.p) + "_" + std::to_string(c.d) + "_" +
+           std::to_string(c.mstart) + "_" + std::to_string(c.minc) + "_s" +
+           std::to_string(c.sieve_length) + "_l" + std::to_string(c.max_prime / 1000000) + "M" +
+           (c.method1 ? ".m1" : "") + ".txt";
+}
+
+Config argparse(int argc, char **argv) {
+    static struct option long_options[] = {
+        {"p", required_argument, 0, 'p'},
+        {"d", required_argument, 0, 'd'},
+        {"mstart", required_argument, 0, 1},
+        {"minc", required_argument, 0, 2},
+        {"mskip", required_argument, 0, 16},
+        {"unknown-filename", required_argument, 0, 'u'},
+        {"sieve-length", required_argument, 0, 4},
+        {"max-prime", required_argument, 0, 5},
+        {"threads", required_argument, 0, 't'},
+        {"min-merit", required_argument, 0, 3},
+        {"save", no_argument, 0, 7},
+        {"save-unknowns", no_argument, 0, 7},
+        {"rle", no_argument, 0, 13},
+        {"bitcompressed", no_argument, 0, 15},
+        {"uncompressed", no_argument, 0, 17},
+        {"max-mem", required_argument, 0, 14},
+        {"search-db", required_argument, 0, 9},
+        {"prime-gaps-db", required_argument, 0, 10},
+        {"method1", no_argument, 0, 8},
+        {"hide-timing", no_argument, 0, 11},
+        {"testing", no_argument, 0, 12},
+        {"quiet", no_argument, 0, 'q'},
+        {"help", no_argument, 0, 'h'},
+        {0, 0, 0, 0}};
+    Config c;
+    int option_index = 0;
+    int ch;
+    while ((ch = getopt_long(argc, argv, "qhp:d:u:t:", long_options, &option_index)) >= 0) {
+        switch (ch) {
+            case 'h': show_usage(argv[0]); exit(0);
+            case 'q': c.verbose--; break;
+            case 'p': c.p = atoi(optarg); break;
+            case 'd': c.d = atoi(optarg); break;
+            case 1: c.mstart = atoll(optarg); break;
+            case 2: c.minc = atoll(optarg); break;
+            case 16: c.mskip = atoll(optarg); break;
+            case 'u': {
+                // <dir>/<P>_<d>_<mstart>_<minc>_s<SL>_l<MP>M[.m1].txt (gap_common.cpp:877-925)
+                std::string full = optarg;
+                char *t1 = strdup(optarg);
+                std::string dir = dirname(t1);
+                free(t1);
+                char *t2 = strdup(optarg);
+                std::string base = basename(t2);
+                free(t2);
+                dir = (dir == ".") ? "unknowns" : dir;
+                c.unknown_filename = dir + "/" + base;
+                unsigned us = 0;
+                for (char x : base) us += x == '_';
+                unsigned long long ms = 0, mi = 0, mp = 0;
+                unsigned p = 0, d = 0, sl = 0;
+                char tail[32] = {0};
+                if (us != 5 || sscanf(base.c_str(), "%u_%u_%llu_%llu_s%u_l%llu%31s", &p, &d, &ms,
+                                      &mi, &sl, &mp, tail) != 7 ||
+                    (strcmp(tail, "M.txt") != 0 && strcmp(tail, "M.m1.txt") != 0)) {
+                    printf("can't parse unknown filename '%s'\n", base.c_str());
+                    exit(1);
+                }
+                c.p = p;
+                c.d = d;
+                c.mstart = ms;
+                c.minc = mi;
+                c.sieve_length = sl;
+                c.max_prime = mp * 1000000ull;
+                c.method1 = strcmp(tail, "M.m1.txt") == 0;
+                break;
+            }
+            case 't': c.threads = atoi(optarg); break;
+            case 3: c.min_merit = atof(optarg); break;
+            case 4: c.sieve_length = atoi(optarg); break;
+            case 5: c.max_prime = atol(optarg) * 1000000ull; break;
+            case 7: c.save_unknowns = true; break;
+            case 8: c.method1 = true; break;
+            case 9: c.search_db = optarg; require_file(optarg); break;
+            case 10: c.gaps_db = optarg; require_file(optarg); break;
+            case 11: c.show_timing = false; break;
+            case 12: c.testing = true; break;
+            case 13: c.compression = 1; break;
+            case 15: c.compression = 2; break;
+            case 17: c.compression = 3; break;
+            case 14: c.max_mem = atol(optarg); break;
+            default: c.valid = 0;
+        }
+    }
+    if (optind < argc) {
+        c.valid = 0;
+        printf("unknown positional argument: ");
+        while (optind < argc) printf("%s ", argv[optind++]);
+        printf("\n");
+    }
+    if (c.testing) c.save_unknowns = false;
+    // validation (gap_common.cpp:1007-1094)
+    if (c.mstart <= 0) {
+        c.valid = 0;
+        printf("mstart must be greater than 0: %llu\n", (unsigned long long)c.mstart);
+    }
+    int64_t last_m = (int64_t)(c.mstart + c.minc);
+    if (last_m <= 0 || last_m > 10000000001LL) {
+        c.valid = 0;
+        printf("mstart + minc must be <= 10e9\n");
+    }
+    if (c.minc <= 0) {
+        c.valid = 0;
+        printf("minc must be greater than 0: %llu\n", (unsigned long long)c.minc);
+    }
+    if (c.minc >= 0x7FFFFFFFull) {
+        c.valid = 0;
+        printf("minc must be less than 2B %llu\n", (unsigned long long)c.minc);
+    }
+    if (c.max_prime > 40000000000000ull) {
+        c.valid = 0;
+        printf("max_prime > 40 Trillion not supported\n");
+    }
+    if (c.method1 && c.max_prime) {
+        uint64_t max_m = UINT64_MAX / c.max_prime;
+        if (max_m < 1000 || (max_m + 1000) <= (uint64_t)last_m) {
+            c.valid = 0;
+            printf("max_prime * last_m(%lld) would overflow int64\n", (long long)last_m);
+        }
+    }
+    if (!(c.p < 10000000u && (c.p < 4 || is_prime_brute(c.p)))) {
+        printf("p# not prime (p=%u)\n", c.p);
+        exit(1);
+    }
+    if (c.sieve_length % 500 != 0) {
+        for (uint32_t q = 2; q < c.p; q += 1 + (q > 2)) {
+            if (is_prime_brute(q) && c.sieve_length % q == 0 && c.d % q != 0) {
+                c.valid = 0;
+                printf("SL=%u not coprime (p=%u)\n", c.sieve_length, q);
+            }
+        }
+    }
+    if (c.d <= 0) {
+        c.valid = 0;
+        printf("d must be greater than 0: %u\n", c.d);
+    }
+    if (c.threads <= 0 || c.threads > 16) {
+        c.valid = 0;
+        printf("invalid number of threads(%d) only 1 - 16 supported\n", c.threads);
+    }
+    if (c.valid == 0) printf("\n");
+    return c;
+}
+
+// config hash used as the range id (gap_common.cpp:1112-1121)
+uint64_t config_hash(const Config &c) {
+    uint64_t hash = c.mstart;
+    hash = hash * 31 + c.minc;
+    hash = hash * 31 + c.p;
+    hash = hash * 31 + c.d;
+    hash = hash * 31 + c.sieve_length;
+    hash = hash * 31 + c.max_prime;
+    return hash;
+}
+
+// insert_range_db (combined_sieve.cpp:347-380) through the system sqlite3.
+int insert_range_db(const Config &c, long num_rows, float time_sieve) {
+    require_file(c.search_db.c_str());
+    void *h = dlopen("libsqlite3.so.0", RTLD_NOW);
+    if (!h) {
+        printf("\nrange INSERT failed: libsqlite3.so.0 not available\n");
+        return 1;
+    }
+    typedef int (*open_t)(const char *, void **);
+    typedef int (*close_t)(void *);
+    typedef const char *(*errmsg_t)(void *);
+    typedef int (*exec_t)(void *, const char *, void *, void *, char **);
+    auto s_open = (open_t)dlsym(h, "sqlite3_open");
+    auto s_close = (close_t)dlsym(h, "sqlite3_close");
+    auto s_errmsg = (errmsg_t)dlsym(h, "sqlite3_errmsg");
+    auto s_exec = (exec_t)dlsym(h, "sqlite3_exec");
+    if (!s_open || !s_close || !s_errmsg || !s_exec) return 1;
+    void *db = nullptr;
+    if (s_open(c.search_db.c_str(), &db) != 0) {
+        printf("Can't open database(%s): %s\n", c.search_db.c_str(), s_errmsg(db));
+        return 1;
+    }
+    char sql[400];
+    snprintf(sql, sizeof sql,
+             "INSERT INTO range(rid, P,D, m_start,m_inc,sieve_length, max_prime,min_merit,num_m,"
+             "time_sieve)VALUES(%ld,  %d,%d, %ld,%ld,%d,%ld, %.3f,%ld,  %.2f)"
+             "ON CONFLICT(rid) DO UPDATE SET time_sieve=%.2f",
+             (long)config_hash(c), (int)c.p, (int)c.d, (long)c.mstart, (long)c.minc,
+             (int)c.sieve_length, (long)c.max_prime, c.min_merit, num_rows, time_sieve, time_sieve);
+    char *zerr = nullptr;
+    int rc = s_exec(db, sql, nullptr, nullptr, &zerr);
+    if (rc != 0) {
+        printf("\nrange INSERT failed %d: %s\n", rc, s_errmsg(db));
+        s_close(db);
+        return 1;
+    }
+    s_close(db);
+    return 0;
+}
+
+}  // namespace
+
+int main(int argc, char **argv) {
+    Config c = argparse(argc, argv);
+    if (c.valid == 0) {
+        show_usage(argv[0]);
+        return 1;
+    }
+    // set_defaults (combined_sieve.cpp:160-344)
+    if (c.d % 4 == 0) {
+        printf("d optimizer (d %% 4 == 0) is not part of this build\n");
+        return 1;
+    }
+    if (c.sieve_length == 0) {
+        printf("--sieve-length must be given (automatic choice is not part of this build)\n");
+        return 1;
+    }
+    if (c.max_prime == 0) {
+        pgs_job probe{c.p, c.d, c.mstart, c.minc, c.sieve_length, 10000000000ull, 0, 0};
+        pgs_plan plan;
+        pgs_plan_job(&probe, &plan);
+        double k_log = plan.k_bits * std::log(2.0);
+        c.max_prime = k_log >= 1500 ? 100000000000ull : 10000000000ull;
+        if (c.method1) {
+            printf("Can't use method1 and not set max_prime");
+            return 1;
+        }
+        if (c.verbose >= 0)
+            printf("AUTO SET: max_prime (log(K) = ~%.0f): %llu\n", k_log,
+                   (unsigned long long)c.max_prime);
+    }
+    // main()'s checks (combined_sieve.cpp:86-135)
+    if (!c.save_unknowns && !c.testing) {
+        printf("Must set --save-unknowns\n");
+        return 1;
+    }
+    if (c.sieve_length < 6 * c.p || c.sieve_length > 22 * c.p) {
+        int sl_min = ((c.p * 8 - 1) / 500 + 1) * 500;
+        int sl_max = ((c.p * 20 - 1) / 500 + 1) * 500;
+        printf("--sieve_length(%d) should be between [%d, %d]\n", c.sieve_length, sl_min, sl_max);
+        return 1;
+    }
+    const std::string fn = gen_unknown_fn(c);
+    if (c.save_unknowns && file_exists(fn)) {
+        printf("\nOutput file '%s' already exists\n", fn.c_str());
+        return 1;
+    }
+    if (!c.compression && (c.minc * c.sieve_length) > 100000000000ull) {
+        printf("\tSetting --bitcompress to prevent very large output file\n");
+        c.compression = 2;
+    }
+    if (!c.compression && (c.minc * c.sieve_length) > 30000000000ull) {
+        printf("\tSetting --rle to prevent very large output file\n");
+        c.compression = 1;
+    }
+    if (c.verbose >= 0) {
+        printf("\n");
+        printf("Testing m * %u#/%u, m = %llu + [0, %llu)\n", c.p, c.d, (unsigned long long)c.mstart,
+               (unsigned long long)c.minc);
+    }
+
+    auto t0 = std::chrono::steady_clock::now();
+    pgs_ctx *ctx = nullptr;
+    int rc = pgs_create(0, &ctx);
+    if (rc != PGS_OK) {
+        printf("no CUDA device available (%d)\n", rc);
+        return 1;
+    }
+    pgs_job job{c.p, c.d, c.mstart, c.minc, c.sieve_length, c.max_prime,
+                c.compression == 3 ? 0 : c.compression, 0};
+    pgs_result res;
+    rc = pgs_method2(ctx, &job, &res);
+    if (rc != PGS_OK) {
+        printf("combined_sieve failed (%d): %s\n", rc, pgs_last_error(ctx));
+        pgs_destroy(ctx);
+        return 1;
+    }
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    if (c.verbose >= 1) {
+        printf("sieve_length:  2x %u\n", c.sieve_length);
+        printf("max_prime:        %llu\n", (unsigned long long)c.max_prime);
+        printf("primes sieved:    %llu\n", (unsigned long long)res.primes);
+        printf("device time:      %.2f ms\n", res.ms_total);
+    }
+    int exit_code = 0;
+    if (c.save_unknowns) {
+        printf("\nSaving unknowns to '%s'\n", fn.c_str());
+        FILE *f = fopen(fn.c_str(), "wb");
+        if (!f) {
+            printf("can't open '%s'\n", fn.c_str());
+            exit_code = 1;
+        } else {
+            size_t w = fwrite(res.text, 1, res.text_len, f);
+            if (fclose(f) != 0 || w != res.text_len) exit_code = 1;
+        }
+        if (!exit_code) exit_code = insert_range_db(c, (long)res.rows, (float)(c.threads * secs));
+    }
+    pgs_result_free(&res);
+    pgs_destroy(ctx);
+    return exit_code;
+}

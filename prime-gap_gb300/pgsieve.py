@@ -1,0 +1,315 @@
+"""ctypes binding of libpgsieve (C ABI declared in include/pgsieve.h).
+
+Mirrors the reference's method2 entry point prime_gap_parallel
+(combined_sieve.cpp:2014) as ``Sieve.method2(job) -> bytes`` (the unknowns
+file contents) plus the number-theory primitives the sieve is built from.
+The CUDA library is required: loading fails loudly when it is missing.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+from dataclasses import dataclass
+from pathlib import Path
+
+PKG = Path(__file__).resolve().parent
+LIB_PATH = Path(os.environ.get("PGSIEVE_LIB", PKG / "_build" / "libpgsieve.so"))
+HEADER = PKG.parent / "include" / "pgsieve.h"
+
+PGS_OK = 0
+PGS_EINVAL = -1
+PGS_ENOMEM = -2
+PGS_ECUDA = -3
+PGS_EABORT = -4
+PGS_ENODEV = -5
+PGS_ETIMEOUT = -6
+
+STAGES = ["setup", "primes", "kmod", "large", "rows", "text", "d2h", "spare"]
+
+
+class PgsError(RuntimeError):
+    def __init__(self, code: int, msg: str = ""):
+        super().__init__(f"pgsieve error {code}: {msg}")
+        self.code = code
+
+
+class Job(ctypes.Structure):
+    _fields_ = [
+        ("p", ctypes.c_uint32),
+        ("d", ctypes.c_uint32),
+        ("mstart", ctypes.c_uint64),
+        ("minc", ctypes.c_uint64),
+        ("sieve_length", ctypes.c_uint32),
+        ("max_prime", ctypes.c_uint64),
+        ("compression", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
+    ]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [
+        ("text", ctypes.POINTER(ctypes.c_char)),
+        ("text_len", ctypes.c_uint64),
+        ("rows", ctypes.c_uint64),
+        ("primes", ctypes.c_uint64),
+        ("prime_limit", ctypes.c_uint64),
+        ("unknowns", ctypes.c_uint64),
+        ("ms_total", ctypes.c_double),
+        ("ms_stage", ctypes.c_double * 8),
+        ("launches", ctypes.c_uint64),
+        ("internal", ctypes.c_void_p),
+    ]
+
+
+class Plan(ctypes.Structure):
+    _fields_ = [
+        ("valid_ms", ctypes.c_uint64),
+        ("coprime_x", ctypes.c_uint64),
+        ("small_threshold", ctypes.c_uint64),
+        ("medium_threshold", ctypes.c_uint64),
+        ("prime_limit", ctypes.c_uint64),
+        ("k_bits", ctypes.c_uint32),
+        ("filename", ctypes.c_char * 256),
+    ]
+
+
+@dataclass
+class JobSpec:
+    """Config fields of one method2 job; max_prime is absolute."""
+
+    p: int
+    d: int
+    mstart: int
+    minc: int
+    sieve_length: int
+    max_prime: int
+    compression: int = 0
+
+    def c(self) -> Job:
+        return Job(self.p, self.d, self.mstart, self.minc, self.sieve_length, self.max_prime,
+                   self.compression, 0)
+
+    @property
+    def filename(self) -> str:
+        """Args::gen_unknown_fn (gap_common.cpp:732-749)."""
+        return (f"{self.p}_{self.d}_{self.mstart}_{self.minc}_s{self.sieve_length}"
+                f"_l{self.max_prime // 1_000_000}M.txt")
+
+
+_u64p = ctypes.POINTER(ctypes.c_uint64)
+_u32p = ctypes.POINTER(ctypes.c_uint32)
+
+_SIGNATURES = {
+    "pgs_version": (ctypes.c_char_p, []),
+    "pgs_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]),
+    "pgs_destroy": (None, [ctypes.c_void_p]),
+    "pgs_last_error": (ctypes.c_char_p, [ctypes.c_void_p]),
+    "pgs_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    "pgs_get_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
+    "pgs_method2": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.POINTER(Result)]),
+    "pgs_result_free": (None, [ctypes.POINTER(Result)]),
+    "pgs_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_void_p)]),
+    "pgs_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
+    "pgs_fetch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Result)]),
+    "pgs_prepared_free": (None, [ctypes.c_void_p]),
+    "pgs_plan_job": (ctypes.c_int, [ctypes.POINTER(Job), ctypes.POINTER(Plan)]),
+    "pgs_stage_ms": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double),
+                                    ctypes.POINTER(ctypes.c_double)]),
+    "pgs_int_peak": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]),
+    "pgs_primes": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64, _u64p,
+                                  ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "pgs_k_mod_p": (ctypes.c_int, [ctypes.c_void_p, _u32p, ctypes.c_int, _u64p, ctypes.c_size_t, _u64p]),
+    "pgs_modulo_search": (ctypes.c_int, [ctypes.c_void_p, _u64p, _u64p, _u64p, _u64p, _u64p,
+                                         ctypes.c_size_t]),
+    "pgs_large_hits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                      ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _u32p,
+                                      _u64p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+}
+
+_lib: ctypes.CDLL | None = None
+
+
+def load(path: str | os.PathLike | None = None) -> ctypes.CDLL:
+    """Load libpgsieve.so (built by prime-gap_gb300/build.py)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(f"libpgsieve not built: {p} (run prime-gap_gb300/build.py)")
+    lib = ctypes.CDLL(str(p))
+    for name, (res, args) in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def header_symbols() -> list[str]:
+    """Function names declared in include/pgsieve.h."""
+    import re
+
+    text = HEADER.read_text()
+    return sorted(set(re.findall(r"^\s*(?:[\w\s\*]+?)\b(pgs_\w+)\s*\(", text, re.M)))
+
+
+def plan(job: JobSpec) -> dict:
+    lib = load()
+    pl = Plan()
+    rc = lib.pgs_plan_job(ctypes.byref(job.c()), ctypes.byref(pl))
+    return {
+        "rc": rc,
+        "valid_ms": pl.valid_ms,
+        "coprime_x": pl.coprime_x,
+        "small_threshold": pl.small_threshold,
+        "medium_threshold": pl.medium_threshold,
+        "prime_limit": pl.prime_limit,
+        "k_bits": pl.k_bits,
+        "filename": pl.filename.decode(),
+    }
+
+
+def _arr(ctype, values):
+    a = (ctype * max(1, len(values)))()
+    for i, v in enumerate(values):
+        a[i] = v
+    return a
+
+
+class Sieve:
+    """One library context on a CUDA device."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = ctypes.c_void_p()
+        rc = self.lib.pgs_create(device, ctypes.byref(h))
+        if rc != PGS_OK:
+            raise PgsError(rc, "pgs_create failed (no usable CUDA device?)")
+        self.h = h
+
+    def close(self) -> None:
+        if self.h:
+            self.lib.pgs_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int) -> None:
+        if rc != PGS_OK:
+            raise PgsError(rc, self.lib.pgs_last_error(self.h).decode(errors="replace"))
+
+    @property
+    def stream(self) -> int:
+        return self.lib.pgs_get_stream(self.h) or 0
+
+    def set_stream(self, stream_ptr: int | None) -> None:
+        self._check(self.lib.pgs_set_stream(self.h, stream_ptr))
+
+    def method2(self, job: JobSpec, stats: dict | None = None) -> bytes:
+        """Unknowns file bytes for one job (prime_gap_parallel + save)."""
+        res = Result()
+        self._check(self.lib.pgs_method2(self.h, ctypes.byref(job.c()), ctypes.byref(res)))
+        try:
+            data = ctypes.string_at(res.text, res.text_len)
+            if stats is not None:
+                stats.update(_result_stats(res))
+        finally:
+            self.lib.pgs_result_free(ctypes.byref(res))
+        return data
+
+    def prepare(self, job: JobSpec) -> "Prepared":
+        h = ctypes.c_void_p()
+        self._check(self.lib.pgs_prepare(self.h, ctypes.byref(job.c()), ctypes.byref(h)))
+        return Prepared(self, h)
+
+    def int_peak(self) -> float:
+        """Measured 32-bit IMAD issue rate (per second)."""
+        v = ctypes.c_double()
+        self._check(self.lib.pgs_int_peak(self.h, ctypes.byref(v)))
+        return v.value
+
+    def primes(self, lo: int, hi: int) -> list[int]:
+        n = ctypes.c_size_t()
+        self._check(self.lib.pgs_primes(self.h, lo, hi, None, 0, ctypes.byref(n)))
+        out = (ctypes.c_uint64 * max(1, n.value))()
+        self._check(self.lib.pgs_primes(self.h, lo, hi, out, n.value, ctypes.byref(n)))
+        return list(out[: n.value])
+
+    def k_mod_p(self, limbs: list[int], q: list[int]) -> list[int]:
+        out = (ctypes.c_uint64 * max(1, len(q)))()
+        self._check(self.lib.pgs_k_mod_p(self.h, _arr(ctypes.c_uint32, limbs), len(limbs),
+                                         _arr(ctypes.c_uint64, q), len(q), out))
+        return list(out[: len(q)])
+
+    def modulo_search(self, p, a, l, r) -> list[int]:
+        n = len(p)
+        out = (ctypes.c_uint64 * max(1, n))()
+        self._check(self.lib.pgs_modulo_search(self.h, _arr(ctypes.c_uint64, p), _arr(ctypes.c_uint64, a),
+                                               _arr(ctypes.c_uint64, l), _arr(ctypes.c_uint64, r), out, n))
+        return list(out[:n])
+
+    def large_hits(self, M: int, max_mi: int, SL: int, prime: int, base_r: int,
+                   cap: int = 1 << 20) -> list[tuple[int, int]]:
+        mi = (ctypes.c_uint32 * cap)()
+        md = (ctypes.c_uint64 * cap)()
+        n = ctypes.c_size_t()
+        self._check(self.lib.pgs_large_hits(self.h, M, max_mi, SL, prime, base_r, mi, md, cap,
+                                            ctypes.byref(n)))
+        k = min(n.value, cap)
+        return list(zip(mi[:k], md[:k]))
+
+
+class Prepared:
+    """A job whose tables are resident on the device (pgs_prepare)."""
+
+    def __init__(self, sieve: Sieve, h: ctypes.c_void_p):
+        self.sieve, self.h = sieve, h
+
+    def run(self, record_stages: bool = True) -> None:
+        self.sieve._check(self.sieve.lib.pgs_run(self.sieve.h, self.h, int(record_stages)))
+
+    def stage_ms(self) -> tuple[dict, float]:
+        out = (ctypes.c_double * 8)()
+        tot = ctypes.c_double()
+        self.sieve._check(self.sieve.lib.pgs_stage_ms(self.sieve.h, self.h, out, ctypes.byref(tot)))
+        return {STAGES[i]: out[i] for i in range(8)}, tot.value
+
+    def fetch(self, stats: dict | None = None) -> bytes:
+        res = Result()
+        self.sieve._check(self.sieve.lib.pgs_fetch(self.sieve.h, self.h, ctypes.byref(res)))
+        try:
+            data = ctypes.string_at(res.text, res.text_len)
+            if stats is not None:
+                stats.update(_result_stats(res))
+        finally:
+            self.sieve.lib.pgs_result_free(ctypes.byref(res))
+        return data
+
+    def close(self) -> None:
+        if self.h:
+            self.sieve.lib.pgs_prepared_free(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+def _result_stats(res: Result) -> dict:
+    return {
+        "text_len": res.text_len,
+        "rows": res.rows,
+        "primes": res.primes,
+        "prime_limit": res.prime_limit,
+        "ms_total": res.ms_total,
+        "ms_stage": {STAGES[i]: res.ms_stage[i] for i in range(8)},
+        "launches": res.launches,
+    }

@@ -1,0 +1,81 @@
+// Host build of the device arithmetic (prime-gap_gb300/csrc/pg_arith.cuh) for
+// CPU unit tests: the exact functions the kernels run, compiled by g++.
+#include <cstddef>
+#include <cstdint>
+
+#include "pg_arith.cuh"
+
+extern "C" {
+
+uint64_t ah_modsearch(uint64_t p, uint64_t a, uint64_t l, uint64_t r, uint64_t *v) {
+    pg::ModSearch64 s = pg::modsearch64(p, a, l, r);
+    if (v) *v = s.v;
+    return s.k;
+}
+
+void ah_three_gap(uint64_t p, uint64_t a, uint64_t w, uint64_t *out4) {
+    if (p < 0xFFFFFFFFull) {
+        pg::ThreeGap<uint32_t> g = pg::three_gap<uint32_t>((uint32_t)p, (uint32_t)a, (uint32_t)w);
+        out4[0] = g.kp, out4[1] = g.up, out4[2] = g.kn, out4[3] = g.dn;
+    } else {
+        pg::ThreeGap<uint64_t> g = pg::three_gap<uint64_t>(p, a, w);
+        out4[0] = g.kp, out4[1] = g.up, out4[2] = g.kn, out4[3] = g.dn;
+    }
+}
+
+struct Collect {
+    uint32_t *mi_out;
+    uint64_t *mod_out;
+    size_t cap, n;
+    void operator()(uint64_t mi, uint64_t y) {
+        if (n < cap) mi_out[n] = (uint32_t)mi, mod_out[n] = y;
+        n++;
+    }
+};
+
+// Hits of one prime over [0, max_mi), split into chunks of chunk_len values of
+// mi the way the large-prime kernel splits them (chunk_len 0 = one chunk).
+size_t ah_hits(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint64_t r,
+               uint32_t chunk_len, uint32_t *mi_out, uint64_t *mod_out, size_t cap) {
+    Collect c{mi_out, mod_out, cap, 0};
+    if (chunk_len == 0) chunk_len = max_mi;
+    if (p < 0xFFFFFFFFull) {
+        uint32_t pinv, r2;
+        uint32_t p32 = (uint32_t)p, r32 = (uint32_t)r;
+        (void)pinv, (void)r2;
+        uint32_t t0 = (uint32_t)((((M % p32) * (uint64_t)r32) % p32 + SL) % p32);
+        for (uint64_t lo = 0; lo < max_mi; lo += chunk_len) {
+            uint64_t hi = lo + chunk_len < max_mi ? lo + chunk_len : max_mi;
+            uint32_t y = pg::advance_residue(t0, lo, r32, p32);
+            pg::enumerate_hits<uint32_t>(p32, r32, y, lo, hi, 2 * SL, c);
+        }
+    } else {
+        uint64_t t0 = pg::mulmod_u64(M % p, r, p, 1.0 / (double)p) + SL;
+        if (t0 >= p) t0 -= p;
+        for (uint64_t lo = 0; lo < max_mi; lo += chunk_len) {
+            uint64_t hi = lo + chunk_len < max_mi ? lo + chunk_len : max_mi;
+            uint64_t y = pg::advance_residue(t0, lo, r, p);
+            pg::enumerate_hits<uint64_t>(p, r, y, lo, hi, 2ull * SL, c);
+        }
+    }
+    return c.n;
+}
+
+uint64_t ah_kmod(const uint32_t *limbs, int n, uint64_t q) {
+    if (q < 0x80000000ull) {
+        uint32_t pinv, r2;
+        return pg::kmod32(limbs, n, (uint32_t)q, pinv, r2);
+    }
+    return pg::kmod64(limbs, n, q);
+}
+
+// (r * M + sl) mod p through the Montgomery path of the K mod p kernel.
+uint32_t ah_start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p) {
+    uint32_t pinv = pg::neg_inv32(p);
+    uint32_t r1 = (0u - p) % p;
+    uint32_t r2 = (uint32_t)(((uint64_t)r1 * r1) % p);
+    return pg::start32(r, M, sl, p, pinv, r2);
+}
+
+uint64_t ah_mulmod(uint64_t a, uint64_t b, uint64_t p) { return pg::mulmod_u64(a, b, p, 1.0 / (double)p); }
+}

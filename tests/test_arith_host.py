@@ -1,0 +1,163 @@
+"""The device arithmetic (pg_arith.cuh), compiled for the host, against the oracle.
+
+These are the exact functions the kernels run: the Euclid modulo search with
+residue-tracking unwinding, the three-gap return structure, the chunked hit
+enumeration that replaces modulo_search_euclid_all_large
+(modulo_search.cpp:339-376), and the Montgomery K mod p.
+"""
+from __future__ import annotations
+
+import ctypes
+import random
+
+import pytest
+
+import pgo
+
+_lib = None
+
+
+@pytest.fixture(scope="module")
+def ah(built):
+    import build as pkg_build
+
+    lib = ctypes.CDLL(str(pkg_build.ARITH_HOST_LIB))
+    u64 = ctypes.c_uint64
+    lib.ah_modsearch.restype = u64
+    lib.ah_modsearch.argtypes = [u64, u64, u64, u64, ctypes.POINTER(u64)]
+    lib.ah_three_gap.restype = None
+    lib.ah_three_gap.argtypes = [u64, u64, u64, ctypes.POINTER(u64)]
+    lib.ah_hits.restype = ctypes.c_size_t
+    lib.ah_hits.argtypes = [u64, ctypes.c_uint32, ctypes.c_uint32, u64, u64, ctypes.c_uint32,
+                            ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
+    lib.ah_kmod.restype = u64
+    lib.ah_kmod.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int, u64]
+    lib.ah_start32.restype = ctypes.c_uint32
+    lib.ah_start32.argtypes = [ctypes.c_uint32, u64, ctypes.c_uint32, ctypes.c_uint32]
+    lib.ah_mulmod.restype = u64
+    lib.ah_mulmod.argtypes = [u64, u64, u64]
+    return lib
+
+
+def _hits(ah, M, max_mi, SL, p, r, chunk=0, cap=1 << 18):
+    mi = (ctypes.c_uint32 * cap)()
+    md = (ctypes.c_uint64 * cap)()
+    n = ah.ah_hits(M, max_mi, SL, p, r, chunk, mi, md, cap)
+    assert n <= cap
+    return list(zip(mi[:n], md[:n]))
+
+
+def _rand_prime(rng, lo, hi):
+    import sympy
+
+    return sympy.randprime(lo, hi)
+
+
+def test_modsearch_known_answers(ah):
+    v = ctypes.c_uint64()
+    assert ah.ah_modsearch(10**9 + 7, 123, 615, 621, ctypes.byref(v)) == 5
+    assert v.value == 615
+    assert ah.ah_modsearch(10**9 + 7, 123, 609, 615, ctypes.byref(v)) == 5
+
+
+@pytest.mark.parametrize("bits", [20, 31, 32, 34, 40, 45])
+def test_modsearch_vs_oracle(ah, bits):
+    rng = random.Random(bits)
+    v = ctypes.c_uint64()
+    for _ in range(300):
+        p = _rand_prime(rng, 2 ** (bits - 1), 2**bits)
+        a = rng.randrange(1, p)
+        width = rng.choice([0, 1, 5, 1000, 80000, p // 7])
+        width = min(width, p - 2)
+        l = rng.randrange(1, p - width)
+        r = l + width
+        k = ah.ah_modsearch(p, a, l, r, ctypes.byref(v))
+        assert k == pgo.modulo_search(p, a, l, r)
+        assert v.value == (k * a) % p
+        assert l <= v.value <= r
+
+
+def test_three_gap_brute(ah):
+    rng = random.Random(7)
+    out = (ctypes.c_uint64 * 4)()
+    for _ in range(200):
+        p = _rand_prime(rng, 1000, 200000)
+        w = rng.randrange(2, p // 2 - 1)
+        a = rng.randrange(1, p)
+        ah.ah_three_gap(p, a, w, out)
+        kp, up, kn, dn = list(out)
+        # kp / kn: smallest k with k*a mod p in (0, w) / (p - w, p)
+        k_up = next(k for k in range(1, p) if 0 < (k * a) % p < w)
+        k_dn = next(k for k in range(1, p) if p - w < (k * a) % p < p)
+        assert (kp, up) == (k_up, (k_up * a) % p)
+        assert (kn, dn) == (k_dn, p - (k_dn * a) % p)
+        assert up + dn >= w
+
+
+@pytest.mark.parametrize("bits,chunk", [(18, 0), (18, 777), (24, 0), (24, 3000), (31, 0),
+                                        (32, 0), (33, 0), (33, 50000), (36, 0), (40, 0)])
+def test_hits_vs_all_large(ah, bits, chunk):
+    """Every hit of modulo_search_euclid_all_large, in order, chunked or not."""
+    rng = random.Random(bits * 1000 + chunk)
+    for _ in range(60):
+        SL = rng.choice([500, 4000, 20000, 40000])
+        lo = max(4 * SL + 3, 2 ** (bits - 1))
+        p = _rand_prime(rng, lo, max(2 * lo, 2**bits))
+        r = rng.randrange(1, p)
+        M = rng.randrange(1, 10**10)
+        max_mi = rng.choice([1, 17, 1000, 100000])
+        got = _hits(ah, M, max_mi, SL, p, r, chunk)
+        want = pgo.all_large(M, max_mi, SL, p, r)
+        assert got == want
+
+
+def test_hits_dense_small_prime(ah):
+    """p just above 4*SL+2: many hits per prime, exercising all three gaps."""
+    rng = random.Random(3)
+    for _ in range(20):
+        SL = rng.choice([5000, 11000])
+        p = _rand_prime(rng, 4 * SL + 3, 4 * SL + 2000)
+        r = rng.randrange(1, p)
+        M = rng.randrange(1, 10**9)
+        got = _hits(ah, M, 50000, SL, p, r, 4096)
+        assert got == pgo.all_large(M, 50000, SL, p, r)
+
+
+@pytest.mark.parametrize("P,d", [(503, 210), (907, 2190), (1511, 2190), (3001, 2190), (953, 1)])
+def test_kmod_vs_oracle(ah, P, d):
+    limbs = pgo.build_k(P, d)
+    arr = (ctypes.c_uint32 * len(limbs))(*limbs)
+    rng = random.Random(P)
+    qs = pgo.primes(P + 1, P + 3000)[:50]
+    qs += [_rand_prime(rng, 2**30, 2**31) for _ in range(20)]
+    qs += [_rand_prime(rng, 2**31, 2**32) for _ in range(20)]
+    qs += [_rand_prime(rng, 2**32, 2**45) for _ in range(40)]
+    for q in qs:
+        assert ah.ah_kmod(arr, len(limbs), q) == pgo.k_mod(limbs, q)
+
+
+def test_kmod_against_python_bignum(built):
+    from sympy import primorial
+
+    for P, d in [(503, 210), (3001, 2190)]:
+        K = primorial(P, nth=False) // d
+        limbs = pgo.build_k(P, d)
+        assert sum(l << (32 * i) for i, l in enumerate(limbs)) == K
+
+
+def test_start32(ah):
+    rng = random.Random(11)
+    for _ in range(500):
+        p = _rand_prime(rng, 3, 2**32)
+        r = rng.randrange(0, p)
+        M = rng.randrange(1, 10**10 + 1)
+        sl = rng.randrange(0, min(p, 100000))
+        assert ah.ah_start32(r, M, sl, p) == (r * M + sl) % p
+
+
+def test_mulmod(ah):
+    rng = random.Random(5)
+    for _ in range(1000):
+        p = _rand_prime(rng, 3, 2**46)
+        a, b = rng.randrange(p), rng.randrange(p)
+        assert ah.ah_mulmod(a, b, p) == a * b % p
