@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""Throughput of the GB300 method2 sieve (and of the CPU reference arm).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload config2|config1|config3]
+
+One step = one whole method2 job (prime sieve, K mod p, large-prime marks,
+small-prime rows, compaction, text) on the default workload: P=1511, d=2190,
+minc=100000, SL=20000, max_prime=2e9, mstart=12345679 (a fixed draw inside
+[1e6, 1e8) so the output can be checked against the reference's md5).
+Headline metric: (m, p) pairs resolved per second = valid m x sieving primes
+per second, whole job; primes/s is reported beside it.
+
+`value` is device time (CUDA events on the library's stream) with the job's
+tables resident; `e2e` is the public C-ABI call pgs_method2 with host output
+(tables uploaded and the unknowns text copied back every step).  For N > 1
+each rank sieves its own block of m (no data exchange; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "prime-gap_gb300"
+for _p in (ROOT, PKG, ROOT / "oracle"):
+    if str(_p) not in sys.path:
+        sys.path.insert(0, str(_p))
+
+WORKLOADS = {
+    "config1": dict(p=503, d=210, mstart=1234567, minc=10000, sieve_length=5000, max_prime=100_000_000),
+    "config2": dict(p=1511, d=2190, mstart=12345679, minc=100000, sieve_length=20000,
+                    max_prime=2_000_000_000),
+    "config3": dict(p=3001, d=2190, mstart=123457, minc=100000, sieve_length=40000,
+                    max_prime=10_000_000_000),
+}
+GOLDEN = ROOT / "tests" / "golden" / "goldens.json"
+PROFILE_TRAFFIC = ROOT / "profiles" / "large_kernel_traffic.txt"
+
+
+def _dist():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.tmp = None
+
+    def start(self):
+        try:
+            self.tmp = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.device}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.tmp, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.tmp.flush()
+        rows = [r.split(", ") for r in Path(self.tmp.name).read_text().splitlines() if r.strip()]
+        os.unlink(self.tmp.name)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                smax.append(float(r[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def _traffic_per_launch() -> float | None:
+    if not PROFILE_TRAFFIC.exists():
+        return None
+    for line in PROFILE_TRAFFIC.read_text().splitlines():
+        if line.startswith("traffic_bytes_per_launch_config2:"):
+            return float(line.split(":", 1)[1])
+    return None
+
+
+def _cpu_sample(job: dict, threads: int, rows_fraction: float = 0.1) -> dict:
+    """The oracle port of the reference's method2 on a bounded sample of the
+    workload (the first minc/10 values of m): pairs/s on all host threads."""
+    import pgo
+
+    minc = max(1, int(job["minc"] * rows_fraction))
+    pl = pgo.plan(job["p"], job["d"], job["mstart"], minc, job["sieve_length"], job["max_prime"])
+    t = time.perf_counter()
+    pgo.method2(job["p"], job["d"], job["mstart"], minc, job["sieve_length"], job["max_prime"],
+                threads=threads)
+    dt = time.perf_counter() - t
+    primes = _count_primes(pl["prime_limit"])
+    return {"seconds": dt, "pairs": pl["valid_ms"] * primes, "primes": primes,
+            "sample": f"{job} with minc={minc} (first {rows_fraction:.0%} of m)"}
+
+
+_PI = {100_000_000: 5_761_455, 2_000_000_000: 98_222_287, 10_000_000_000: 455_052_511}
+
+
+def _count_primes(limit: int) -> int:
+    for k, v in _PI.items():
+        if k - 1000 <= limit <= k:
+            return v
+    import pgo
+
+    return len(pgo.primes(0, limit))
+
+
+def run_reference(args, rank, world):
+    """CPU reference arm: the oracle port of method2 on the host cores."""
+    if rank != 0:
+        return 0
+    job = WORKLOADS[args.workload]
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        _cpu_sample(job, threads)
+    secs, pairs, sample = 0.0, 0, ""
+    for _ in range(args.steps):
+        r = _cpu_sample(job, threads)
+        secs += r["seconds"]
+        pairs += r["pairs"]
+        sample = r["sample"]
+    value = pairs / secs
+    line = {
+        "impl": "reference", "metric": "method2 sieve (m,p) pairs/s", "value": value,
+        "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32/u64 integer", "data": "synthetic",
+        "config": {"workload": args.workload, **job},
+        "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_gb300(args, rank, world, local):
+    import torch
+
+    import pgsieve
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    job = dict(WORKLOADS[args.workload])
+    job["mstart"] = job["mstart"] + rank * job["minc"]  # each rank its own block of m
+    spec = pgsieve.JobSpec(**job)
+    sieve = pgsieve.Sieve(local)
+    ext = torch.cuda.ExternalStream(sieve.stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    imad_peak = sieve.int_peak()
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    prep = sieve.prepare(spec)
+    for _ in range(args.warmup):
+        prep.run(True)
+    torch.cuda.synchronize()
+
+    clocks = ClockSampler(local)
+    stage_sum: dict[str, float] = {}
+    step_ms = []
+    barrier()
+    clocks.start()
+    for _ in range(args.steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()  # > L2 (129 MB): every step starts cold
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            prep.run(True)
+            e1.record(ext)
+        e1.synchronize()
+        step_ms.append(e0.elapsed_time(e1))
+        st, _tot = prep.stage_ms()
+        for k, v in st.items():
+            stage_sum[k] = stage_sum.get(k, 0.0) + v
+    barrier()
+    clock_info = clocks.stop()
+    total_ms = sum(step_ms)
+    if dist:
+        t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        total_ms = float(t.item())
+
+    stats: dict = {}
+    data = prep.fetch(stats)
+    prep.close()
+    md5 = hashlib.md5(data).hexdigest()
+    golden = json.loads(GOLDEN.read_text()).get(args.workload, {}) if GOLDEN.exists() else {}
+    if golden and golden.get("max_prime") != spec.max_prime:
+        golden = {}
+    bit_exact = (md5 == golden["md5"]) if (golden and rank == 0) else None
+    pairs_per_step = stats["rows"] * stats["primes"]
+    value = pairs_per_step * world * args.steps / (total_ms * 1e-3)
+    primes_per_s = stats["primes"] * world * args.steps / (total_ms * 1e-3)
+
+    # end to end through the public call (tables up, text down, every step)
+    for _ in range(min(args.warmup, 2)):
+        sieve.method2(spec)
+    barrier()
+    e2e_s = []
+    e2e_stats: dict = {}
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        out = sieve.method2(spec, e2e_stats)
+        e2e_s.append(time.perf_counter() - t)
+    barrier()
+    e2e_total = sum(e2e_s)
+    if dist:
+        t = torch.tensor([e2e_total], dtype=torch.float64, device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_total = float(t.item())
+    plan = pgsieve.plan(spec)
+    h2d = (4 * ((plan["k_bits"] + 31) // 32) + 4 * spec.minc + 4 * (2 * spec.sieve_length + 1)
+           + 4 * plan["valid_ms"] + 2 * spec.sieve_length)
+    e2e = {"value": pairs_per_step * world * args.steps / e2e_total, "unit": "pairs/s",
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(len(out) + 64),
+           "ms_per_step": e2e_total / args.steps * 1e3}
+
+    # roofline of the dominant kernel (large-prime marks): integer-pipe bound.
+    # Algorithmic integer ops per launch from the model in the design doc.
+    s1 = 4 * spec.sieve_length + 2
+    n_windows = max(1, stats["prime_limit"] // (1 << 30) - (s1 + 1) // (1 << 30) + 1)
+    large_ms = stage_sum.get("large", 0.0) / (args.steps * n_windows)
+    model_ops = large_kernel_model_ops(spec, stats) / n_windows
+    achieved = model_ops / (large_ms * 1e-3) if large_ms else None
+    traffic = _traffic_per_launch()
+    roofline = {"kernel": "large_kernel<uint32_t>", "bound": "int", "achieved": achieved,
+                "peak": imad_peak, "unit": "int ops/s",
+                "frac": achieved / imad_peak if achieved else None, "traffic": traffic,
+                "peak_source": "measured live: IMAD microbenchmark (pgs_int_peak)",
+                "avg_launch_ms": large_ms}
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        r = _cpu_sample(job, os.cpu_count() or 1)
+        cpu = {"value": r["pairs"] / r["seconds"], "unit": "pairs/s", "cores": os.cpu_count(),
+               "kind": "port", "sample": r["sample"], "seconds": round(r["seconds"], 2)}
+    line = {
+        "metric": "method2 sieve (m,p) pairs/s", "value": value, "unit": "pairs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32/u64 integer", "data": "synthetic",
+        "config": {"workload": args.workload, **WORKLOADS[args.workload],
+                   "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}"},
+        "primes_per_s": primes_per_s, "bit_exact": bit_exact, "output_md5": md5,
+        "stage_ms_per_step": {k: v / args.steps for k, v in stage_sum.items()},
+        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,
+        "gpu_launches": int(stats["launches"]) * args.steps,
+    }
+    print(json.dumps(line), flush=True)
+    sieve.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def large_kernel_model_ops(spec, stats) -> float:
+    """Model of the large-prime phase's integer work (ops per job), from the
+    expected hit count sum_p minc*(2SL+1)/p over the phase's primes (Mertens:
+    minc*(2SL+1)*(ln ln P1 - ln ln P0)) at 6 ops per hit, plus one Euclid
+    search and one continued fraction per prime at 8 ops per level with
+    0.843*ln(p/(2SL+1)) levels each (Heilbronn's mean)."""
+    import math
+
+    w = 2 * spec.sieve_length + 1
+    p0 = 4 * spec.sieve_length + 2
+    p1 = stats["prime_limit"]
+    hits = spec.minc * w * (math.log(math.log(p1)) - math.log(math.log(p0)))
+    nprimes = stats["primes"]
+    levels = 2 * 0.843 * math.log(max(p1 / 2, p0) / w)
+    return 6 * hits + 8 * levels * nprimes
+
+
+def main() -> int:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--max-prime", type=int, default=0,
+                    help="override the workload's max_prime (small profiling runs)")
+    args = ap.parse_args()
+    rank, world, local = _dist()
+    if args.max_prime:
+        WORKLOADS[args.workload] = dict(WORKLOADS[args.workload], max_prime=args.max_prime)
+        args.workload_note = "max_prime overridden"
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    return run_gb300(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -343,6 +343,86 @@ PG_HD ThreeGap<T> three_gap(T p, T a, T w) {
 }
 
 // ---------------------------------------------------------------------------
+// first entry and three-gap data in one continued-fraction pass
+//
+// The subtractive continued fraction of three_gap is a Rauzy induction of the
+// rotation y -> y + a (mod p): every level (kp, up, kn, dn) is itself a
+// rotation by `up` on a circle of length C = up + dn, whose steps cost kp
+// (no wrap) or kn (wrap) units of the original time, and which is the
+// first-return map of the original rotation to [0, C).  Going one level down
+// shrinks the circle to C' = max(up, dn), and a point of [0, C) enters
+// [0, C') after at most one step (a wrap, y -> y - dn).  Following the start
+// point y0 through every level therefore gives the first time t >= 0 with
+// (y0 + t*a) mod p < w, and its residue, at O(1) per batch of levels -- no
+// separate modulo search.  Requires p > 2w, 0 < a < p, y0 < p.
+template <typename T>
+struct Entry {
+    uint64_t t;  // first k >= 0 with (y0 + k*a) mod p in [0, w)
+    T y;         // that residue, < w
+    ThreeGap<T> g;
+};
+
+template <typename T>
+PG_HD Entry<T> first_entry(T p, T a, T w, T y0) {
+    T kp = 1, up = a, kn = 1, dn = p - a;
+    T y = y0;
+    uint64_t t = 0;
+    for (int pass = 0; pass < 256 && (up >= w || dn >= w); pass++) {
+        if (up > dn) {
+            T q1 = (up - w) / dn + 1;
+            T q2 = (up - 1) / dn;
+            T q = q1 < q2 ? q1 : q2;
+            if (q == 0) break;
+            // level i of the batch enters [0, up - i*dn): y -= dn whenever
+            // y >= up - i*dn, which, once true, stays true for later levels
+            T s;
+            if (y >= up) {
+                s = q;
+            } else {
+                T f = (up - y + dn - 1) / dn;
+                s = f < q ? q - f : 0;
+            }
+            y -= s * dn;
+            t += (uint64_t)s * kn;
+            up -= q * dn;
+            kp += q * kn;
+        } else {
+            T q1 = (dn - w) / up + 1;
+            T q2 = (dn - 1) / up;
+            T q = q1 < q2 ? q1 : q2;
+            if (q == 0) break;
+            // level i enters [0, dn - i*up) with one wrap y -= dn - i*up at the
+            // first level where y >= dn - i*up (after it y < up: no more)
+            T i = y >= dn ? 0 : (dn - y + up - 1) / up;
+            if (i < q) {
+                y -= dn - i * up;
+                t += kn + (uint64_t)i * kp;
+            }
+            dn -= q * up;
+            kn += q * kp;
+        }
+    }
+    if (y >= w) {  // last level: [0, up + dn) -> [0, w) by one wrap
+        y -= dn;
+        t += kn;
+    }
+    return {t, y, {kp, up, kn, dn}};
+}
+
+// Rotation form of the hits after the first one: step n from a hit
+// (mi0, y0) lands at Y = y0 + n*up, residue Y mod C, and
+// mi = mi0 + (n - W)*kp + W*kn with W = floor(Y / C); it is a hit iff the
+// residue is below w.  Returns an upper bound on the steps n with mi < mi_hi
+// (mi_n - mi0 >= n*p/C - kp - kn since kp*dn + kn*up = p).
+template <typename T>
+PG_HD uint64_t rotation_steps_bound(uint64_t mi0, uint64_t mi_hi, const ThreeGap<T> &g, T p) {
+    if (mi0 >= mi_hi) return 0;
+    const double C = (double)g.up + (double)g.dn;
+    double n = ((double)(mi_hi - mi0) + (double)g.kp + (double)g.kn) * C / (double)p;
+    return (uint64_t)n + 2;
+}
+
+// ---------------------------------------------------------------------------
 // hit enumeration
 
 PG_HD void modsearch_any(uint32_t p, uint32_t a, uint32_t l, uint32_t r, uint64_t &k, uint32_t &v) {
@@ -402,6 +482,28 @@ PG_HD void enumerate_hits(T p, T a, T y, uint64_t mi_lo, uint64_t mi_hi, T two_s
             y = (y + g.up) - g.dn;
         }
         if (mi >= mi_hi) return;
+    }
+}
+
+// Every hit with mi in [mi_lo, mi_hi), from y0 = y(mi_lo): first entry by
+// the continued fraction, then the rotation steps of its last level.
+template <typename T, typename Emit>
+PG_HD void enumerate_hits_cf(T p, T a, T y0, uint64_t mi_lo, uint64_t mi_hi, T two_sl, Emit &emit) {
+    const T w = two_sl + 1;
+    const Entry<T> e = first_entry<T>(p, a, w, y0);
+    if (e.y >= w) return;  // unreachable for prime p > 2w
+    uint64_t mi = mi_lo + e.t;
+    T y = e.y;
+    const T C = e.g.up + e.g.dn;
+    while (mi < mi_hi) {
+        if (y < w) emit(mi, y);
+        y += e.g.up;
+        if (y >= C) {
+            y -= C;
+            mi += e.g.kn;
+        } else {
+            mi += e.g.kp;
+        }
     }
 }
 

@@ -61,6 +61,44 @@ size_t ah_hits(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint64_t r,
     return c.n;
 }
 
+// Same, through the continued-fraction first entry and rotation steps.
+size_t ah_hits_cf(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint64_t r,
+                  uint32_t chunk_len, uint32_t *mi_out, uint64_t *mod_out, size_t cap) {
+    Collect c{mi_out, mod_out, cap, 0};
+    if (chunk_len == 0) chunk_len = max_mi;
+    if (p < 0xFFFFFFFFull) {
+        uint32_t p32 = (uint32_t)p, r32 = (uint32_t)r;
+        uint32_t t0 = (uint32_t)((((M % p32) * (uint64_t)r32) % p32 + SL) % p32);
+        for (uint64_t lo = 0; lo < max_mi; lo += chunk_len) {
+            uint64_t hi = lo + chunk_len < max_mi ? lo + chunk_len : max_mi;
+            uint32_t y = pg::advance_residue(t0, lo, r32, p32);
+            pg::enumerate_hits_cf<uint32_t>(p32, r32, y, lo, hi, 2 * SL, c);
+        }
+    } else {
+        uint64_t t0 = pg::mulmod_u64(M % p, r, p, 1.0 / (double)p) + SL;
+        if (t0 >= p) t0 -= p;
+        for (uint64_t lo = 0; lo < max_mi; lo += chunk_len) {
+            uint64_t hi = lo + chunk_len < max_mi ? lo + chunk_len : max_mi;
+            uint64_t y = pg::advance_residue(t0, lo, r, p);
+            pg::enumerate_hits_cf<uint64_t>(p, r, y, lo, hi, 2ull * SL, c);
+        }
+    }
+    return c.n;
+}
+
+// first_entry: out = {t, y, kp, up, kn, dn}
+void ah_first_entry(uint64_t p, uint64_t a, uint64_t w, uint64_t y0, uint64_t *out6) {
+    if (p < 0xFFFFFFFFull) {
+        auto e = pg::first_entry<uint32_t>((uint32_t)p, (uint32_t)a, (uint32_t)w, (uint32_t)y0);
+        out6[0] = e.t, out6[1] = e.y, out6[2] = e.g.kp, out6[3] = e.g.up, out6[4] = e.g.kn,
+        out6[5] = e.g.dn;
+    } else {
+        auto e = pg::first_entry<uint64_t>(p, a, w, y0);
+        out6[0] = e.t, out6[1] = e.y, out6[2] = e.g.kp, out6[3] = e.g.up, out6[4] = e.g.kn,
+        out6[5] = e.g.dn;
+    }
+}
+
 uint64_t ah_kmod(const uint32_t *limbs, int n, uint64_t q) {
     if (q < 0x80000000ull) {
         uint32_t pinv, r2;

@@ -30,6 +30,10 @@ def ah(built):
     lib.ah_hits.restype = ctypes.c_size_t
     lib.ah_hits.argtypes = [u64, ctypes.c_uint32, ctypes.c_uint32, u64, u64, ctypes.c_uint32,
                             ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
+    lib.ah_hits_cf.restype = ctypes.c_size_t
+    lib.ah_hits_cf.argtypes = lib.ah_hits.argtypes
+    lib.ah_first_entry.restype = None
+    lib.ah_first_entry.argtypes = [u64, u64, u64, u64, ctypes.POINTER(u64)]
     lib.ah_kmod.restype = u64
     lib.ah_kmod.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int, u64]
     lib.ah_start32.restype = ctypes.c_uint32
@@ -39,10 +43,11 @@ def ah(built):
     return lib
 
 
-def _hits(ah, M, max_mi, SL, p, r, chunk=0, cap=1 << 18):
+def _hits(ah, M, max_mi, SL, p, r, chunk=0, cap=1 << 18, cf=False):
     mi = (ctypes.c_uint32 * cap)()
     md = (ctypes.c_uint64 * cap)()
-    n = ah.ah_hits(M, max_mi, SL, p, r, chunk, mi, md, cap)
+    fn = ah.ah_hits_cf if cf else ah.ah_hits
+    n = fn(M, max_mi, SL, p, r, chunk, mi, md, cap)
     assert n <= cap
     return list(zip(mi[:n], md[:n]))
 
@@ -109,6 +114,7 @@ def test_hits_vs_all_large(ah, bits, chunk):
         got = _hits(ah, M, max_mi, SL, p, r, chunk)
         want = pgo.all_large(M, max_mi, SL, p, r)
         assert got == want
+        assert _hits(ah, M, max_mi, SL, p, r, chunk, cf=True) == want
 
 
 def test_hits_dense_small_prime(ah):
@@ -120,7 +126,43 @@ def test_hits_dense_small_prime(ah):
         r = rng.randrange(1, p)
         M = rng.randrange(1, 10**9)
         got = _hits(ah, M, 50000, SL, p, r, 4096)
-        assert got == pgo.all_large(M, 50000, SL, p, r)
+        want = pgo.all_large(M, 50000, SL, p, r)
+        assert got == want
+        assert _hits(ah, M, 50000, SL, p, r, 0, cf=True) == want
+
+
+def test_first_entry_brute(ah):
+    """First k >= 0 with (y0 + k*a) mod p < w, and the three-gap data, by brute force."""
+    rng = random.Random(13)
+    out = (ctypes.c_uint64 * 6)()
+    for _ in range(400):
+        p = _rand_prime(rng, 50, 60000)
+        w = rng.randrange(1, (p - 1) // 2)
+        a = rng.randrange(1, p)
+        y0 = rng.randrange(0, p)
+        ah.ah_first_entry(p, a, w, y0, out)
+        t, y, kp, up, kn, dn = list(out)
+        k = next(k for k in range(0, p) if (y0 + k * a) % p < w)
+        assert (t, y) == (k, (y0 + k * a) % p), (p, a, w, y0)
+        k_up = next(k for k in range(1, p) if 0 < (k * a) % p < w)
+        k_dn = next(k for k in range(1, p) if p - w < (k * a) % p < p)
+        assert (kp, up, kn, dn) == (k_up, (k_up * a) % p, k_dn, p - (k_dn * a) % p)
+
+
+def test_first_entry_wide(ah):
+    """64-bit moduli against the oracle's Euclid search."""
+    rng = random.Random(17)
+    out = (ctypes.c_uint64 * 6)()
+    for _ in range(300):
+        p = _rand_prime(rng, 2**33, 2**45)
+        w = rng.choice([1001, 40001, 80001])
+        a = rng.randrange(1, p)
+        y0 = rng.randrange(w, p)
+        ah.ah_first_entry(p, a, w, y0, out)
+        t, y = out[0], out[1]
+        # smallest k >= 1 with k*a mod p in [p - y0, p - y0 + w - 1]
+        k = pgo.modulo_search(p, a, p - y0, p - y0 + w - 1)
+        assert (t, y) == (k, (y0 + k * a) % p)
 
 
 @pytest.mark.parametrize("P,d", [(503, 210), (907, 2190), (1511, 2190), (3001, 2190), (953, 1)])
