@@ -24,7 +24,6 @@
 namespace {
 
 constexpr uint64_t kWindowSpan = 1ull << 30;
-constexpr uint32_t kDefaultHitsPerItem = 32;
 
 // ---------------------------------------------------------------------------
 // host number theory for job setup
@@ -70,6 +69,7 @@ struct HostJob {
     std::vector<int32_t> col_of_x;
     std::vector<uint32_t> dist;
     std::vector<uint32_t> dq;  // odd primes dividing d
+    std::vector<uint32_t> mmask, xmask;  // valid-m and live-offset bitmasks
     uint32_t x_par = 0, nb = 0, H = 0, Hp = 0, pitch = 0;
     uint64_t coprime_x = 0;
     uint64_t small_threshold = 0, medium_threshold = 0, prime_limit = 0;
@@ -216,10 +216,17 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     h.pitch = (2 * h.Hp / 32 + 3) / 4 * 4;
     if (h.pitch == 0) h.pitch = 4;
     h.col_of_x.assign(interval, -1);
+    h.xmask.assign((interval + 31) / 32, 0);
     for (uint32_t i = 0; i < h.H; i++) {
-        h.col_of_x[SL - h.dist[i]] = (int32_t)i;
-        h.col_of_x[SL + h.dist[i]] = (int32_t)(h.Hp + i);
+        uint32_t lo = SL - h.dist[i], hi = SL + h.dist[i];
+        h.col_of_x[lo] = (int32_t)i;
+        h.col_of_x[hi] = (int32_t)(h.Hp + i);
+        h.xmask[lo >> 5] |= 1u << (lo & 31);
+        h.xmask[hi >> 5] |= 1u << (hi & 31);
     }
+    h.mmask.assign((minc + 31) / 32, 0);
+    for (uint64_t mi = 0; mi < minc; mi++)
+        if (m_ok[mi]) h.mmask[mi >> 5] |= 1u << (mi & 31);
     return PGS_OK;
 }
 
@@ -309,7 +316,7 @@ struct pgs_prepared {
     uint64_t sp_lo = 0, sp_hi = 0, sp_bound = 0;
     uint64_t text_cap = 0;
     uint64_t win_bound = 0;
-    DevBuf klimbs, row_of_mi, col_of_x, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0;
+    DevBuf klimbs, row_of_mi, col_of_x, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0, mmask, xmask;
     DevBuf lists, counts, row_bytes, offsets, scan_tmp, misc, text;
     std::vector<cudaEvent_t> events;
     std::vector<std::pair<int, std::pair<int, int>>> spans;  // stage, (ev a, ev b)
@@ -320,7 +327,8 @@ struct pgs_prepared {
         for (auto e : events) cudaEventDestroy(e);
         DevBuf *all[] = {&klimbs, &row_of_mi, &col_of_x, &valid_mi, &dist,   &dq,
                          &dr,     &comp,      &sp,       &sr,       &sp_t0,  &lists,
-                         &counts, &row_bytes, &offsets,  &scan_tmp, &misc,   &text};
+                         &counts, &row_bytes, &offsets,  &scan_tmp, &misc,   &text,
+                         &mmask,  &xmask};
         for (DevBuf *b : all) b->release();
     }
 };
@@ -346,15 +354,6 @@ cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t s) {
     cudaError_t e = b.ensure(v.size() * sizeof(T));
     if (e || v.empty()) return e;
     return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
-}
-
-uint32_t hits_per_item() {
-    static uint32_t v = [] {
-        const char *s = getenv("PGS_HITS_PER_ITEM");
-        uint32_t x = s ? (uint32_t)atoi(s) : 0;
-        return x ? x : kDefaultHitsPerItem;
-    }();
-    return v;
 }
 
 pg::JobDev job_dev(pgs_prepared *pr) {
@@ -536,6 +535,8 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     CK(upload(pr->valid_mi, h.valid_mi, s));
     CK(upload(pr->dist, h.dist, s));
     CK(upload(pr->dq, h.dq, s));
+    CK(upload(pr->mmask, h.mmask, s));
+    CK(upload(pr->xmask, h.xmask, s));
     CK(pr->dr.ensure(std::max<size_t>(1, h.dq.size()) * 4));
     CK(cudaEventRecord(e1, s));
     // work buffers
@@ -633,7 +634,8 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
                            h.job.sieve_length, ctx->win_r.p, ctx->win_t0.p, win.wide, s));
         CK(mark(e_c));
         CK(pg::large_window(job, win.lo, ctx->win_off.as<uint32_t>(), cnt, win.bound, ctx->win_r.p,
-                            ctx->win_t0.p, win.wide, hits_per_item(), s));
+                            ctx->win_t0.p, win.wide, pr->mmask.as<uint32_t>(),
+                            pr->xmask.as<uint32_t>(), s));
         CK(mark(e_d));
         span(PGS_STAGE_PRIMES, e_a, e_b);
         span(PGS_STAGE_KMOD, e_b, e_c);

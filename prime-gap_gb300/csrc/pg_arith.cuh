@@ -419,7 +419,41 @@ PG_HD uint64_t rotation_steps_bound(uint64_t mi0, uint64_t mi_hi, const ThreeGap
     if (mi0 >= mi_hi) return 0;
     const double C = (double)g.up + (double)g.dn;
     double n = ((double)(mi_hi - mi0) + (double)g.kp + (double)g.kn) * C / (double)p;
-    return (uint64_t)n + 2;
+    uint64_t b = (uint64_t)n + 2;
+    // every step advances mi by at least min(kp, kn)
+    const uint64_t kmin = g.kp < g.kn ? (uint64_t)g.kp : (uint64_t)g.kn;
+    const uint64_t cap = (mi_hi - mi0) / kmin + 1;
+    return b < cap ? b : cap;
+}
+
+// Position of rotation step n0 from the first hit (mi0, y0): residue and mi.
+template <typename T>
+PG_HD void rotation_at(uint64_t mi0, uint32_t y0, const ThreeGap<T> &g, uint64_t n0,
+                       uint32_t &y, uint64_t &mi) {
+    const uint32_t up = (uint32_t)g.up, C = (uint32_t)(g.up + g.dn);
+    const uint64_t Y = y0 + n0 * up;
+    const uint64_t W = Y / C;
+    y = (uint32_t)(Y - W * C);
+    mi = mi0 + (n0 - W) * (uint64_t)g.kp + W * (uint64_t)g.kn;
+}
+
+// Up to `steps` rotation steps from (mi, y), calling emit on the hits, while
+// mi < mi_hi.  up, dn < w < 2^31 so residues fit 32 bits.
+template <typename T, typename Emit>
+PG_HD void rotation_walk(uint64_t mi, uint32_t y, const ThreeGap<T> &g, uint32_t w, uint64_t mi_hi,
+                         uint64_t steps, Emit &emit) {
+    const uint32_t up = (uint32_t)g.up, C = (uint32_t)(g.up + g.dn);
+    const uint64_t kp = g.kp, kn = g.kn;
+    for (uint64_t k = 0; k < steps && mi < mi_hi; k++) {
+        if (y < w) emit(mi, y);
+        y += up;
+        if (y >= C) {
+            y -= C;
+            mi += kn;
+        } else {
+            mi += kp;
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -65,9 +65,11 @@ struct JobDev {
     uint32_t *comp;            // rows * pitch words
 };
 
+// d_mmask: valid-m bitmask (minc bits); d_xmask: live-offset bitmask (2SL+1 bits).
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_count, uint64_t max_count, const void *d_r,
-                         const void *d_t0, bool wide, uint32_t hits_per_item, cudaStream_t stream);
+                         const void *d_t0, bool wide, const uint32_t *d_mmask,
+                         const uint32_t *d_xmask, cudaStream_t stream);
 
 // ---- rows: small primes, merge, extract, format (pg_rows.cu) -----------------
 

@@ -6,17 +6,21 @@
 // With y(mi) = (r*(mstart+mi) + SL) mod p, r = K mod p, a hit is y <= 2*SL and
 // marks offset X = SL - y of m = mstart + mi.
 //
-// The reference runs one Euclid modulo search per hit.  Here one search finds
-// the first hit of a range of mi, then Slater's three-gap theorem gives each
-// following hit in O(1): the return time of y -> y + r (mod p) to [0, 2*SL]
-// takes only the values kp, kn, kp+kn, decided by comparing y against the two
-// record residues up and dn (pg::three_gap).
+// The reference runs one Euclid modulo search per hit.  Here one continued
+// fraction per prime (pg::first_entry) yields both the first hit and the
+// last level (kp, up, kn, dn) of a Rauzy induction of y -> y + r (mod p); after
+// the first hit, the walk is a rotation by `up` on a circle of C = up + dn
+// points, every step costing kp or kn in mi, and every point below 2*SL+1 is a
+// hit.  Step n has the closed form Y = y0 + n*up, residue Y mod C, so a prime's
+// steps split into independent items with no further search.
 //
-// Work is balanced by splitting each prime's mi range into chunks with about
-// `hits_per_item` expected hits; a CTA takes 256 primes, expands their chunks
-// and lets its threads pull (prime, chunk) items.  Hits on a valid m and a
-// live offset set one bit of the L2-resident composite bitset with a global
-// atomicOr.
+// Scheduling: a persistent grid; each CTA takes 256 primes at a time.  Phase 1
+// (one thread per prime) runs the continued fraction; primes with few steps
+// finish right there, the others publish their rotation in shared memory and
+// phase 2 spreads their steps over the CTA in items of kItemSteps.  Hits go
+// through a valid-m bitmask and a live-offset bitmask held in shared memory;
+// only the survivors (a few percent) read the row/column tables and set one
+// bit of the L2-resident composite bitset with a global atomicOr.
 #include "pg_arith.cuh"
 #include "pg_internal.h"
 
@@ -25,73 +29,107 @@ namespace pg {
 namespace {
 
 constexpr int kLargeThreads = 256;
+constexpr uint64_t kDirectSteps = 24;
+constexpr uint32_t kItemSteps = 64;
 
-struct MarkHit {
+struct Marker {
     const JobDev &job;
-    __device__ __forceinline__ void operator()(uint64_t mi, uint64_t y) const {
-        if (y > job.two_sl || mi >= job.minc) return;  // unreachable for prime moduli
-        const uint32_t x = job.two_sl - (uint32_t)y;
+    const uint32_t *mmask;  // valid m bits (shared or global)
+    const uint32_t *xmask;  // live offset bits (shared or global)
+    __device__ __forceinline__ void operator()(uint64_t mi, uint32_t y) const {
+        const uint32_t x = job.two_sl - y;
+        if (!((mmask[mi >> 5] >> (mi & 31)) & 1u)) return;
+        if (!((xmask[x >> 5] >> (x & 31)) & 1u)) return;
         const int32_t row = __ldg(&job.row_of_mi[mi]);
-        if (row < 0) return;
         const int32_t col = __ldg(&job.col_of_x[x]);
-        if (col < 0) return;
         atomicOr(&job.comp[(uint64_t)row * job.pitch + ((uint32_t)col >> 5)], 1u << (col & 31));
     }
+};
+
+template <typename T>
+struct Slots {
+    uint32_t mi0[kLargeThreads];
+    uint32_t y0[kLargeThreads];
+    uint32_t up[kLargeThreads];
+    uint32_t dn[kLargeThreads];
+    T kp[kLargeThreads];
+    T kn[kLargeThreads];
+    uint32_t start[kLargeThreads + 1];
 };
 
 template <typename T>
 __global__ void __launch_bounds__(kLargeThreads)
     large_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
                  const unsigned long long *count, uint64_t max_count, const T *__restrict__ r_in,
-                 const T *__restrict__ t0_in, uint32_t hits_per_item) {
-    __shared__ uint32_t s_start[kLargeThreads + 1];
-    __shared__ T s_p[kLargeThreads], s_r[kLargeThreads], s_t0[kLargeThreads];
-    __shared__ uint32_t s_len[kLargeThreads];
-    const uint64_t n = min((uint64_t)*count, max_count);
-    const uint64_t first = (uint64_t)blockIdx.x * kLargeThreads;
-    if (first >= n) return;
-    const uint64_t i = first + threadIdx.x;
-    uint32_t nch = 0;
-    if (i < n) {
-        const T p = (T)(base + off[i]);
-        s_p[threadIdx.x] = p;
-        s_r[threadIdx.x] = r_in[i];
-        s_t0[threadIdx.x] = t0_in[i];
-        const float e = (float)job.minc * (float)(job.two_sl + 1) / (float)p;
-        float want = ceilf(e / (float)hits_per_item);
-        uint32_t c = want < 1.f ? 1u : (want > (float)job.minc ? job.minc : (uint32_t)want);
-        uint32_t len = (job.minc + c - 1) / c;
-        nch = (job.minc + len - 1) / len;
-        s_len[threadIdx.x] = len;
+                 const T *__restrict__ t0_in, const uint32_t *__restrict__ g_mmask,
+                 const uint32_t *__restrict__ g_xmask, int masks_in_shared) {
+    extern __shared__ uint32_t s_masks[];
+    __shared__ Slots<T> sl;
+    const uint32_t mwords = (job.minc + 31) / 32;
+    const uint32_t xwords = (job.two_sl + 1 + 31) / 32;
+    const uint32_t *mmask = g_mmask, *xmask = g_xmask;
+    if (masks_in_shared) {
+        for (uint32_t i = threadIdx.x; i < mwords; i += blockDim.x) s_masks[i] = g_mmask[i];
+        for (uint32_t i = threadIdx.x; i < xwords; i += blockDim.x) s_masks[mwords + i] = g_xmask[i];
+        mmask = s_masks;
+        xmask = s_masks + mwords;
     }
-    s_start[threadIdx.x + 1] = nch;
-    if (threadIdx.x == 0) s_start[0] = 0;
     __syncthreads();
-    // inclusive scan over s_start[1..256]
-    for (int o = 1; o < kLargeThreads; o <<= 1) {
-        uint32_t v = threadIdx.x >= (uint32_t)o ? s_start[threadIdx.x + 1 - o] : 0;
-        __syncthreads();
-        s_start[threadIdx.x + 1] += v;
-        __syncthreads();
-    }
-    const uint32_t total = s_start[kLargeThreads];
-    for (uint32_t it = threadIdx.x; it < total; it += kLargeThreads) {
-        // slot s with s_start[s] <= it < s_start[s+1]
-        uint32_t lo = 0, hi = kLargeThreads;
-        while (hi - lo > 1) {
-            uint32_t mid = (lo + hi) >> 1;
-            if (s_start[mid] <= it) lo = mid;
-            else hi = mid;
+    const Marker mark{job, mmask, xmask};
+    const uint64_t n = min((uint64_t)*count, max_count);
+    const T w = (T)job.two_sl + 1;
+    const uint64_t minc = job.minc;
+
+    for (uint64_t group = blockIdx.x; group * kLargeThreads < n; group += gridDim.x) {
+        const uint64_t i = group * kLargeThreads + threadIdx.x;
+        uint32_t items = 0;
+        if (i < n) {
+            const T p = (T)(base + off[i]);
+            const T r = r_in[i];
+            const Entry<T> e = first_entry<T>(p, r, w, t0_in[i]);
+            if (e.t < minc && e.y < w) {
+                const uint64_t bound = rotation_steps_bound<T>(e.t, minc, e.g, p);
+                if (bound <= kDirectSteps) {
+                    // few steps: walk the rotation here
+                    rotation_walk<T>(e.t, (uint32_t)e.y, e.g, (uint32_t)w, minc, bound, mark);
+                } else {
+                    sl.mi0[threadIdx.x] = (uint32_t)e.t;
+                    sl.y0[threadIdx.x] = (uint32_t)e.y;
+                    sl.up[threadIdx.x] = (uint32_t)e.g.up;
+                    sl.dn[threadIdx.x] = (uint32_t)e.g.dn;
+                    sl.kp[threadIdx.x] = e.g.kp;
+                    sl.kn[threadIdx.x] = e.g.kn;
+                    items = (uint32_t)((bound + kItemSteps - 1) / kItemSteps);
+                }
+            }
         }
-        const uint32_t s = lo;
-        const uint32_t c = it - s_start[s];
-        const uint64_t mi_lo = (uint64_t)c * s_len[s];
-        uint64_t mi_hi = mi_lo + s_len[s];
-        if (mi_hi > job.minc) mi_hi = job.minc;
-        const T p = s_p[s], r = s_r[s];
-        const T y = advance_residue(s_t0[s], mi_lo, r, p);
-        MarkHit mark{job};
-        enumerate_hits<T>(p, r, y, mi_lo, mi_hi, (T)job.two_sl, mark);
+        // exclusive scan of item counts
+        sl.start[threadIdx.x + 1] = items;
+        if (threadIdx.x == 0) sl.start[0] = 0;
+        __syncthreads();
+        for (int o = 1; o < kLargeThreads; o <<= 1) {
+            uint32_t v = threadIdx.x >= (uint32_t)o ? sl.start[threadIdx.x + 1 - o] : 0;
+            __syncthreads();
+            sl.start[threadIdx.x + 1] += v;
+            __syncthreads();
+        }
+        const uint32_t total = sl.start[kLargeThreads];
+        for (uint32_t it = threadIdx.x; it < total; it += kLargeThreads) {
+            uint32_t lo = 0, hi = kLargeThreads;
+            while (hi - lo > 1) {
+                uint32_t mid = (lo + hi) >> 1;
+                if (sl.start[mid] <= it) lo = mid;
+                else hi = mid;
+            }
+            const uint32_t s = lo;
+            const uint64_t n0 = (uint64_t)(it - sl.start[s]) * kItemSteps;
+            const ThreeGap<T> g{sl.kp[s], (T)sl.up[s], sl.kn[s], (T)sl.dn[s]};
+            uint32_t y;
+            uint64_t mi;
+            rotation_at<T>(sl.mi0[s], sl.y0[s], g, n0, y, mi);
+            rotation_walk<T>(mi, y, g, (uint32_t)w, minc, kItemSteps, mark);
+        }
+        __syncthreads();
     }
 }
 
@@ -99,15 +137,43 @@ __global__ void __launch_bounds__(kLargeThreads)
 
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_count, uint64_t max_count, const void *d_r,
-                         const void *d_t0, bool wide, uint32_t hits_per_item, cudaStream_t stream) {
+                         const void *d_t0, bool wide, const uint32_t *d_mmask,
+                         const uint32_t *d_xmask, cudaStream_t stream) {
     if (max_count == 0) return cudaSuccess;
-    uint64_t blocks = (max_count + kLargeThreads - 1) / kLargeThreads;
+    const size_t mask_bytes = 4ull * ((job.minc + 31) / 32 + (job.two_sl + 1 + 31) / 32);
+    const int in_shared = mask_bytes <= 96 * 1024;
+    const size_t smem = in_shared ? mask_bytes : 0;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e;
+    if (wide) {
+        if (smem > 48 * 1024 &&
+            (e = cudaFuncSetAttribute(large_kernel<uint64_t>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, large_kernel<uint64_t>,
+                                                      kLargeThreads, smem);
+    } else {
+        if (smem > 48 * 1024 &&
+            (e = cudaFuncSetAttribute(large_kernel<uint32_t>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
+            return e;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, large_kernel<uint32_t>,
+                                                      kLargeThreads, smem);
+    }
+    if (per_sm < 1) per_sm = 1;
+    uint64_t groups = (max_count + kLargeThreads - 1) / kLargeThreads;
+    uint64_t blocks = (uint64_t)sms * per_sm;
+    if (blocks > groups) blocks = groups;
     if (wide)
-        large_kernel<uint64_t><<<(unsigned)blocks, kLargeThreads, 0, stream>>>(
-            job, base, d_off, d_count, max_count, (const uint64_t *)d_r, (const uint64_t *)d_t0, hits_per_item);
+        large_kernel<uint64_t><<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
+            job, base, d_off, d_count, max_count, (const uint64_t *)d_r, (const uint64_t *)d_t0,
+            d_mmask, d_xmask, in_shared);
     else
-        large_kernel<uint32_t><<<(unsigned)blocks, kLargeThreads, 0, stream>>>(
-            job, base, d_off, d_count, max_count, (const uint32_t *)d_r, (const uint32_t *)d_t0, hits_per_item);
+        large_kernel<uint32_t><<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
+            job, base, d_off, d_count, max_count, (const uint32_t *)d_r, (const uint32_t *)d_t0,
+            d_mmask, d_xmask, in_shared);
     return cudaGetLastError();
 }
 

@@ -52,11 +52,11 @@ __global__ void large_hits_kernel(uint64_t M, uint32_t max_mi, uint32_t sl, uint
         uint32_t p32 = (uint32_t)p, r32 = (uint32_t)r;
         // y(0) = (r*M + SL) mod p
         uint32_t y = (uint32_t)((((M % p32) * (uint64_t)r32) % p32 + sl) % p32);
-        enumerate_hits<uint32_t>(p32, r32, y, 0, max_mi, (uint32_t)two_sl, c);
+        enumerate_hits_cf<uint32_t>(p32, r32, y, 0, max_mi, (uint32_t)two_sl, c);
     } else {
         uint64_t y = mulmod_u64(M % p, r, p, 1.0 / (double)p) + sl;
         if (y >= p) y -= p;
-        enumerate_hits<uint64_t>(p, r, y, 0, max_mi, two_sl, c);
+        enumerate_hits_cf<uint64_t>(p, r, y, 0, max_mi, two_sl, c);
     }
     *count = c.n;
 }

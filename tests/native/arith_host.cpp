@@ -86,6 +86,43 @@ size_t ah_hits_cf(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint64_t
     return c.n;
 }
 
+// Hits of one prime split the way the large-prime kernel splits them: first
+// entry, then either a direct walk (bound <= direct) or items of item_steps
+// steps started from the closed form.  Returns the hit count (hits in order).
+size_t ah_hits_items(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint64_t r,
+                     uint32_t direct, uint32_t item_steps, uint32_t *mi_out, uint64_t *mod_out,
+                     size_t cap) {
+    Collect c{mi_out, mod_out, cap, 0};
+    auto run = [&](auto p_, auto r_, auto t0) {
+        using T = decltype(p_);
+        const T w = (T)(2 * SL + 1);
+        pg::Entry<T> e = pg::first_entry<T>(p_, r_, w, t0);
+        if (e.t >= max_mi || e.y >= w) return;
+        uint64_t bound = pg::rotation_steps_bound<T>(e.t, max_mi, e.g, p_);
+        if (bound <= direct) {
+            pg::rotation_walk<T>(e.t, (uint32_t)e.y, e.g, (uint32_t)w, max_mi, bound, c);
+            return;
+        }
+        uint64_t items = (bound + item_steps - 1) / item_steps;
+        for (uint64_t it = 0; it < items; it++) {
+            uint32_t y;
+            uint64_t mi;
+            pg::rotation_at<T>(e.t, (uint32_t)e.y, e.g, it * item_steps, y, mi);
+            pg::rotation_walk<T>(mi, y, e.g, (uint32_t)w, max_mi, item_steps, c);
+        }
+    };
+    if (p < 0xFFFFFFFFull) {
+        uint32_t p32 = (uint32_t)p, r32 = (uint32_t)r;
+        uint32_t t0 = (uint32_t)((((M % p32) * (uint64_t)r32) % p32 + SL) % p32);
+        run(p32, r32, t0);
+    } else {
+        uint64_t t0 = pg::mulmod_u64(M % p, r, p, 1.0 / (double)p) + SL;
+        if (t0 >= p) t0 -= p;
+        run(p, r, t0);
+    }
+    return c.n;
+}
+
 // first_entry: out = {t, y, kp, up, kn, dn}
 void ah_first_entry(uint64_t p, uint64_t a, uint64_t w, uint64_t y0, uint64_t *out6) {
     if (p < 0xFFFFFFFFull) {

@@ -32,6 +32,10 @@ def ah(built):
                             ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
     lib.ah_hits_cf.restype = ctypes.c_size_t
     lib.ah_hits_cf.argtypes = lib.ah_hits.argtypes
+    lib.ah_hits_items.restype = ctypes.c_size_t
+    lib.ah_hits_items.argtypes = [u64, ctypes.c_uint32, ctypes.c_uint32, u64, u64, ctypes.c_uint32,
+                                  ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
+                                  ctypes.POINTER(u64), ctypes.c_size_t]
     lib.ah_first_entry.restype = None
     lib.ah_first_entry.argtypes = [u64, u64, u64, u64, ctypes.POINTER(u64)]
     lib.ah_kmod.restype = u64
@@ -129,6 +133,30 @@ def test_hits_dense_small_prime(ah):
         want = pgo.all_large(M, 50000, SL, p, r)
         assert got == want
         assert _hits(ah, M, 50000, SL, p, r, 0, cf=True) == want
+
+
+def _hits_items(ah, M, max_mi, SL, p, r, direct, item, cap=1 << 18):
+    mi = (ctypes.c_uint32 * cap)()
+    md = (ctypes.c_uint64 * cap)()
+    n = ah.ah_hits_items(M, max_mi, SL, p, r, direct, item, mi, md, cap)
+    assert n <= cap
+    return list(zip(mi[:n], md[:n]))
+
+
+@pytest.mark.parametrize("bits", [18, 24, 31, 32, 34, 40])
+def test_hits_items_vs_all_large(ah, bits):
+    """The kernel's split: direct walk or closed-form items of 64 (and odd sizes)."""
+    rng = random.Random(bits + 77)
+    for _ in range(80):
+        SL = rng.choice([500, 4000, 20000, 40000])
+        lo = max(4 * SL + 3, 2 ** (bits - 1))
+        p = _rand_prime(rng, lo, max(2 * lo, 2**bits))
+        r = rng.randrange(1, p)
+        M = rng.randrange(1, 10**10)
+        max_mi = rng.choice([1, 17, 1000, 100000])
+        want = pgo.all_large(M, max_mi, SL, p, r)
+        for direct, item in ((24, 64), (0, 64), (0, 7), (10**9, 64)):
+            assert _hits_items(ah, M, max_mi, SL, p, r, direct, item) == want
 
 
 def test_first_entry_brute(ah):
