@@ -306,7 +306,7 @@ struct pgs_ctx {
     std::mutex mu;
     std::string err;
     pg::BasePrimes base;
-    DevBuf win_off, win_r, win_t0;
+    DevBuf win_off, win_r, win_t0, large_ctr, heavy;
 };
 
 struct pgs_prepared {
@@ -437,6 +437,8 @@ void pgs_destroy(pgs_ctx *ctx) {
     ctx->win_off.release();
     ctx->win_r.release();
     ctx->win_t0.release();
+    ctx->large_ctr.release();
+    ctx->heavy.release();
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
@@ -560,6 +562,8 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     CK(ctx->win_off.ensure(pr->win_bound * 4 + 4));
     CK(ctx->win_r.ensure(pr->win_bound * 8 + 8));
     CK(ctx->win_t0.ensure(pr->win_bound * 8 + 8));
+    CK(ctx->large_ctr.ensure(2 * sizeof(unsigned long long)));
+    CK(ctx->heavy.ensure((size_t)pg::heavy_capacity() * pg::kHeavyPrimeBytes));
     CK(cudaStreamSynchronize(s));
     float ms = 0;
     cudaEventElapsedTime(&ms, e0, e1);
@@ -635,12 +639,15 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
         CK(mark(e_c));
         CK(pg::large_window(job, win.lo, ctx->win_off.as<uint32_t>(), cnt, win.bound, ctx->win_r.p,
                             ctx->win_t0.p, win.wide, pr->mmask.as<uint32_t>(),
-                            pr->xmask.as<uint32_t>(), s));
+                            pr->xmask.as<uint32_t>(),
+                            pg::LargeScratch{ctx->large_ctr.as<unsigned long long>(),
+                                             ctx->heavy.as<pg::HeavyPrime>(), pg::heavy_capacity()},
+                            s));
         CK(mark(e_d));
         span(PGS_STAGE_PRIMES, e_a, e_b);
         span(PGS_STAGE_KMOD, e_b, e_c);
         span(PGS_STAGE_LARGE, e_c, e_d);
-        pr->launches += 3;
+        pr->launches += 4;
     }
     // rows, text
     CK(mark(a));

@@ -369,9 +369,9 @@ PG_HD Entry<T> first_entry(T p, T a, T w, T y0) {
     uint64_t t = 0;
     for (int pass = 0; pass < 256 && (up >= w || dn >= w); pass++) {
         if (up > dn) {
-            T q1 = (up - w) / dn + 1;
-            T q2 = (up - 1) / dn;
-            T q = q1 < q2 ? q1 : q2;
+            // subtract dn until up < w or up <= dn: q = ceil((up - max(w-1, dn)) / dn)
+            const T lim = (w - 1) > dn ? (w - 1) : dn;
+            T q = (up - lim + dn - 1) / dn;
             if (q == 0) break;
             // level i of the batch enters [0, up - i*dn): y -= dn whenever
             // y >= up - i*dn, which, once true, stays true for later levels
@@ -387,9 +387,8 @@ PG_HD Entry<T> first_entry(T p, T a, T w, T y0) {
             up -= q * dn;
             kp += q * kn;
         } else {
-            T q1 = (dn - w) / up + 1;
-            T q2 = (dn - 1) / up;
-            T q = q1 < q2 ? q1 : q2;
+            const T lim = (w - 1) > up ? (w - 1) : up;
+            T q = (dn - lim + up - 1) / up;
             if (q == 0) break;
             // level i enters [0, dn - i*up) with one wrap y -= dn - i*up at the
             // first level where y >= dn - i*up (after it y < up: no more)
@@ -417,9 +416,10 @@ PG_HD Entry<T> first_entry(T p, T a, T w, T y0) {
 template <typename T>
 PG_HD uint64_t rotation_steps_bound(uint64_t mi0, uint64_t mi_hi, const ThreeGap<T> &g, T p) {
     if (mi0 >= mi_hi) return 0;
-    const double C = (double)g.up + (double)g.dn;
-    double n = ((double)(mi_hi - mi0) + (double)g.kp + (double)g.kn) * C / (double)p;
-    uint64_t b = (uint64_t)n + 2;
+    const float C = (float)g.up + (float)g.dn;
+    // single precision with a relative margin: the result only sizes work
+    float n = ((float)(mi_hi - mi0) + (float)g.kp + (float)g.kn) * C / (float)p;
+    uint64_t b = (uint64_t)(n * 1.0001f) + 2;
     // every step advances mi by at least min(kp, kn)
     const uint64_t kmin = g.kp < g.kn ? (uint64_t)g.kp : (uint64_t)g.kn;
     const uint64_t cap = (mi_hi - mi0) / kmin + 1;

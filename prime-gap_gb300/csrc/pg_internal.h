@@ -65,11 +65,22 @@ struct JobDev {
     uint32_t *comp;            // rows * pitch words
 };
 
+struct HeavyPrime;
+// Device scratch of the large-prime phase: two counters (group claims, heavy
+// primes) and the heavy-prime list.
+struct LargeScratch {
+    unsigned long long *counters;
+    HeavyPrime *heavy;
+    uint32_t heavy_cap;
+};
+uint32_t heavy_capacity();
+constexpr size_t kHeavyPrimeBytes = 40;
+
 // d_mmask: valid-m bitmask (minc bits); d_xmask: live-offset bitmask (2SL+1 bits).
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_count, uint64_t max_count, const void *d_r,
                          const void *d_t0, bool wide, const uint32_t *d_mmask,
-                         const uint32_t *d_xmask, cudaStream_t stream);
+                         const uint32_t *d_xmask, LargeScratch scratch, cudaStream_t stream);
 
 // ---- rows: small primes, merge, extract, format (pg_rows.cu) -----------------
 

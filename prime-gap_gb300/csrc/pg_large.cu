@@ -14,10 +14,13 @@
 // hit.  Step n has the closed form Y = y0 + n*up, residue Y mod C, so a prime's
 // steps split into independent items with no further search.
 //
-// Scheduling: a persistent grid; each CTA takes 256 primes at a time.  Phase 1
-// (one thread per prime) runs the continued fraction; primes with few steps
-// finish right there, the others publish their rotation in shared memory and
-// phase 2 spreads their steps over the CTA in items of kItemSteps.  Hits go
+// Scheduling: a persistent grid whose CTAs claim groups of 256 primes from an
+// atomic counter (the prime list is roughly ascending, so the heavy small
+// primes go first).  Phase 1 (one thread per prime) runs the continued
+// fraction; primes with few steps finish right there, primes with very many
+// steps (the smallest ones) go to a device list for heavy_kernel, one CTA per
+// prime, and the rest publish their rotation in shared memory for phase 2,
+// which spreads their steps over the CTA in items of kItemSteps.  Hits go
 // through a valid-m bitmask and a live-offset bitmask held in shared memory;
 // only the survivors (a few percent) read the row/column tables and set one
 // bit of the L2-resident composite bitset with a global atomicOr.
@@ -31,6 +34,7 @@ namespace {
 constexpr int kLargeThreads = 256;
 constexpr uint64_t kDirectSteps = 24;
 constexpr uint32_t kItemSteps = 64;
+constexpr uint64_t kHeavySteps = 16384;
 
 struct Marker {
     const JobDev &job;
@@ -46,6 +50,16 @@ struct Marker {
     }
 };
 
+}  // namespace
+
+struct HeavyPrime {
+    uint32_t mi0, y0, up, dn;
+    uint64_t kp, kn, steps;
+};
+static_assert(sizeof(HeavyPrime) == kHeavyPrimeBytes, "heavy list stride");
+
+namespace {
+
 template <typename T>
 struct Slots {
     uint32_t mi0[kLargeThreads];
@@ -57,30 +71,46 @@ struct Slots {
     uint32_t start[kLargeThreads + 1];
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kLargeThreads)
-    large_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
-                 const unsigned long long *count, uint64_t max_count, const T *__restrict__ r_in,
-                 const T *__restrict__ t0_in, const uint32_t *__restrict__ g_mmask,
-                 const uint32_t *__restrict__ g_xmask, int masks_in_shared) {
-    extern __shared__ uint32_t s_masks[];
-    __shared__ Slots<T> sl;
+__device__ __forceinline__ void load_masks(const JobDev &job, const uint32_t *g_mmask,
+                                           const uint32_t *g_xmask, int in_shared,
+                                           uint32_t *s_masks, const uint32_t *&mmask,
+                                           const uint32_t *&xmask) {
     const uint32_t mwords = (job.minc + 31) / 32;
     const uint32_t xwords = (job.two_sl + 1 + 31) / 32;
-    const uint32_t *mmask = g_mmask, *xmask = g_xmask;
-    if (masks_in_shared) {
+    mmask = g_mmask;
+    xmask = g_xmask;
+    if (in_shared) {
         for (uint32_t i = threadIdx.x; i < mwords; i += blockDim.x) s_masks[i] = g_mmask[i];
         for (uint32_t i = threadIdx.x; i < xwords; i += blockDim.x) s_masks[mwords + i] = g_xmask[i];
         mmask = s_masks;
         xmask = s_masks + mwords;
     }
     __syncthreads();
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kLargeThreads)
+    large_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
+                 const unsigned long long *count, uint64_t max_count, const T *__restrict__ r_in,
+                 const T *__restrict__ t0_in, const uint32_t *__restrict__ g_mmask,
+                 const uint32_t *__restrict__ g_xmask, int masks_in_shared,
+                 unsigned long long *group_ctr, HeavyPrime *heavy, unsigned long long *heavy_count,
+                 uint32_t heavy_cap) {
+    extern __shared__ uint32_t s_masks[];
+    __shared__ Slots<T> sl;
+    __shared__ unsigned long long s_group;
+    const uint32_t *mmask, *xmask;
+    load_masks(job, g_mmask, g_xmask, masks_in_shared, s_masks, mmask, xmask);
     const Marker mark{job, mmask, xmask};
     const uint64_t n = min((uint64_t)*count, max_count);
     const T w = (T)job.two_sl + 1;
     const uint64_t minc = job.minc;
 
-    for (uint64_t group = blockIdx.x; group * kLargeThreads < n; group += gridDim.x) {
+    for (;;) {
+        if (threadIdx.x == 0) s_group = atomicAdd(group_ctr, 1ull);
+        __syncthreads();
+        const uint64_t group = s_group;
+        if (group * kLargeThreads >= n) break;
         const uint64_t i = group * kLargeThreads + threadIdx.x;
         uint32_t items = 0;
         if (i < n) {
@@ -89,10 +119,22 @@ __global__ void __launch_bounds__(kLargeThreads)
             const Entry<T> e = first_entry<T>(p, r, w, t0_in[i]);
             if (e.t < minc && e.y < w) {
                 const uint64_t bound = rotation_steps_bound<T>(e.t, minc, e.g, p);
+                bool local = true;
                 if (bound <= kDirectSteps) {
                     // few steps: walk the rotation here
                     rotation_walk<T>(e.t, (uint32_t)e.y, e.g, (uint32_t)w, minc, bound, mark);
-                } else {
+                    local = false;
+                } else if (bound > kHeavySteps) {
+                    // very many steps: one CTA of heavy_kernel takes this prime
+                    const unsigned long long h = atomicAdd(heavy_count, 1ull);
+                    if (h < heavy_cap) {
+                        heavy[h] = HeavyPrime{(uint32_t)e.t, (uint32_t)e.y, (uint32_t)e.g.up,
+                                              (uint32_t)e.g.dn, (uint64_t)e.g.kp,
+                                              (uint64_t)e.g.kn, bound};
+                        local = false;
+                    }
+                }
+                if (local) {
                     sl.mi0[threadIdx.x] = (uint32_t)e.t;
                     sl.y0[threadIdx.x] = (uint32_t)e.y;
                     sl.up[threadIdx.x] = (uint32_t)e.g.up;
@@ -133,12 +175,39 @@ __global__ void __launch_bounds__(kLargeThreads)
     }
 }
 
+// One CTA per heavy prime: its rotation steps split over the CTA's threads.
+__global__ void __launch_bounds__(kLargeThreads)
+    heavy_kernel(JobDev job, const HeavyPrime *__restrict__ heavy,
+                 const unsigned long long *heavy_count, uint32_t heavy_cap,
+                 const uint32_t *__restrict__ g_mmask, const uint32_t *__restrict__ g_xmask,
+                 int masks_in_shared) {
+    extern __shared__ uint32_t s_masks[];
+    const uint32_t *mmask, *xmask;
+    load_masks(job, g_mmask, g_xmask, masks_in_shared, s_masks, mmask, xmask);
+    const Marker mark{job, mmask, xmask};
+    const uint64_t nh = min((uint64_t)*heavy_count, (uint64_t)heavy_cap);
+    const uint32_t w = job.two_sl + 1;
+    for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const HeavyPrime hp = heavy[h];
+        const ThreeGap<uint64_t> g{hp.kp, hp.up, hp.kn, hp.dn};
+        const uint64_t items = (hp.steps + kItemSteps - 1) / kItemSteps;
+        for (uint64_t it = threadIdx.x; it < items; it += blockDim.x) {
+            uint32_t y;
+            uint64_t mi;
+            rotation_at<uint64_t>(hp.mi0, hp.y0, g, it * kItemSteps, y, mi);
+            rotation_walk<uint64_t>(mi, y, g, w, job.minc, kItemSteps, mark);
+        }
+    }
+}
+
 }  // namespace
+
+uint32_t heavy_capacity() { return 1u << 20; }
 
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_count, uint64_t max_count, const void *d_r,
                          const void *d_t0, bool wide, const uint32_t *d_mmask,
-                         const uint32_t *d_xmask, cudaStream_t stream) {
+                         const uint32_t *d_xmask, LargeScratch scratch, cudaStream_t stream) {
     if (max_count == 0) return cudaSuccess;
     const size_t mask_bytes = 4ull * ((job.minc + 31) / 32 + (job.two_sl + 1 + 31) / 32);
     const int in_shared = mask_bytes <= 96 * 1024;
@@ -147,21 +216,18 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaError_t e;
-    if (wide) {
-        if (smem > 48 * 1024 &&
-            (e = cudaFuncSetAttribute(large_kernel<uint64_t>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-            return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, large_kernel<uint64_t>,
-                                                      kLargeThreads, smem);
-    } else {
-        if (smem > 48 * 1024 &&
-            (e = cudaFuncSetAttribute(large_kernel<uint32_t>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem)))
-            return e;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, large_kernel<uint32_t>,
-                                                      kLargeThreads, smem);
-    }
+    if ((e = cudaMemsetAsync(scratch.counters, 0, 2 * sizeof(unsigned long long), stream))) return e;
+    unsigned long long *group_ctr = scratch.counters, *heavy_count = scratch.counters + 1;
+    auto prep = [&](auto kernel) -> cudaError_t {
+        if (smem > 48 * 1024) {
+            cudaError_t err =
+                cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            if (err) return err;
+        }
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kLargeThreads, smem);
+        return cudaSuccess;
+    };
+    if ((e = wide ? prep(large_kernel<uint64_t>) : prep(large_kernel<uint32_t>))) return e;
     if (per_sm < 1) per_sm = 1;
     uint64_t groups = (max_count + kLargeThreads - 1) / kLargeThreads;
     uint64_t blocks = (uint64_t)sms * per_sm;
@@ -169,11 +235,16 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
     if (wide)
         large_kernel<uint64_t><<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
             job, base, d_off, d_count, max_count, (const uint64_t *)d_r, (const uint64_t *)d_t0,
-            d_mmask, d_xmask, in_shared);
+            d_mmask, d_xmask, in_shared, group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
     else
         large_kernel<uint32_t><<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
             job, base, d_off, d_count, max_count, (const uint32_t *)d_r, (const uint32_t *)d_t0,
-            d_mmask, d_xmask, in_shared);
+            d_mmask, d_xmask, in_shared, group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
+    if ((e = cudaGetLastError())) return e;
+    if ((e = prep(heavy_kernel))) return e;
+    if (per_sm < 1) per_sm = 1;
+    heavy_kernel<<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(
+        job, scratch.heavy, heavy_count, scratch.heavy_cap, d_mmask, d_xmask, in_shared);
     return cudaGetLastError();
 }
 

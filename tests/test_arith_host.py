@@ -57,9 +57,13 @@ def _hits(ah, M, max_mi, SL, p, r, chunk=0, cap=1 << 18, cf=False):
 
 
 def _rand_prime(rng, lo, hi):
+    """A prime in [lo, hi) drawn from the seeded generator."""
     import sympy
 
-    return sympy.randprime(lo, hi)
+    while True:
+        q = sympy.nextprime(rng.randrange(lo, hi) - 1)
+        if q < hi:
+            return q
 
 
 def test_modsearch_known_answers(ah):
@@ -165,7 +169,7 @@ def test_first_entry_brute(ah):
     out = (ctypes.c_uint64 * 6)()
     for _ in range(400):
         p = _rand_prime(rng, 50, 60000)
-        w = rng.randrange(1, (p - 1) // 2)
+        w = rng.randrange(2, (p - 1) // 2)  # the sieve's window is 2*SL+1 >= 3
         a = rng.randrange(1, p)
         y0 = rng.randrange(0, p)
         ah.ah_first_entry(p, a, w, y0, out)
