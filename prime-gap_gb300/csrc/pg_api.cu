@@ -233,21 +233,65 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
 // ---------------------------------------------------------------------------
 // device buffers and the pinned host pool
 
+// Device allocations recycled across jobs on one context: a job's buffers
+// (several GB for the larger configs) are returned here instead of freed, so
+// repeated jobs pay no cudaMalloc/cudaFree.
+struct DevicePool {
+    std::mutex mu;
+    std::vector<std::pair<void *, size_t>> free_list;
+    cudaError_t get(size_t n, void **p, size_t *cap) {
+        {
+            std::lock_guard<std::mutex> g(mu);
+            size_t best = (size_t)-1;
+            for (size_t i = 0; i < free_list.size(); i++)
+                if (free_list[i].second >= n &&
+                    (best == (size_t)-1 || free_list[i].second < free_list[best].second))
+                    best = i;
+            // reuse only blocks that are not much larger than the request
+            if (best != (size_t)-1 && free_list[best].second <= 2 * n + (1u << 20)) {
+                *p = free_list[best].first;
+                *cap = free_list[best].second;
+                free_list.erase(free_list.begin() + best);
+                return cudaSuccess;
+            }
+        }
+        cudaError_t e = cudaMalloc(p, n);
+        if (e == cudaErrorMemoryAllocation) {
+            trim();  // give cached blocks back and retry once
+            e = cudaMalloc(p, n);
+        }
+        if (e == cudaSuccess) *cap = n;
+        return e;
+    }
+    void put(void *p, size_t cap) {
+        std::lock_guard<std::mutex> g(mu);
+        free_list.push_back({p, cap});
+    }
+    void trim() {
+        std::lock_guard<std::mutex> g(mu);
+        for (auto &b : free_list) cudaFree(b.first);
+        free_list.clear();
+    }
+};
+
 struct DevBuf {
     void *p = nullptr;
     size_t n = 0;
+    DevicePool *pool = nullptr;
     cudaError_t ensure(size_t bytes) {
         if (bytes <= n && p) return cudaSuccess;
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
+        release();
         size_t want = bytes < 256 ? 256 : bytes;
+        if (pool) return pool->get(want, &p, &n);
         cudaError_t e = cudaMalloc(&p, want);
         if (e == cudaSuccess) n = want;
         return e;
     }
     void release() {
-        if (p) cudaFree(p);
+        if (p) {
+            if (pool) pool->put(p, n);
+            else cudaFree(p);
+        }
         p = nullptr;
         n = 0;
     }
@@ -307,6 +351,7 @@ struct pgs_ctx {
     std::string err;
     pg::BasePrimes base;
     DevBuf win_off, win_r, win_t0, large_ctr, heavy;
+    DevicePool dpool;
 };
 
 struct pgs_prepared {
@@ -323,13 +368,14 @@ struct pgs_prepared {
     double ms_setup = 0;
     uint64_t launches = 0;
     bool ran = false;
+    std::vector<DevBuf *> all() {
+        return {&klimbs, &row_of_mi, &col_of_x, &valid_mi, &dist,   &dq,     &dr,
+                &comp,   &sp,        &sr,       &sp_t0,    &lists,  &counts, &row_bytes,
+                &offsets, &scan_tmp, &misc,     &text,     &mmask,  &xmask};
+    }
     ~pgs_prepared() {
         for (auto e : events) cudaEventDestroy(e);
-        DevBuf *all[] = {&klimbs, &row_of_mi, &col_of_x, &valid_mi, &dist,   &dq,
-                         &dr,     &comp,      &sp,       &sr,       &sp_t0,  &lists,
-                         &counts, &row_bytes, &offsets,  &scan_tmp, &misc,   &text,
-                         &mmask,  &xmask};
-        for (DevBuf *b : all) b->release();
+        for (DevBuf *b : all()) b->release();
     }
 };
 
@@ -439,6 +485,7 @@ void pgs_destroy(pgs_ctx *ctx) {
     ctx->win_t0.release();
     ctx->large_ctr.release();
     ctx->heavy.release();
+    ctx->dpool.trim();
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
@@ -496,6 +543,7 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     }
     auto *pr = new pgs_prepared();
     pr->ctx = ctx;
+    for (DevBuf *b : pr->all()) b->pool = &ctx->dpool;
     int rc = derive(*job, pr->hj, ctx->err, true);
     if (rc != PGS_OK) {
         delete pr;

@@ -116,6 +116,41 @@ PG_HD uint32_t kmod32(const uint32_t *limbs, int n, uint32_t p, uint32_t &pinv_o
     return redc32((uint64_t)u * r2, p, pinv);
 }
 
+// kmod32 for NP primes at once: NP independent Montgomery chains share each
+// limb read and hide each other's multiply latency.
+template <int NP>
+PG_HD void kmod32_multi(const uint32_t *limbs, int n, const uint32_t *p, uint32_t *r,
+                        uint32_t *pinv, uint32_t *r2) {
+    uint32_t u[NP];
+    bool lazy = true;
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        pinv[k] = neg_inv32(p[k]);
+        const uint32_t r1 = (0u - p[k]) % p[k];
+        r2[k] = (uint32_t)(((uint64_t)r1 * r1) % p[k]);
+        u[k] = 0;
+        lazy = lazy && p[k] < 0x80000000u;
+    }
+    if (lazy) {
+        for (int i = n - 1; i >= 0; i--) {
+            const uint32_t l = limbs[i];
+#pragma unroll
+            for (int k = 0; k < NP; k++) u[k] = redc32_lazy((uint64_t)u[k] * r2[k] + l, p[k], pinv[k]);
+        }
+#pragma unroll
+        for (int k = 0; k < NP; k++)
+            if (u[k] >= p[k]) u[k] -= p[k];
+    } else {
+        for (int i = n - 1; i >= 0; i--) {
+            const uint32_t l = limbs[i];
+#pragma unroll
+            for (int k = 0; k < NP; k++) u[k] = redc32((uint64_t)u[k] * r2[k] + l, p[k], pinv[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < NP; k++) r[k] = redc32((uint64_t)u[k] * r2[k], p[k], pinv[k]);
+}
+
 // (r * M + sl) mod p with the Montgomery constants of p (M < 3 * 2^32, sl < p).
 PG_HD uint32_t start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p, uint32_t pinv,
                        uint32_t r2) {

@@ -18,6 +18,7 @@ namespace {
 
 constexpr int kKmodThreads = 256;
 constexpr int kMaxSharedLimbs = 12288;  // 48 KiB
+constexpr int kPrimesPerThread = 4;     // 32-bit primes
 
 template <bool kWide>
 __global__ void __launch_bounds__(kKmodThreads)
@@ -31,15 +32,26 @@ __global__ void __launch_bounds__(kKmodThreads)
     __syncthreads();
     const uint32_t *limbs = in_shared ? s_limbs : klimbs;
     const uint64_t n = min((uint64_t)*count, max_count);  // never past the list's capacity
-    const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (idx >= n) return;
-    const uint64_t p = base + off[idx];
     if (!kWide) {
-        uint32_t pinv, r2;
-        uint32_t r = kmod32(limbs, nlimbs, (uint32_t)p, pinv, r2);
-        ((uint32_t *)r_out)[idx] = r;
-        ((uint32_t *)t0_out)[idx] = start32(r, mstart, sl, (uint32_t)p, pinv, r2);
+        // kPrimesPerThread consecutive primes per thread, interleaved chains
+        const uint64_t idx0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kPrimesPerThread;
+        if (idx0 >= n) return;
+        uint32_t p[kPrimesPerThread], r[kPrimesPerThread], pinv[kPrimesPerThread],
+            r2[kPrimesPerThread];
+#pragma unroll
+        for (int k = 0; k < kPrimesPerThread; k++)
+            p[k] = idx0 + k < n ? (uint32_t)(base + off[idx0 + k]) : 3u;  // pad with a prime
+        kmod32_multi<kPrimesPerThread>(limbs, nlimbs, p, r, pinv, r2);
+#pragma unroll
+        for (int k = 0; k < kPrimesPerThread; k++) {
+            if (idx0 + k >= n) break;
+            ((uint32_t *)r_out)[idx0 + k] = r[k];
+            ((uint32_t *)t0_out)[idx0 + k] = start32(r[k], mstart, sl, p[k], pinv[k], r2[k]);
+        }
     } else {
+        const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (idx >= n) return;
+        const uint64_t p = base + off[idx];
         const uint64_t r = kmod64(limbs, nlimbs, p);
         const double inv_p = 1.0 / (double)p;
         uint64_t mm = mstart % p;
@@ -65,7 +77,9 @@ cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, con
                         const unsigned long long *d_count, uint64_t max_count, uint64_t mstart,
                         uint32_t sl, void *d_r, void *d_t0, bool wide, cudaStream_t stream) {
     if (max_count == 0) return cudaSuccess;
-    uint64_t blocks = (max_count + kKmodThreads - 1) / kKmodThreads;
+    const uint64_t per_thread = wide ? 1 : kPrimesPerThread;
+    const uint64_t threads = (max_count + per_thread - 1) / per_thread;
+    uint64_t blocks = (threads + kKmodThreads - 1) / kKmodThreads;
     size_t smem = nlimbs <= kMaxSharedLimbs ? (size_t)nlimbs * sizeof(uint32_t) : 0;
     if (wide)
         kmod_kernel<true><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(

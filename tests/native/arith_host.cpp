@@ -144,6 +144,12 @@ uint64_t ah_kmod(const uint32_t *limbs, int n, uint64_t q) {
     return pg::kmod64(limbs, n, q);
 }
 
+// Four primes through the interleaved chains of the K mod p kernel.
+void ah_kmod4(const uint32_t *limbs, int n, const uint32_t *q4, uint32_t *out4) {
+    uint32_t pinv[4], r2[4];
+    pg::kmod32_multi<4>(limbs, n, q4, out4, pinv, r2);
+}
+
 // (r * M + sl) mod p through the Montgomery path of the K mod p kernel.
 uint32_t ah_start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p) {
     uint32_t pinv = pg::neg_inv32(p);

@@ -210,6 +210,22 @@ def test_kmod_vs_oracle(ah, P, d):
         assert ah.ah_kmod(arr, len(limbs), q) == pgo.k_mod(limbs, q)
 
 
+def test_kmod4_interleaved(ah):
+    ah.ah_kmod4.restype = None
+    ah.ah_kmod4.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int,
+                            ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32)]
+    rng = random.Random(21)
+    for P, d in [(503, 210), (1511, 2190)]:
+        limbs = pgo.build_k(P, d)
+        arr = (ctypes.c_uint32 * len(limbs))(*limbs)
+        for lo, hi in [(P + 1, 10**5), (2**30, 2**31), (2**31, 2**32)]:
+            for _ in range(20):
+                qs = [_rand_prime(rng, lo, hi) for _ in range(4)]
+                out = (ctypes.c_uint32 * 4)()
+                ah.ah_kmod4(arr, len(limbs), (ctypes.c_uint32 * 4)(*qs), out)
+                assert list(out) == [pgo.k_mod(limbs, q) for q in qs]
+
+
 def test_kmod_against_python_bignum(built):
     from sympy import primorial
 
