@@ -75,6 +75,7 @@ struct HostJob {
     uint64_t small_threshold = 0, medium_threshold = 0, prime_limit = 0;
     uint64_t s1 = 0;
     uint64_t primes_to_P = 0;  // primes <= min(P, prime_limit), 2 included
+    pg::WalkParams walk{};
     std::string filename;
 };
 
@@ -227,6 +228,27 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     h.mmask.assign((minc + 31) / 32, 0);
     for (uint64_t mi = 0; mi < minc; mi++)
         if (m_ok[mi]) h.mmask[mi >> 5] |= 1u << (mi & 31);
+    // parity-reduced large-prime walk (pg::WalkParams)
+    pg::WalkParams &w = h.walk;
+    if (d_even) {
+        w.stride = 2;
+        w.mi_base = (ms & 1) ? 0 : 1;  // valid m are odd
+        w.jmax = minc > w.mi_base ? (minc - w.mi_base + 1) / 2 : 0;
+        w.c_add = SL / 2;
+        w.w = 2 * (SL / 2) + 1;
+        w.xc = 2 * (SL / 2) + SL;
+        w.odd_d = 0;
+    } else {
+        const uint32_t hi = (SL - 1) / 2, lo = (SL + 1) / 2;  // X' in [-lo, hi]
+        w.stride = 1;
+        w.mi_base = 0;
+        w.jmax = minc;
+        w.c_add = hi;
+        w.w = hi + lo + 1;
+        w.xc = 2 * hi + 1 + SL;
+        w.odd_d = 1;
+    }
+    w.m0 = ms + w.mi_base;
     return PGS_OK;
 }
 
@@ -416,6 +438,7 @@ pg::JobDev job_dev(pgs_prepared *pr) {
     j.row_of_mi = pr->row_of_mi.as<int32_t>();
     j.col_of_x = pr->col_of_x.as<int32_t>();
     j.comp = pr->comp.as<uint32_t>();
+    j.walk = h.walk;
     return j;
 }
 
@@ -662,8 +685,8 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
         CK(mark(b));
         span(PGS_STAGE_PRIMES, a, b);
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), pr->sp_lo,
-                           pr->sp.as<uint32_t>(), misc + 1, pr->sp_bound, h.job.mstart,
-                           h.job.sieve_length, pr->sr.p, pr->sp_t0.p, false, s));
+                           pr->sp.as<uint32_t>(), misc + 1, pr->sp_bound, nullptr, pr->sr.p,
+                           pr->sp_t0.p, false, s));
         CK(mark(a));
         span(PGS_STAGE_KMOD, b, a);
         pr->launches += 2;
@@ -682,8 +705,8 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
         CK(pg::sieve_window(ctx->base, win.lo, win.hi, ctx->win_off.as<uint32_t>(), win.bound, cnt, s));
         CK(mark(e_b));
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
-                           ctx->win_off.as<uint32_t>(), cnt, win.bound, h.job.mstart,
-                           h.job.sieve_length, ctx->win_r.p, ctx->win_t0.p, win.wide, s));
+                           ctx->win_off.as<uint32_t>(), cnt, win.bound, &h.walk, ctx->win_r.p,
+                           ctx->win_t0.p, win.wide, s));
         CK(mark(e_c));
         CK(pg::large_window(job, win.lo, ctx->win_off.as<uint32_t>(), cnt, win.bound, ctx->win_r.p,
                             ctx->win_t0.p, win.wide, pr->mmask.as<uint32_t>(),

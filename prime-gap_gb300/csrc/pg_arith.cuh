@@ -378,6 +378,36 @@ PG_HD ThreeGap<T> three_gap(T p, T a, T w) {
 }
 
 // ---------------------------------------------------------------------------
+// parity-reduced walk of a large prime
+//
+// Only odd m*K + X can be prime.  For d even, valid m are odd and K is odd,
+// so X must be even: with m = m0 + 2j and X = 2X', p | m*K + X becomes
+// X' == -m*K/2 (mod p), a walk in j whose step is r = K mod p again
+// (2 * (1/2) = 1), over a window of 2*floor(SL/2)+1 values of X'.  For d odd,
+// K is even and X must be odd: X = 2X' + 1 gives X' == -(m*K + 1)/2, a walk
+// in m with step r/2 mod p.  Either way the residue of walk index 0 is
+// t0 = (r/2 * m0 + c) mod p, with c = floor(SL/2) (d even) or
+// floor((SL-1)/2) + (p+1)/2 (d odd), and a residue Y < w is the hit
+// X = xc - 2*Y - SL.  This removes the hits on even m*K + X before they are
+// generated: 4x fewer walk steps for d even, 2x for d odd.
+struct WalkParams {
+    uint32_t stride;   // mi = mi_base + stride * j
+    uint32_t mi_base;
+    uint64_t jmax;     // walk indices j in [0, jmax)
+    uint32_t w;        // hits: residue Y < w
+    uint32_t xc;       // offset index x = X + SL = xc - 2*Y
+    uint32_t c_add;    // floor(SL/2) (d even) or floor((SL-1)/2) (d odd)
+    uint32_t odd_d;    // 1 when d is odd: step r/2, constant c_add + (p+1)/2
+    uint64_t m0;       // m of walk index 0
+};
+
+// r / 2 mod p for odd p.
+PG_HD uint32_t half_mod(uint32_t r, uint32_t p) {
+    return (r & 1u) ? (uint32_t)(((uint64_t)r + p) >> 1) : (r >> 1);
+}
+PG_HD uint64_t half_mod(uint64_t r, uint64_t p) { return (r & 1u) ? ((r + p) >> 1) : (r >> 1); }
+
+// ---------------------------------------------------------------------------
 // first entry and three-gap data in one continued-fraction pass
 //
 // The subtractive continued fraction of three_gap is a Rauzy induction of the

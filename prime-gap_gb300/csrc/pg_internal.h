@@ -6,6 +6,8 @@
 #include <string>
 #include <vector>
 
+#include "pg_arith.cuh"
+
 namespace pg {
 
 // ---- prime sieve (pg_primes.cu) -------------------------------------------
@@ -38,12 +40,14 @@ cudaError_t sieve_window(const BasePrimes &bp, uint64_t lo, uint64_t hi, uint32_
 
 // ---- K mod p (pg_kmod.cu) ---------------------------------------------------
 
-// For primes base + off[i] (i < *d_count), write r[i] = K mod p and
-// t0[i] = (r * mstart + SL) mod p.  Primes below 2^32 use 32-bit words
-// (d_r32/d_t032), others 64-bit (d_r64/d_t064).  K limbs on the device.
+// For primes base + off[i] (i < *d_count): with walk == nullptr write
+// r[i] = K mod p; otherwise write the parity-reduced walk step (r or r/2) and
+// its start residue t0[i] (see WalkParams).  Primes below 2^32 use 32-bit
+// words, others 64-bit (wide).  K limbs on the device.
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
-                        const unsigned long long *d_count, uint64_t max_count, uint64_t mstart,
-                        uint32_t sl, void *d_r, void *d_t0, bool wide, cudaStream_t stream);
+                        const unsigned long long *d_count, uint64_t max_count,
+                        const WalkParams *walk, void *d_r, void *d_t0, bool wide,
+                        cudaStream_t stream);
 
 // K mod q for an explicit list of 32-bit primes (d-primes, tests).
 cudaError_t kmod_list32(const uint32_t *d_klimbs, int nlimbs, const uint32_t *d_q, uint32_t n,
@@ -63,6 +67,7 @@ struct JobDev {
     const int32_t *row_of_mi;  // minc entries, -1 if gcd(m, d) > 1
     const int32_t *col_of_x;   // 2*SL+1 entries, -1 if not a live offset
     uint32_t *comp;            // rows * pitch words
+    WalkParams walk;           // parity-reduced large-prime walk
 };
 
 struct HeavyPrime;

@@ -24,7 +24,7 @@ template <bool kWide>
 __global__ void __launch_bounds__(kKmodThreads)
     kmod_kernel(const uint32_t *__restrict__ klimbs, int nlimbs, uint64_t base,
                 const uint32_t *__restrict__ off, const unsigned long long *count,
-                uint64_t max_count, uint64_t mstart, uint32_t sl, void *r_out, void *t0_out) {
+                uint64_t max_count, WalkParams walk, int with_walk, void *r_out, void *t0_out) {
     extern __shared__ uint32_t s_limbs[];
     const bool in_shared = nlimbs <= kMaxSharedLimbs;
     if (in_shared)
@@ -45,19 +45,29 @@ __global__ void __launch_bounds__(kKmodThreads)
 #pragma unroll
         for (int k = 0; k < kPrimesPerThread; k++) {
             if (idx0 + k >= n) break;
-            ((uint32_t *)r_out)[idx0 + k] = r[k];
-            ((uint32_t *)t0_out)[idx0 + k] = start32(r[k], mstart, sl, p[k], pinv[k], r2[k]);
+            if (!with_walk) {
+                ((uint32_t *)r_out)[idx0 + k] = r[k];
+                continue;
+            }
+            const uint32_t rh = half_mod(r[k], p[k]);
+            const uint32_t c = walk.c_add + (walk.odd_d ? (p[k] >> 1) + 1 : 0u);
+            ((uint32_t *)r_out)[idx0 + k] = walk.odd_d ? rh : r[k];
+            ((uint32_t *)t0_out)[idx0 + k] = start32(rh, walk.m0, c, p[k], pinv[k], r2[k]);
         }
     } else {
         const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
         if (idx >= n) return;
         const uint64_t p = base + off[idx];
         const uint64_t r = kmod64(limbs, nlimbs, p);
-        const double inv_p = 1.0 / (double)p;
-        uint64_t mm = mstart % p;
-        uint64_t t = mulmod_u64(r, mm, p, inv_p) + sl;
+        if (!with_walk) {
+            ((uint64_t *)r_out)[idx] = r;
+            return;
+        }
+        const uint64_t rh = half_mod(r, p);
+        const uint64_t c = walk.c_add + (walk.odd_d ? (p >> 1) + 1 : 0ull);
+        uint64_t t = mulmod_u64(rh, walk.m0 % p, p, 1.0 / (double)p) + c;
         if (t >= p) t -= p;
-        ((uint64_t *)r_out)[idx] = r;
+        ((uint64_t *)r_out)[idx] = walk.odd_d ? rh : r;
         ((uint64_t *)t0_out)[idx] = t;
     }
 }
@@ -74,8 +84,11 @@ __global__ void __launch_bounds__(kKmodThreads)
 }  // namespace
 
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
-                        const unsigned long long *d_count, uint64_t max_count, uint64_t mstart,
-                        uint32_t sl, void *d_r, void *d_t0, bool wide, cudaStream_t stream) {
+                        const unsigned long long *d_count, uint64_t max_count,
+                        const WalkParams *walk, void *d_r, void *d_t0, bool wide,
+                        cudaStream_t stream) {
+    const WalkParams wp = walk ? *walk : WalkParams{};
+    const int with_walk = walk != nullptr;
     if (max_count == 0) return cudaSuccess;
     const uint64_t per_thread = wide ? 1 : kPrimesPerThread;
     const uint64_t threads = (max_count + per_thread - 1) / per_thread;
@@ -83,10 +96,10 @@ cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, con
     size_t smem = nlimbs <= kMaxSharedLimbs ? (size_t)nlimbs * sizeof(uint32_t) : 0;
     if (wide)
         kmod_kernel<true><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(
-            d_klimbs, nlimbs, base, d_off, d_count, max_count, mstart, sl, d_r, d_t0);
+            d_klimbs, nlimbs, base, d_off, d_count, max_count, wp, with_walk, d_r, d_t0);
     else
         kmod_kernel<false><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(
-            d_klimbs, nlimbs, base, d_off, d_count, max_count, mstart, sl, d_r, d_t0);
+            d_klimbs, nlimbs, base, d_off, d_count, max_count, wp, with_walk, d_r, d_t0);
     return cudaGetLastError();
 }
 

@@ -1,5 +1,6 @@
 // Large-prime phase: for every prime p > 4*SL+2, every m in
-// [mstart, mstart+minc) and offset X in [-SL, SL] with p | m*K + X.
+// [mstart, mstart+minc) and offset X in [-SL, SL] with p | m*K + X and
+// m*K + X odd (the parity-reduced walk of WalkParams, pg_arith.cuh).
 //
 // Replaces method2_large_primes (combined_sieve.cpp:1763-2011) and the
 // enumeration modulo_search_euclid_all_large (modulo_search.cpp:339-376).
@@ -36,14 +37,16 @@ constexpr uint64_t kDirectSteps = 24;
 constexpr uint32_t kItemSteps = 64;
 constexpr uint64_t kHeavySteps = 16384;
 
+// A walk hit (j, Y) is m = mstart + mi_base + stride*j, x = X + SL = xc - 2Y.
 struct Marker {
     const JobDev &job;
     const uint32_t *mmask;  // valid m bits (shared or global)
     const uint32_t *xmask;  // live offset bits (shared or global)
-    __device__ __forceinline__ void operator()(uint64_t mi, uint32_t y) const {
-        const uint32_t x = job.two_sl - y;
-        if (!((mmask[mi >> 5] >> (mi & 31)) & 1u)) return;
+    __device__ __forceinline__ void operator()(uint64_t j, uint32_t y) const {
+        const uint32_t x = job.walk.xc - 2 * y;
         if (!((xmask[x >> 5] >> (x & 31)) & 1u)) return;
+        const uint64_t mi = job.walk.mi_base + job.walk.stride * j;
+        if (!((mmask[mi >> 5] >> (mi & 31)) & 1u)) return;
         const int32_t row = __ldg(&job.row_of_mi[mi]);
         const int32_t col = __ldg(&job.col_of_x[x]);
         atomicOr(&job.comp[(uint64_t)row * job.pitch + ((uint32_t)col >> 5)], 1u << (col & 31));
@@ -103,8 +106,8 @@ __global__ void __launch_bounds__(kLargeThreads)
     load_masks(job, g_mmask, g_xmask, masks_in_shared, s_masks, mmask, xmask);
     const Marker mark{job, mmask, xmask};
     const uint64_t n = min((uint64_t)*count, max_count);
-    const T w = (T)job.two_sl + 1;
-    const uint64_t minc = job.minc;
+    const T w = (T)job.walk.w;
+    const uint64_t minc = job.walk.jmax;  // the walk runs over j, not mi
 
     for (;;) {
         if (threadIdx.x == 0) s_group = atomicAdd(group_ctr, 1ull);
@@ -186,7 +189,7 @@ __global__ void __launch_bounds__(kLargeThreads)
     load_masks(job, g_mmask, g_xmask, masks_in_shared, s_masks, mmask, xmask);
     const Marker mark{job, mmask, xmask};
     const uint64_t nh = min((uint64_t)*heavy_count, (uint64_t)heavy_cap);
-    const uint32_t w = job.two_sl + 1;
+    const uint32_t w = job.walk.w;
     for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
         const HeavyPrime hp = heavy[h];
         const ThreeGap<uint64_t> g{hp.kp, hp.up, hp.kn, hp.dn};
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(kLargeThreads)
             uint32_t y;
             uint64_t mi;
             rotation_at<uint64_t>(hp.mi0, hp.y0, g, it * kItemSteps, y, mi);
-            rotation_walk<uint64_t>(mi, y, g, w, job.minc, kItemSteps, mark);
+            rotation_walk<uint64_t>(mi, y, g, w, job.walk.jmax, kItemSteps, mark);
         }
     }
 }

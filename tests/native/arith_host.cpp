@@ -123,6 +123,50 @@ size_t ah_hits_items(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint6
     return c.n;
 }
 
+// Parity-reduced walk of one prime (the large-prime kernel's walk): hits as
+// (mi, x = X + SL) for d even (odd_d = 0) or d odd (odd_d = 1).
+size_t ah_hits_parity(uint64_t M, uint32_t minc, uint32_t SL, uint64_t p, uint64_t r, int odd_d,
+                      uint32_t *mi_out, uint64_t *x_out, size_t cap) {
+    pg::WalkParams w{};
+    if (!odd_d) {
+        w.stride = 2;
+        w.mi_base = (M & 1) ? 0 : 1;
+        w.jmax = minc > w.mi_base ? (minc - w.mi_base + 1) / 2 : 0;
+        w.c_add = SL / 2;
+        w.w = 2 * (SL / 2) + 1;
+        w.xc = 2 * (SL / 2) + SL;
+    } else {
+        uint32_t hi = (SL - 1) / 2, lo = (SL + 1) / 2;
+        w.stride = 1;
+        w.jmax = minc;
+        w.c_add = hi;
+        w.w = hi + lo + 1;
+        w.xc = 2 * hi + 1 + SL;
+        w.odd_d = 1;
+    }
+    w.m0 = M + w.mi_base;
+    struct C {
+        const pg::WalkParams &w;
+        uint32_t *mi_out;
+        uint64_t *x_out;
+        size_t cap, n;
+        void operator()(uint64_t j, uint64_t y) {
+            if (n < cap) mi_out[n] = (uint32_t)(w.mi_base + w.stride * j), x_out[n] = w.xc - 2 * y;
+            n++;
+        }
+    } c{w, mi_out, x_out, cap, 0};
+    unsigned __int128 rh = pg::half_mod(r, p);
+    uint64_t cc = w.c_add + (w.odd_d ? (p >> 1) + 1 : 0);
+    uint64_t t0 = (uint64_t)((rh * (w.m0 % p) + cc) % p);
+    uint64_t a = w.odd_d ? (uint64_t)rh : r;
+    if (p < 0xFFFFFFFFull)
+        pg::enumerate_hits_cf<uint32_t>((uint32_t)p, (uint32_t)a, (uint32_t)t0, 0, w.jmax,
+                                        (uint32_t)(w.w - 1), c);
+    else
+        pg::enumerate_hits_cf<uint64_t>(p, a, t0, 0, w.jmax, (uint64_t)(w.w - 1), c);
+    return c.n;
+}
+
 // first_entry: out = {t, y, kp, up, kn, dn}
 void ah_first_entry(uint64_t p, uint64_t a, uint64_t w, uint64_t y0, uint64_t *out6) {
     if (p < 0xFFFFFFFFull) {

@@ -163,6 +163,41 @@ def test_hits_items_vs_all_large(ah, bits):
             assert _hits_items(ah, M, max_mi, SL, p, r, direct, item) == want
 
 
+@pytest.mark.parametrize("odd_d", [0, 1])
+@pytest.mark.parametrize("bits", [18, 26, 31, 33, 40])
+def test_parity_walk_vs_all_large(ah, bits, odd_d):
+    """The parity-reduced walk yields exactly the hits with m*K + X odd."""
+    ah.ah_hits_parity.restype = ctypes.c_size_t
+    ah.ah_hits_parity.argtypes = [ctypes.c_uint64, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                  ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32),
+                                  ctypes.POINTER(ctypes.c_uint64), ctypes.c_size_t]
+    rng = random.Random(bits * 10 + odd_d)
+    cap = 1 << 18
+    mi = (ctypes.c_uint32 * cap)()
+    xs = (ctypes.c_uint64 * cap)()
+    for _ in range(60):
+        SL = rng.choice([500, 501, 4000, 4001, 20000, 40000])
+        lo = max(4 * SL + 3, 2 ** (bits - 1))
+        p = _rand_prime(rng, lo, max(2 * lo, 2**bits))
+        r = rng.randrange(1, p)
+        M = rng.randrange(1, 10**10)
+        minc = rng.choice([1, 2, 17, 1000, 100000])
+        n = ah.ah_hits_parity(M, minc, SL, p, r, odd_d, mi, xs, cap)
+        got = sorted(zip(mi[:n], xs[:n]))
+        want = []
+        for m_i, t in pgo.all_large(M, minc, SL, p, r):
+            x = 2 * SL - t
+            X = x - SL
+            m = M + m_i
+            if odd_d:  # K even: m*K + X odd iff X odd
+                ok = X % 2 == 1
+            else:  # K odd, valid m odd: X even
+                ok = m % 2 == 1 and X % 2 == 0
+            if ok:
+                want.append((m_i, x))
+        assert got == sorted(want), (SL, p, r, M, minc)
+
+
 def test_first_entry_brute(ah):
     """First k >= 0 with (y0 + k*a) mod p < w, and the three-gap data, by brute force."""
     rng = random.Random(13)
