@@ -240,14 +240,17 @@ def run_gb300(args, rank, world, local):
 
     # end to end through the public call (tables up, text down, every step)
     for _ in range(min(args.warmup, 2)):
-        sieve.method2(spec)
+        sieve.method2_view(spec).close()
     barrier()
     e2e_s = []
     e2e_stats: dict = {}
+    out_len = 0
     for _ in range(args.steps):
         t = time.perf_counter()
-        out = sieve.method2(spec, e2e_stats)
+        view = sieve.method2_view(spec, e2e_stats)  # text is in host memory on return
         e2e_s.append(time.perf_counter() - t)
+        out_len = len(view)
+        view.close()
     barrier()
     e2e_total = sum(e2e_s)
     if dist:
@@ -258,7 +261,7 @@ def run_gb300(args, rank, world, local):
     h2d = (4 * ((plan["k_bits"] + 31) // 32) + 4 * spec.minc + 4 * (2 * spec.sieve_length + 1)
            + 4 * plan["valid_ms"] + 2 * spec.sieve_length)
     e2e = {"value": pairs_per_step * world * args.steps / e2e_total, "unit": "pairs/s",
-           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(len(out) + 64),
+           "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(out_len + 64),
            "ms_per_step": e2e_total / args.steps * 1e3}
 
     # roofline of the dominant kernel (large-prime marks): integer-pipe bound.
@@ -266,7 +269,7 @@ def run_gb300(args, rank, world, local):
     s1 = 4 * spec.sieve_length + 2
     n_windows = max(1, stats["prime_limit"] // (1 << 30) - (s1 + 1) // (1 << 30) + 1)
     large_ms = stage_sum.get("large", 0.0) / (args.steps * n_windows)
-    model_ops = large_kernel_model_ops(spec, stats) / n_windows
+    model_ops = large_kernel_model_ops(spec, stats, plan) / n_windows
     achieved = model_ops / (large_ms * 1e-3) if large_ms else None
     traffic = _traffic_per_launch()
     roofline = {"kernel": "large_kernel<uint32_t>", "bound": "int", "achieved": achieved,
@@ -301,20 +304,23 @@ def run_gb300(args, rank, world, local):
     return 0
 
 
-def large_kernel_model_ops(spec, stats) -> float:
-    """Model of the large-prime phase's integer work (ops per job), from the
-    expected hit count sum_p minc*(2SL+1)/p over the phase's primes (Mertens:
-    minc*(2SL+1)*(ln ln P1 - ln ln P0)) at 6 ops per hit, plus one Euclid
-    search and one continued fraction per prime at 8 ops per level with
-    0.843*ln(p/(2SL+1)) levels each (Heilbronn's mean)."""
+def large_kernel_model_ops(spec, stats, plan) -> float:
+    """Model of the large-prime phase's integer work (ops per job).
+
+    The parity-reduced walk visits minc*(2SL+1)/p / 4 hits per prime for d
+    even (only odd m and even X) and / 2 for d odd; summed over the phase's
+    primes with Mertens' estimate that is minc*(2SL+1)*(ln ln P1 - ln ln P0)/4.
+    6 integer ops per hit, plus one continued fraction per prime at 8 ops per
+    level over 0.843*ln(p/w) levels (Heilbronn's mean)."""
     import math
 
     w = 2 * spec.sieve_length + 1
     p0 = 4 * spec.sieve_length + 2
     p1 = stats["prime_limit"]
-    hits = spec.minc * w * (math.log(math.log(p1)) - math.log(math.log(p0)))
+    reduce = 4 if spec.d % 2 == 0 else 2
+    hits = spec.minc * w * (math.log(math.log(p1)) - math.log(math.log(p0))) / reduce
     nprimes = stats["primes"]
-    levels = 2 * 0.843 * math.log(max(p1 / 2, p0) / w)
+    levels = 0.843 * math.log(max(p1 / 2, p0) / (w / 2))
     return 6 * hits + 8 * levels * nprimes
 
 

@@ -466,9 +466,9 @@ pg::RowsDev rows_dev(pgs_prepared *pr) {
     return rd;
 }
 
-uint32_t rows_per_block(uint32_t nb) {
+uint32_t rows_per_block(uint32_t nb, int compression) {
     uint32_t nbw = (nb + 31) / 32;
-    uint32_t r = 98304u / (nbw * 4u);
+    uint32_t r = 98304u / (nbw * 4u * (compression == 2 ? 2u : 1u));
     if (r > 32) r = 32;
     if (r < 1) r = 1;
     return r;
@@ -560,10 +560,6 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     if (!ctx || !job || !out) return PGS_EINVAL;
     std::lock_guard<std::mutex> g(ctx->mu);
     *out = nullptr;
-    if (job->compression == 2) {
-        ctx->err = "bitcompressed output is not supported by this build";
-        return PGS_EINVAL;
-    }
     auto *pr = new pgs_prepared();
     pr->ctx = ctx;
     for (DevBuf *b : pr->all()) b->pool = &ctx->dpool;
@@ -722,7 +718,7 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
     }
     // rows, text
     CK(mark(a));
-    CK(pg::rows_extract(rd, rows_per_block(h.nb), s));
+    CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression), s));
     CK(mark(b));
     span(PGS_STAGE_ROWS, a, b);
     CK(pg::scan_u64(pr->row_bytes.as<uint64_t>(), pr->offsets.as<uint64_t>(), pr->misc.as<uint64_t>(),

@@ -49,6 +49,8 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
     const uint32_t nrows = min(rows_per_block, job.rows - r0);
     uint32_t *s_mi = sh + (size_t)rows_per_block * nbw;  // rows_per_block entries
     uint32_t *s_h0 = s_mi + rows_per_block;               // rows_per_block * kMaxDPrimes
+    // bitcompressed rows also need the d-prime pattern alone
+    uint32_t *s_pat = s_h0 + (size_t)rows_per_block * kMaxDPrimes;
     const uint32_t sl = job.sl, x_par = rd.x_par;
 
     for (uint32_t j = threadIdx.x; j < nrows; j += blockDim.x) s_mi[j] = rd.valid_mi[r0 + j];
@@ -74,6 +76,7 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
             if (o < 32) word |= word_pattern(q) << o;
         }
         sh[j * nbw + w] = word;
+        if (rd.compression == 2) s_pat[j * nbw + w] = word;
     }
     __syncthreads();
 
@@ -102,6 +105,62 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const uint32_t H = job.half_cols;
     const uint32_t lt_mask = (1u << lane) - 1;
+    if (rd.compression == 2) {
+        // Bitcompressed rows (combined_sieve.cpp:1327-1385): over the offsets
+        // in increasing X that are coprime to K and to every prime of d
+        // (live and not in the d-prime pattern), the composite flags, 7 per
+        // byte with bit 7 set.  The byte list goes to the row's list slot.
+        for (uint32_t j = warp; j < nrows; j += nwarps) {
+            const uint32_t row = r0 + j;
+            const uint32_t *grow = job.comp + (uint64_t)row * job.pitch;
+            uint8_t *bytes = (uint8_t *)(rd.lists + (uint64_t)row * 2 * H);
+            uint32_t unk = 0, nbytes = 0, bit = 0, b = 0x80;
+            for (uint32_t side = 0; side < 2; side++) {
+                for (uint32_t h0 = 0; h0 < H; h0 += 32) {
+                    // side 0 walks its columns backwards: increasing X
+                    const uint32_t k = h0 + lane;
+                    bool fc = false, composite = false;
+                    if (k < H) {
+                        const uint32_t h = side ? k : H - 1 - k;
+                        const uint32_t d = rd.dist[h];
+                        const uint32_t x = side ? sl + d : sl - d;
+                        const uint32_t hx = (x - x_par) >> 1;
+                        const uint32_t pat = (s_pat[j * nbw + (hx >> 5)] >> (hx & 31)) & 1;
+                        const uint32_t sb = (sh[j * nbw + (hx >> 5)] >> (hx & 31)) & 1;
+                        const uint32_t col = side * job.side_pad + h;
+                        const uint32_t gb = (grow[col >> 5] >> (col & 31)) & 1;
+                        fc = !pat;
+                        composite = (sb | gb) != 0;
+                    }
+                    const uint32_t fcm = __ballot_sync(0xFFFFFFFFu, fc);
+                    const uint32_t cm = __ballot_sync(0xFFFFFFFFu, composite);
+                    unk += __popc(fcm & ~cm);
+                    if (lane == 0) {
+                        uint32_t m = fcm;
+                        while (m) {
+                            const uint32_t i = __ffs(m) - 1;
+                            m &= m - 1;
+                            b |= ((cm >> i) & 1u) << bit;
+                            if (++bit == 7) {
+                                bytes[nbytes++] = (uint8_t)b;
+                                b = 0x80;
+                                bit = 0;
+                            }
+                        }
+                    }
+                }
+            }
+            if (lane == 0) {
+                if (bit) bytes[nbytes++] = (uint8_t)b;
+                rd.counts[2 * row] = unk;
+                rd.counts[2 * row + 1] = nbytes;
+                const uint64_t m = job.mstart + s_mi[j];
+                // "m : U B || <bytes>\n"
+                rd.row_bytes[row] = ndigits(m) + ndigits(unk) + ndigits(nbytes) + 9 + nbytes;
+            }
+        }
+        return;
+    }
     for (uint32_t j = warp; j < nrows; j += nwarps) {
         const uint32_t row = r0 + j;
         const uint32_t *grow = job.comp + (uint64_t)row * job.pitch;
@@ -265,6 +324,27 @@ __global__ void __launch_bounds__(256) format_kernel(RowsDev rd, const uint64_t 
     if (offsets[row] + rd.row_bytes[row] > rd.text_cap) return;
     char *out = text + offsets[row];
     uint64_t pos = 0;
+    if (rd.compression == 2) {
+        const uint64_t m = job.mstart + rd.valid_mi[row];
+        if (lane == 0) {
+            pos += put_u64(out + pos, m);
+            out[pos++] = ' ';
+            out[pos++] = ':';
+            out[pos++] = ' ';
+            pos += put_u64(out + pos, cnt[0]);
+            out[pos++] = ' ';
+            pos += put_u64(out + pos, cnt[1]);
+            out[pos++] = ' ';
+            out[pos++] = '|';
+            out[pos++] = '|';
+            out[pos++] = ' ';
+        }
+        pos = __shfl_sync(0xFFFFFFFFu, pos, 0);
+        const uint8_t *bytes = (const uint8_t *)list;
+        for (uint32_t i = lane; i < cnt[1]; i += 32) out[pos + i] = (char)bytes[i];
+        if (lane == 0) out[pos + cnt[1]] = '\n';
+        return;
+    }
     if (lane == 0) {
         uint64_t m = job.mstart + rd.valid_mi[row];
         pos += put_u64(out + pos, m);
@@ -327,7 +407,7 @@ cudaError_t rows_extract(const RowsDev &rd, uint32_t rows_per_block, cudaStream_
     if (rd.job.rows == 0) return cudaSuccess;
     if (rd.nd > (uint32_t)kMaxDPrimes) return cudaErrorInvalidValue;
     const uint32_t nbw = (rd.nb + 31) / 32;
-    size_t smem = ((size_t)rows_per_block * nbw + rows_per_block +
+    size_t smem = ((size_t)rows_per_block * nbw * (rd.compression == 2 ? 2 : 1) + rows_per_block +
                    (size_t)rows_per_block * kMaxDPrimes) * sizeof(uint32_t);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(rows_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,

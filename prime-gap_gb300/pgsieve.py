@@ -223,6 +223,15 @@ class Sieve:
             self.lib.pgs_result_free(ctypes.byref(res))
         return data
 
+    def method2_view(self, job: JobSpec, stats: dict | None = None) -> "ResultView":
+        """Like method2 but without copying: a view of the library-owned host
+        buffer, valid until the returned object is closed."""
+        res = Result()
+        self._check(self.lib.pgs_method2(self.h, ctypes.byref(job.c()), ctypes.byref(res)))
+        if stats is not None:
+            stats.update(_result_stats(res))
+        return ResultView(self.lib, res)
+
     def prepare(self, job: JobSpec) -> "Prepared":
         h = ctypes.c_void_p()
         self._check(self.lib.pgs_prepare(self.h, ctypes.byref(job.c()), ctypes.byref(h)))
@@ -263,6 +272,33 @@ class Sieve:
                                             ctypes.byref(n)))
         k = min(n.value, cap)
         return list(zip(mi[:k], md[:k]))
+
+
+class ResultView:
+    """Zero-copy access to a pgs_result's text (freed by close())."""
+
+    def __init__(self, lib, res: Result):
+        self.lib, self.res = lib, res
+        self.view = (ctypes.c_char * res.text_len).from_address(
+            ctypes.cast(res.text, ctypes.c_void_p).value or 0) if res.text_len else b""
+
+    def __len__(self) -> int:
+        return self.res.text_len
+
+    def bytes(self) -> bytes:
+        return bytes(self.view)
+
+    def close(self) -> None:
+        if self.res is not None:
+            self.lib.pgs_result_free(ctypes.byref(self.res))
+            self.res = None
+            self.view = b""
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
 
 
 class Prepared:

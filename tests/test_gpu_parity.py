@@ -15,7 +15,7 @@ import pgsieve
 
 pytestmark = pytest.mark.gpu
 
-GOLDEN_NAMES = ["fn1", "fn1_rle", "fn2", "config1", "small_d1", "small_d2", "small_d30",
+GOLDEN_NAMES = ["fn1", "fn1_rle", "fn1_bitcompressed", "small_bc_d30", "fn2", "config1", "small_d1", "small_d2", "small_d30",
                 "small_d2190", "small_d30030", "small_d7_odd", "small_d73_sl_odd",
                 "small_rle_d210", "edge_maxprime_1M", "ext_907_210"]
 
@@ -63,7 +63,7 @@ def _random_jobs(n, seed):
         minc = rng.choice([1, 7, 100, 1000, 3000])
         mstart = rng.randrange(1, 10**9)
         max_prime = rng.choice([1, 3, 10, 40]) * 1_000_000
-        comp = rng.choice([0, 0, 1])
+        comp = rng.choice([0, 0, 1, 2])
         jobs.append((P, d, mstart, minc, SL, max_prime, comp))
     return jobs
 
