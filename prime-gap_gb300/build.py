@@ -31,7 +31,8 @@ NVCC_FLAGS = ARCH + [
     "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall",
     f"-I{INCLUDE}", f"-I{CSRC}",
 ]
-CU_SOURCES = ["pg_primes.cu", "pg_kmod.cu", "pg_large.cu", "pg_rows.cu", "pg_tools.cu", "pg_api.cu"]
+CU_SOURCES = ["pg_primes.cu", "pg_kmod.cu", "pg_large.cu", "pg_rows.cu", "pg_tools.cu", "pg_host.cu",
+              "pg_api.cu"]
 
 LIB = BUILD / "libpgsieve.so"
 CLI = BUILD / "combined_sieve"

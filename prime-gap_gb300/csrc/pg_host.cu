@@ -1,0 +1,285 @@
+// Host-side job derivation and buffer helpers of libpgsieve (see pg_host.h).
+//
+// A job's tables follow prime_gap_parallel's setup (combined_sieve.cpp:2014-2200):
+// validation (gap_common.cpp:1007-1094, combined_sieve.cpp:86-135),
+// K = P#/d (gap_common.cpp:116-121), valid m (gap_common.cpp:307-342),
+// offsets coprime to K (combined_sieve.cpp:1143-1169) and the thresholds of
+// calculate_thresholds_method2 (gap_common.cpp:345-375).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+
+#include "pg_host.h"
+
+namespace pgh {
+
+bool is_prime_u64(uint64_t n) {
+    if (n < 2) return false;
+    if (n % 2 == 0) return n == 2;
+    for (uint64_t t = 3; t * t <= n; t += 2)
+        if (n % t == 0) return false;
+    return true;
+}
+
+uint64_t next_prime_above(uint64_t n) {
+    uint64_t c = n + 1;
+    while (!is_prime_u64(c)) c++;
+    return c;
+}
+
+std::vector<uint32_t> primes_upto(uint32_t n) {
+    std::vector<uint32_t> out;
+    if (n < 2) return out;
+    std::vector<uint8_t> comp(n + 1, 0);
+    for (uint32_t i = 2; i <= n; i++) {
+        if (comp[i]) continue;
+        out.push_back(i);
+        for (uint64_t j = (uint64_t)i * i; j <= n; j += i) comp[j] = 1;
+    }
+    return out;
+}
+
+uint32_t ndigits(uint64_t v) {
+    uint32_t n = 1;
+    while (v >= 10) v /= 10, n++;
+    return n;
+}
+
+int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
+    h.job = j;
+    // Args::argparse validation (gap_common.cpp:1007-1094)
+    if (j.p < 2) {
+        err = "p must be a prime >= 2";
+        return PGS_EABORT;  // get_sieve_primes(P).back() == P asserts
+    }
+    if (j.p >= 10000000u || !is_prime_u64(j.p)) {
+        err = "p# not prime";
+        return PGS_EINVAL;
+    }
+    if (j.mstart == 0) return err = "mstart must be greater than 0", PGS_EINVAL;
+    if (j.minc == 0) return err = "minc must be greater than 0", PGS_EINVAL;
+    if (j.minc >= 0x7FFFFFFFull) return err = "minc must be less than 2B", PGS_EINVAL;
+    if (j.mstart + j.minc > 10000000001ull) return err = "mstart + minc must be <= 10e9", PGS_EINVAL;
+    if (j.max_prime > 40000000000000ull) return err = "max_prime > 40 Trillion not supported", PGS_EINVAL;
+    if (j.max_prime < 3) return err = "max_prime must be set", PGS_EINVAL;
+    if (j.d == 0) return err = "d must be greater than 0", PGS_EINVAL;
+    if (j.compression < 0 || j.compression > 2) return err = "unknown compression", PGS_EINVAL;
+    const uint32_t P = j.p, D = j.d, SL = j.sieve_length;
+    std::vector<uint32_t> pp = primes_upto(P);
+    if (SL % 500 != 0) {
+        for (uint32_t q : pp) {
+            if (q >= P) break;
+            if (SL % q == 0 && D % q != 0) return err = "SL not coprime", PGS_EINVAL;
+        }
+    }
+    // combined_sieve.cpp:97-103
+    if ((uint64_t)SL < 6ull * P || (uint64_t)SL > 22ull * P)
+        return err = "sieve_length outside [6P, 22P]", PGS_EINVAL;
+    if (2ull * SL + 1 > 4000000ull) return err = "sieve_length too large for this build", PGS_EINVAL;
+
+    // K = P#/d (gap_common.cpp:116-121); d must divide P#
+    {
+        uint32_t rest = D;
+        std::vector<uint32_t> limbs{1};
+        for (uint32_t q : pp) {
+            if (rest % q == 0) {
+                rest /= q;
+                if (q != 2) h.dq.push_back(q);
+                continue;
+            }
+            uint64_t carry = 0;
+            for (auto &l : limbs) {
+                uint64_t t = (uint64_t)l * q + carry;
+                l = (uint32_t)t;
+                carry = t >> 32;
+            }
+            if (carry) limbs.push_back((uint32_t)carry);
+        }
+        if (rest != 1) return err = "d does not divide P#", PGS_EABORT;
+        if (limbs.size() == 1 && limbs[0] <= 1) return err = "K <= 1", PGS_EABORT;
+        h.klimbs = limbs;
+        h.kbits = 32 * (uint32_t)(limbs.size() - 1) + (32 - __builtin_clz(limbs.back()));
+    }
+    const bool d_even = (D % 2) == 0;
+    h.x_par = d_even ? (SL & 1) : ((SL + 1) & 1);
+    h.nb = h.x_par == 0 ? SL + 1 : SL;
+
+    // valid m (gap_common.cpp:307-342)
+    const uint64_t minc = j.minc, ms = j.mstart;
+    std::vector<uint8_t> m_ok(minc, 1);
+    for (uint32_t q : pp) {
+        if (D % q) continue;
+        uint64_t first = (q - (ms % q)) % q;
+        for (uint64_t mi = first; mi < minc; mi += q) m_ok[mi] = 0;
+    }
+    uint64_t valid = 0;
+    for (uint64_t mi = 0; mi < minc; mi++) valid += m_ok[mi];
+    if (valid == 0) return err = "no m coprime to d", PGS_EABORT;
+
+    // offsets coprime to K (combined_sieve.cpp:1143-1169)
+    const uint32_t interval = 2 * SL + 1;
+    std::vector<uint8_t> coprime(interval, 1);
+    for (uint32_t q : pp) {
+        if (D % q == 0) continue;
+        for (uint32_t x = SL % q; x < interval; x += q) coprime[x] = 0;
+    }
+    uint64_t cc = 0;
+    for (uint32_t x = 0; x < interval; x++) cc += coprime[x];
+    h.coprime_x = cc;
+
+    // calculate_thresholds_method2 (gap_common.cpp:345-375), same conversions
+    {
+        uint32_t sieve_interval = interval;
+        double sm = std::log(8.0) * (double)minc / (double)valid;
+        float SMALL_MULT = (float)(8.0 > sm ? 8.0 : sm);
+        uint64_t MEDIUM_CROSSOVER_SMALL = (uint64_t)(1.0 * (double)cc * (double)minc / (double)valid);
+        float M_PER_P_CROSSOVER = (float)(1.0 * (double)minc * sieve_interval / (double)cc);
+        double mm = 0.65 * std::log2((double)(M_PER_P_CROSSOVER / (float)cc));
+        float MEDIUM_MULT = (float)(1.9 > mm ? 1.9 : mm);
+        uint64_t MEDIUM_CROSSOVER_SEARCH = (uint64_t)(MEDIUM_MULT * M_PER_P_CROSSOVER);
+        uint64_t SMALL = (uint64_t)SMALL_MULT * sieve_interval;
+        if (MEDIUM_CROSSOVER_SMALL < SMALL) SMALL = MEDIUM_CROSSOVER_SMALL;
+        if (SMALL < sieve_interval) SMALL = sieve_interval + 1;
+        uint64_t MEDIUM = SMALL > MEDIUM_CROSSOVER_SEARCH ? SMALL : MEDIUM_CROSSOVER_SEARCH;
+        if (MEDIUM > j.max_prime) MEDIUM = j.max_prime;
+        h.small_threshold = SMALL;
+        h.medium_threshold = MEDIUM;
+        // combined_sieve.cpp:2080-2082 asserts MEDIUM >= SMALL
+        if (MEDIUM < SMALL) return err = "MEDIUM_THRESHOLD < SMALL_THRESHOLD", PGS_EABORT;
+    }
+    // Primes sieved by the reference: all primes < max_prime, and the small
+    // phase runs through the first prime above SMALL_THRESHOLD
+    // (combined_sieve.cpp:1481-1504).
+    {
+        uint64_t small_last = next_prime_above(h.small_threshold);
+        h.prime_limit = std::max<uint64_t>(j.max_prime - 1, small_last);
+    }
+    h.s1 = 4ull * SL + 2;
+    for (uint32_t q : pp)
+        if (q <= h.prime_limit) h.primes_to_P++;
+
+    char fn[256];
+    snprintf(fn, sizeof fn, "unknowns/%u_%u_%llu_%llu_s%u_l%lluM.txt", P, D,
+             (unsigned long long)ms, (unsigned long long)minc, SL,
+             (unsigned long long)(j.max_prime / 1000000ull));
+    h.filename = fn;
+    if (!tables) return PGS_OK;
+
+    h.valid_mi.reserve(valid);
+    h.row_of_mi.assign(minc, -1);
+    for (uint64_t mi = 0; mi < minc; mi++) {
+        if (m_ok[mi]) {
+            h.row_of_mi[mi] = (int32_t)h.valid_mi.size();
+            h.valid_mi.push_back((uint32_t)mi);
+        }
+    }
+    // live offsets: coprime to K and of the parity that makes m*K + X odd
+    for (uint32_t dd = 1; dd <= SL; dd++) {
+        uint32_t x = SL + dd;
+        if (coprime[x] && ((x & 1) == h.x_par)) h.dist.push_back(dd);
+    }
+    h.H = (uint32_t)h.dist.size();
+    h.Hp = (h.H + 31) / 32 * 32;
+    h.pitch = (2 * h.Hp / 32 + 3) / 4 * 4;
+    if (h.pitch == 0) h.pitch = 4;
+    h.col_of_x.assign(interval, -1);
+    h.xmask.assign((interval + 31) / 32, 0);
+    for (uint32_t i = 0; i < h.H; i++) {
+        uint32_t lo = SL - h.dist[i], hi = SL + h.dist[i];
+        h.col_of_x[lo] = (int32_t)i;
+        h.col_of_x[hi] = (int32_t)(h.Hp + i);
+        h.xmask[lo >> 5] |= 1u << (lo & 31);
+        h.xmask[hi >> 5] |= 1u << (hi & 31);
+    }
+    h.mmask.assign((minc + 31) / 32, 0);
+    for (uint64_t mi = 0; mi < minc; mi++)
+        if (m_ok[mi]) h.mmask[mi >> 5] |= 1u << (mi & 31);
+    // parity-reduced large-prime walk (pg::WalkParams)
+    pg::WalkParams &w = h.walk;
+    if (d_even) {
+        w.stride = 2;
+        w.mi_base = (ms & 1) ? 0 : 1;  // valid m are odd
+        w.jmax = minc > w.mi_base ? (minc - w.mi_base + 1) / 2 : 0;
+        w.c_add = SL / 2;
+        w.w = 2 * (SL / 2) + 1;
+        w.xc = 2 * (SL / 2) + SL;
+        w.odd_d = 0;
+    } else {
+        const uint32_t hi = (SL - 1) / 2, lo = (SL + 1) / 2;  // X' in [-lo, hi]
+        w.stride = 1;
+        w.mi_base = 0;
+        w.jmax = minc;
+        w.c_add = hi;
+        w.w = hi + lo + 1;
+        w.xc = 2 * hi + 1 + SL;
+        w.odd_d = 1;
+    }
+    w.m0 = ms + w.mi_base;
+    return PGS_OK;
+}
+
+PinnedPool &pinned_pool() {
+    static PinnedPool *pool = new PinnedPool();  // lives until exit
+    return *pool;
+}
+
+int fail(pgs_ctx *ctx, cudaError_t e, const char *what) {
+    if (ctx) {
+        ctx->err = std::string(what) + ": " + cudaGetErrorString(e);
+    }
+    if (e == cudaErrorMemoryAllocation) return PGS_ENOMEM;
+    return PGS_ECUDA;
+}
+
+pg::JobDev job_dev(pgs_prepared *pr) {
+    const HostJob &h = pr->hj;
+    pg::JobDev j{};
+    j.mstart = h.job.mstart;
+    j.minc = (uint32_t)h.job.minc;
+    j.sl = h.job.sieve_length;
+    j.two_sl = 2 * h.job.sieve_length;
+    j.rows = (uint32_t)h.valid_mi.size();
+    j.half_cols = h.H;
+    j.side_pad = h.Hp;
+    j.pitch = h.pitch;
+    j.row_of_mi = pr->row_of_mi.as<int32_t>();
+    j.col_of_x = pr->col_of_x.as<int32_t>();
+    j.comp = pr->comp.as<uint32_t>();
+    j.walk = h.walk;
+    return j;
+}
+
+pg::RowsDev rows_dev(pgs_prepared *pr) {
+    const HostJob &h = pr->hj;
+    pg::RowsDev rd{};
+    rd.job = job_dev(pr);
+    rd.x_par = h.x_par;
+    rd.nb = h.nb;
+    rd.valid_mi = pr->valid_mi.as<uint32_t>();
+    rd.dist = pr->dist.as<uint32_t>();
+    rd.nd = (uint32_t)h.dq.size();
+    rd.dq = pr->dq.as<uint32_t>();
+    rd.dr = pr->dr.as<uint32_t>();
+    rd.sp_base = (uint32_t)pr->sp_lo;
+    rd.sp = pr->sp.as<uint32_t>();
+    rd.sr = pr->sr.as<uint32_t>();
+    rd.sp_range = pr->misc.as<unsigned long long>() + 1;
+    rd.sp_cap = pr->sp_bound;
+    rd.text_cap = pr->text_cap;
+    rd.lists = pr->lists.as<uint32_t>();
+    rd.counts = pr->counts.as<uint32_t>();
+    rd.row_bytes = pr->row_bytes.as<uint64_t>();
+    rd.compression = h.job.compression;
+    return rd;
+}
+
+uint32_t rows_per_block(uint32_t nb, int compression) {
+    uint32_t nbw = (nb + 31) / 32;
+    uint32_t r = 98304u / (nbw * 4u * (compression == 2 ? 2u : 1u));
+    if (r > 32) r = 32;
+    if (r < 1) r = 1;
+    return r;
+}
+
+}  // namespace pgh

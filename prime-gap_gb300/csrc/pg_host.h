@@ -1,0 +1,214 @@
+// Host-side internals of libpgsieve shared by the plain path (pg_api.cu) and
+// the batched / served paths (pg_batch.cu): derived job tables, device and
+// pinned buffer pools, the context and the prepared-job objects.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "pg_internal.h"
+#include "pgsieve.h"
+
+namespace pgh {
+
+constexpr uint64_t kWindowSpan = 1ull << 30;
+
+bool is_prime_u64(uint64_t n);
+uint64_t next_prime_above(uint64_t n);
+std::vector<uint32_t> primes_upto(uint32_t n);
+uint32_t ndigits(uint64_t v);
+
+struct HostJob {
+    pgs_job job{};
+    std::vector<uint32_t> klimbs;
+    uint32_t kbits = 0;
+    std::vector<uint32_t> valid_mi;
+    std::vector<int32_t> row_of_mi;
+    std::vector<int32_t> col_of_x;
+    std::vector<uint32_t> dist;
+    std::vector<uint32_t> dq;  // odd primes dividing d
+    std::vector<uint32_t> mmask, xmask;  // valid-m and live-offset bitmasks
+    uint32_t x_par = 0, nb = 0, H = 0, Hp = 0, pitch = 0;
+    uint64_t coprime_x = 0;
+    uint64_t small_threshold = 0, medium_threshold = 0, prime_limit = 0;
+    uint64_t s1 = 0;
+    uint64_t primes_to_P = 0;  // primes <= min(P, prime_limit), 2 included
+    pg::WalkParams walk{};
+    std::string filename;
+};
+
+// Validate a job (the reference's argparse/main rules) and derive its tables;
+// tables=false stops after the scalar parameters.
+int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables);
+
+// Device allocations recycled across jobs on one context: a job's buffers
+// (several GB for the larger configs) are returned here instead of freed, so
+// repeated jobs pay no cudaMalloc/cudaFree.
+struct DevicePool {
+    std::mutex mu;
+    std::vector<std::pair<void *, size_t>> free_list;
+    cudaError_t get(size_t n, void **p, size_t *cap) {
+        {
+            std::lock_guard<std::mutex> g(mu);
+            size_t best = (size_t)-1;
+            for (size_t i = 0; i < free_list.size(); i++)
+                if (free_list[i].second >= n &&
+                    (best == (size_t)-1 || free_list[i].second < free_list[best].second))
+                    best = i;
+            // reuse only blocks that are not much larger than the request
+            if (best != (size_t)-1 && free_list[best].second <= 2 * n + (1u << 20)) {
+                *p = free_list[best].first;
+                *cap = free_list[best].second;
+                free_list.erase(free_list.begin() + best);
+                return cudaSuccess;
+            }
+        }
+        cudaError_t e = cudaMalloc(p, n);
+        if (e == cudaErrorMemoryAllocation) {
+            trim();  // give cached blocks back and retry once
+            e = cudaMalloc(p, n);
+        }
+        if (e == cudaSuccess) *cap = n;
+        return e;
+    }
+    void put(void *p, size_t cap) {
+        std::lock_guard<std::mutex> g(mu);
+        free_list.push_back({p, cap});
+    }
+    void trim() {
+        std::lock_guard<std::mutex> g(mu);
+        for (auto &b : free_list) cudaFree(b.first);
+        free_list.clear();
+    }
+};
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t n = 0;
+    DevicePool *pool = nullptr;
+    cudaError_t ensure(size_t bytes) {
+        if (bytes <= n && p) return cudaSuccess;
+        release();
+        size_t want = bytes < 256 ? 256 : bytes;
+        if (pool) return pool->get(want, &p, &n);
+        cudaError_t e = cudaMalloc(&p, want);
+        if (e == cudaSuccess) n = want;
+        return e;
+    }
+    void release() {
+        if (p) {
+            if (pool) pool->put(p, n);
+            else cudaFree(p);
+        }
+        p = nullptr;
+        n = 0;
+    }
+    template <typename T>
+    T *as() const {
+        return (T *)p;
+    }
+};
+
+struct PinnedPool {
+    std::mutex mu;
+    std::vector<std::pair<char *, size_t>> free_list;
+    char *get(size_t n, size_t *cap) {
+        std::lock_guard<std::mutex> g(mu);
+        size_t best = (size_t)-1;
+        for (size_t i = 0; i < free_list.size(); i++)
+            if (free_list[i].second >= n && (best == (size_t)-1 || free_list[i].second < free_list[best].second))
+                best = i;
+        if (best != (size_t)-1) {
+            auto e = free_list[best];
+            free_list.erase(free_list.begin() + best);
+            *cap = e.second;
+            return e.first;
+        }
+        char *p = nullptr;
+        size_t want = n < 4096 ? 4096 : n;
+        if (cudaMallocHost(&p, want) != cudaSuccess) return nullptr;
+        *cap = want;
+        return p;
+    }
+    void put(char *p, size_t cap) {
+        std::lock_guard<std::mutex> g(mu);
+        free_list.push_back({p, cap});
+    }
+};
+
+PinnedPool &pinned_pool();
+
+struct PinnedOwner {
+    size_t cap;
+};
+
+struct Window {
+    uint64_t lo, hi, bound;
+    bool wide;
+};
+
+}  // namespace pgh
+
+struct PrimeTable;
+struct Lane;
+
+struct pgs_ctx {
+    int device = 0;
+    cudaStream_t own = nullptr;
+    cudaStream_t stream = nullptr;
+    std::mutex mu;
+    std::string err;
+    pg::BasePrimes base;
+    pgh::DevBuf win_off, win_r, win_t0, large_ctr, heavy;
+    pgh::DevicePool dpool;
+};
+
+struct pgs_prepared {
+    pgs_ctx *ctx = nullptr;
+    pgh::HostJob hj;
+    std::vector<pgh::Window> windows;
+    uint64_t sp_lo = 0, sp_hi = 0, sp_bound = 0;
+    uint64_t text_cap = 0;
+    uint64_t win_bound = 0;
+    pgh::DevBuf klimbs, row_of_mi, col_of_x, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0, mmask, xmask;
+    pgh::DevBuf lists, counts, row_bytes, offsets, scan_tmp, misc, text;
+    std::vector<cudaEvent_t> events;
+    std::vector<std::pair<int, std::pair<int, int>>> spans;  // stage, (ev a, ev b)
+    double ms_setup = 0;
+    uint64_t launches = 0;
+    bool ran = false;
+    std::vector<pgh::DevBuf *> all() {
+        return {&klimbs, &row_of_mi, &col_of_x, &valid_mi, &dist,   &dq,     &dr,
+                &comp,   &sp,        &sr,       &sp_t0,    &lists,  &counts, &row_bytes,
+                &offsets, &scan_tmp, &misc,     &text,     &mmask,  &xmask};
+    }
+    ~pgs_prepared() {
+        for (auto e : events) cudaEventDestroy(e);
+        for (pgh::DevBuf *b : all()) b->release();
+    }
+};
+
+namespace pgh {
+
+int fail(pgs_ctx *ctx, cudaError_t e, const char *what);
+
+#define CK(x)                                              \
+    do {                                                   \
+        cudaError_t e_ = (x);                              \
+        if (e_ != cudaSuccess) return fail(ctx, e_, #x);   \
+    } while (0)
+
+template <typename T>
+cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t s) {
+    cudaError_t e = b.ensure(v.size() * sizeof(T));
+    if (e || v.empty()) return e;
+    return cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s);
+}
+
+pg::JobDev job_dev(pgs_prepared *pr);
+pg::RowsDev rows_dev(pgs_prepared *pr);
+uint32_t rows_per_block(uint32_t nb, int compression);
+
+}  // namespace pgh

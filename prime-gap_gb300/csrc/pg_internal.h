@@ -38,14 +38,28 @@ uint64_t prime_count_bound(uint64_t lo, uint64_t hi);
 cudaError_t sieve_window(const BasePrimes &bp, uint64_t lo, uint64_t hi, uint32_t *d_out,
                          uint64_t cap, unsigned long long *d_count, cudaStream_t stream);
 
+// Sorted odd primes of [lo, hi] (hi - lo < 2^32) as offsets from lo; count
+// to *d_count.  d_tmp: sieve_sorted_tmp_bytes(lo, hi) bytes of scratch.
+uint64_t sieve_sorted_tmp_bytes(uint64_t lo, uint64_t hi);
+cudaError_t sieve_window_sorted(const BasePrimes &bp, uint64_t lo, uint64_t hi, uint32_t *d_out,
+                                uint64_t cap, unsigned long long *d_count, void *d_tmp,
+                                cudaStream_t stream);
+// d_out = {begin, end}: the indexes of the sorted list base + off[0..count)
+// whose values lie in [lo_val, hi_val].
+cudaError_t find_range(const uint32_t *d_off, uint64_t count, uint64_t base, uint64_t lo_val,
+                       uint64_t hi_val, unsigned long long *d_out, cudaStream_t stream);
+// d_out = {a, b} written by a kernel (capturable in a CUDA graph).
+cudaError_t set_pair(unsigned long long *d_out, uint64_t a, uint64_t b, cudaStream_t stream);
+
 // ---- K mod p (pg_kmod.cu) ---------------------------------------------------
 
-// For primes base + off[i] (i < *d_count): with walk == nullptr write
+// For primes base + off[i], i in [d_range[0], d_range[1]) (device values,
+// at most max_count of them): with walk == nullptr write
 // r[i] = K mod p; otherwise write the parity-reduced walk step (r or r/2) and
 // its start residue t0[i] (see WalkParams).  Primes below 2^32 use 32-bit
 // words, others 64-bit (wide).  K limbs on the device.
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
-                        const unsigned long long *d_count, uint64_t max_count,
+                        const unsigned long long *d_range, uint64_t max_count,
                         const WalkParams *walk, void *d_r, void *d_t0, bool wide,
                         cudaStream_t stream);
 
@@ -83,7 +97,7 @@ constexpr size_t kHeavyPrimeBytes = 40;
 
 // d_mmask: valid-m bitmask (minc bits); d_xmask: live-offset bitmask (2SL+1 bits).
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
-                         const unsigned long long *d_count, uint64_t max_count, const void *d_r,
+                         const unsigned long long *d_range, uint64_t max_count, const void *d_r,
                          const void *d_t0, bool wide, const uint32_t *d_mmask,
                          const uint32_t *d_xmask, LargeScratch scratch, cudaStream_t stream);
 
@@ -103,8 +117,8 @@ struct RowsDev {
     uint32_t sp_base;
     const uint32_t *sp;
     const uint32_t *sr;
-    const unsigned long long *sp_count;
-    uint64_t sp_cap;           // capacity of sp / sr
+    const unsigned long long *sp_range;  // {begin, end} into sp (device)
+    uint64_t sp_cap;           // capacity of sr (and of the range)
     uint64_t text_cap;         // capacity of the text buffer
     // outputs
     uint32_t *lists;       // rows * 2H distances (low side then high side)

@@ -23,7 +23,7 @@ constexpr int kPrimesPerThread = 4;     // 32-bit primes
 template <bool kWide>
 __global__ void __launch_bounds__(kKmodThreads)
     kmod_kernel(const uint32_t *__restrict__ klimbs, int nlimbs, uint64_t base,
-                const uint32_t *__restrict__ off, const unsigned long long *count,
+                const uint32_t *__restrict__ off, const unsigned long long *range,
                 uint64_t max_count, WalkParams walk, int with_walk, void *r_out, void *t0_out) {
     extern __shared__ uint32_t s_limbs[];
     const bool in_shared = nlimbs <= kMaxSharedLimbs;
@@ -31,7 +31,10 @@ __global__ void __launch_bounds__(kKmodThreads)
         for (int i = threadIdx.x; i < nlimbs; i += blockDim.x) s_limbs[i] = klimbs[i];
     __syncthreads();
     const uint32_t *limbs = in_shared ? s_limbs : klimbs;
-    const uint64_t n = min((uint64_t)*count, max_count);  // never past the list's capacity
+    // primes off[range[0] .. range[1]), never more than the list's capacity
+    const uint64_t begin = range[0];
+    const uint64_t n = min((uint64_t)(range[1] - begin), max_count);
+    off += begin;
     if (!kWide) {
         // kPrimesPerThread consecutive primes per thread, interleaved chains
         const uint64_t idx0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kPrimesPerThread;
@@ -84,7 +87,7 @@ __global__ void __launch_bounds__(kKmodThreads)
 }  // namespace
 
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
-                        const unsigned long long *d_count, uint64_t max_count,
+                        const unsigned long long *d_range, uint64_t max_count,
                         const WalkParams *walk, void *d_r, void *d_t0, bool wide,
                         cudaStream_t stream) {
     const WalkParams wp = walk ? *walk : WalkParams{};
@@ -96,10 +99,10 @@ cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, con
     size_t smem = nlimbs <= kMaxSharedLimbs ? (size_t)nlimbs * sizeof(uint32_t) : 0;
     if (wide)
         kmod_kernel<true><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(
-            d_klimbs, nlimbs, base, d_off, d_count, max_count, wp, with_walk, d_r, d_t0);
+            d_klimbs, nlimbs, base, d_off, d_range, max_count, wp, with_walk, d_r, d_t0);
     else
         kmod_kernel<false><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(
-            d_klimbs, nlimbs, base, d_off, d_count, max_count, wp, with_walk, d_r, d_t0);
+            d_klimbs, nlimbs, base, d_off, d_range, max_count, wp, with_walk, d_r, d_t0);
     return cudaGetLastError();
 }
 

@@ -94,7 +94,7 @@ __device__ __forceinline__ void load_masks(const JobDev &job, const uint32_t *g_
 template <typename T>
 __global__ void __launch_bounds__(kLargeThreads)
     large_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
-                 const unsigned long long *count, uint64_t max_count, const T *__restrict__ r_in,
+                 const unsigned long long *range, uint64_t max_count, const T *__restrict__ r_in,
                  const T *__restrict__ t0_in, const uint32_t *__restrict__ g_mmask,
                  const uint32_t *__restrict__ g_xmask, int masks_in_shared,
                  unsigned long long *group_ctr, HeavyPrime *heavy, unsigned long long *heavy_count,
@@ -105,7 +105,8 @@ __global__ void __launch_bounds__(kLargeThreads)
     const uint32_t *mmask, *xmask;
     load_masks(job, g_mmask, g_xmask, masks_in_shared, s_masks, mmask, xmask);
     const Marker mark{job, mmask, xmask};
-    const uint64_t n = min((uint64_t)*count, max_count);
+    const uint64_t n = min((uint64_t)(range[1] - range[0]), max_count);
+    off += range[0];
     const T w = (T)job.walk.w;
     const uint64_t minc = job.walk.jmax;  // the walk runs over j, not mi
 
@@ -208,7 +209,7 @@ __global__ void __launch_bounds__(kLargeThreads)
 uint32_t heavy_capacity() { return 1u << 20; }
 
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
-                         const unsigned long long *d_count, uint64_t max_count, const void *d_r,
+                         const unsigned long long *d_range, uint64_t max_count, const void *d_r,
                          const void *d_t0, bool wide, const uint32_t *d_mmask,
                          const uint32_t *d_xmask, LargeScratch scratch, cudaStream_t stream) {
     if (max_count == 0) return cudaSuccess;
@@ -237,11 +238,11 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
     if (blocks > groups) blocks = groups;
     if (wide)
         large_kernel<uint64_t><<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            job, base, d_off, d_count, max_count, (const uint64_t *)d_r, (const uint64_t *)d_t0,
+            job, base, d_off, d_range, max_count, (const uint64_t *)d_r, (const uint64_t *)d_t0,
             d_mmask, d_xmask, in_shared, group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
     else
         large_kernel<uint32_t><<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            job, base, d_off, d_count, max_count, (const uint32_t *)d_r, (const uint32_t *)d_t0,
+            job, base, d_off, d_range, max_count, (const uint32_t *)d_r, (const uint32_t *)d_t0,
             d_mmask, d_xmask, in_shared, group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
     if ((e = cudaGetLastError())) return e;
     if ((e = prep(heavy_kernel))) return e;

@@ -14,6 +14,7 @@
 // consumer treats primes independently.
 #include "pg_internal.h"
 
+#include <algorithm>
 #include <cmath>
 
 namespace pg {
@@ -263,6 +264,98 @@ __global__ void __launch_bounds__(1024) small_primes_kernel(uint32_t *out, uint3
     if (threadIdx.x == 0) *count = s_total;
 }
 
+// Sorted sieve, pass 1: bitmap of primes and count per segment.
+__global__ void __launch_bounds__(kSieveThreads)
+    seg_bitmap_kernel(uint64_t win_hi, uint64_t first_odd, const uint32_t *base, uint32_t nbase,
+                      uint32_t *gbits, uint64_t *seg_counts) {
+    __shared__ uint32_t bits[kSegWords];
+    __shared__ uint32_t s_cnt;
+    const uint64_t seg_lo = first_odd + (uint64_t)blockIdx.x * kSegSpan;
+    uint64_t seg_hi = seg_lo + kSegSpan - 2;
+    if (seg_hi > win_hi) seg_hi = win_hi;
+    if (threadIdx.x == 0) s_cnt = 0;
+    sieve_segment(bits, seg_lo, seg_hi, base, nbase);
+    const uint32_t nbits = (uint32_t)((seg_hi - seg_lo) / 2 + 1);
+    uint32_t cnt = 0;
+    for (uint32_t w = threadIdx.x; w < kSegWords; w += blockDim.x) {
+        const uint32_t b0 = w * 32;
+        uint32_t valid = 0;
+        if (b0 < nbits) valid = (nbits - b0 >= 32) ? 0xFFFFFFFFu : ((1u << (nbits - b0)) - 1);
+        const uint32_t primes = ~bits[w] & valid;
+        gbits[(uint64_t)blockIdx.x * kSegWords + w] = primes;
+        cnt += __popc(primes);
+    }
+    cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&s_cnt, cnt);
+    __syncthreads();
+    if (threadIdx.x == 0) seg_counts[blockIdx.x] = s_cnt;
+}
+
+// Sorted sieve, pass 2: each segment writes its primes (offsets from win_lo)
+// at its prefix-sum position, in increasing order.
+__global__ void __launch_bounds__(kSieveThreads)
+    seg_extract_kernel(uint64_t win_lo, uint64_t first_odd, const uint32_t *gbits,
+                       const uint64_t *seg_offsets, uint32_t *out, uint64_t cap) {
+    __shared__ uint32_t s_scan[kSieveThreads];
+    const uint64_t seg_lo = first_odd + (uint64_t)blockIdx.x * kSegSpan;
+    const uint32_t per = kSegWords / kSieveThreads;
+    const uint32_t *g = gbits + (uint64_t)blockIdx.x * kSegWords + threadIdx.x * per;
+    uint32_t words[kSegWords / kSieveThreads];
+    uint32_t cnt = 0;
+#pragma unroll
+    for (uint32_t k = 0; k < per; k++) {
+        words[k] = g[k];
+        cnt += __popc(words[k]);
+    }
+    s_scan[threadIdx.x] = cnt;
+    __syncthreads();
+    for (int off = 1; off < kSieveThreads; off <<= 1) {
+        uint32_t v = threadIdx.x >= (uint32_t)off ? s_scan[threadIdx.x - off] : 0;
+        __syncthreads();
+        s_scan[threadIdx.x] += v;
+        __syncthreads();
+    }
+    uint64_t pos = seg_offsets[blockIdx.x] + s_scan[threadIdx.x] - cnt;
+#pragma unroll
+    for (uint32_t k = 0; k < per; k++) {
+        uint32_t m = words[k];
+        const uint32_t b0 = (threadIdx.x * per + k) * 32;
+        while (m) {
+            const uint32_t b = __ffs(m) - 1;
+            m &= m - 1;
+            if (pos < cap) out[pos] = (uint32_t)(seg_lo + 2ull * (b0 + b) - win_lo);
+            pos++;
+        }
+    }
+}
+
+// [begin, end) of the sorted list base + off[0..count) within [lo_val, hi_val].
+__global__ void range_kernel(const uint32_t *off, uint64_t count, uint64_t base, uint64_t lo_val,
+                             uint64_t hi_val, unsigned long long *out) {
+    if (threadIdx.x != 0) return;
+    uint64_t a = 0, b = count;
+    while (a < b) {  // first >= lo_val
+        uint64_t mid = (a + b) >> 1;
+        if (base + off[mid] < lo_val) a = mid + 1;
+        else b = mid;
+    }
+    uint64_t c = a, d = count;
+    while (c < d) {  // first > hi_val
+        uint64_t mid = (c + d) >> 1;
+        if (base + off[mid] <= hi_val) c = mid + 1;
+        else d = mid;
+    }
+    out[0] = a;
+    out[1] = hi_val >= lo_val ? c : a;
+}
+
+__global__ void set_pair_kernel(unsigned long long *out, unsigned long long a, unsigned long long b) {
+    if (threadIdx.x == 0) {
+        out[0] = a;
+        out[1] = b;
+    }
+}
+
 uint64_t isqrt64(uint64_t n) {
     uint64_t r = (uint64_t)std::sqrt((double)n);
     while (r * r > n) r--;
@@ -342,6 +435,44 @@ cudaError_t sieve_window(const BasePrimes &bp, uint64_t lo, uint64_t hi, uint32_
     uint64_t nseg = (hi - first_odd) / kSegSpan + 1;
     sieve_window_kernel<<<(unsigned)nseg, kSieveThreads, 0, stream>>>(
         lo, hi, first_odd, bp.d_primes, bp.count, d_out, cap, d_count);
+    return cudaGetLastError();
+}
+
+uint64_t sieve_sorted_tmp_bytes(uint64_t lo, uint64_t hi) {
+    uint64_t first_odd = std::max<uint64_t>(lo | 1, 3);
+    if (first_odd > hi) return 256;
+    uint64_t nseg = (hi - first_odd) / kSegSpan + 1;
+    return nseg * kSegWords * 4 + nseg * 16 + scan_tmp_words(nseg) * 8 + 256;
+}
+
+cudaError_t sieve_window_sorted(const BasePrimes &bp, uint64_t lo, uint64_t hi, uint32_t *d_out,
+                                uint64_t cap, unsigned long long *d_count, void *d_tmp,
+                                cudaStream_t stream) {
+    if (hi > bp.covers || hi - lo >= (1ull << 32)) return cudaErrorInvalidValue;
+    uint64_t first_odd = std::max<uint64_t>(lo | 1, 3);
+    if (first_odd > hi) return cudaMemsetAsync(d_count, 0, 8, stream);
+    const uint64_t nseg = (hi - first_odd) / kSegSpan + 1;
+    uint32_t *gbits = (uint32_t *)d_tmp;
+    uint64_t *seg_counts = (uint64_t *)(gbits + nseg * kSegWords);
+    uint64_t *seg_offsets = seg_counts + nseg;
+    uint64_t *scan_tmp = seg_offsets + nseg;
+    seg_bitmap_kernel<<<(unsigned)nseg, kSieveThreads, 0, stream>>>(hi, first_odd, bp.d_primes,
+                                                                    bp.count, gbits, seg_counts);
+    cudaError_t e = scan_u64(seg_counts, seg_offsets, (uint64_t *)d_count, nseg, scan_tmp, stream);
+    if (e) return e;
+    seg_extract_kernel<<<(unsigned)nseg, kSieveThreads, 0, stream>>>(lo, first_odd, gbits,
+                                                                     seg_offsets, d_out, cap);
+    return cudaGetLastError();
+}
+
+cudaError_t find_range(const uint32_t *d_off, uint64_t count, uint64_t base, uint64_t lo_val,
+                       uint64_t hi_val, unsigned long long *d_out, cudaStream_t stream) {
+    range_kernel<<<1, 32, 0, stream>>>(d_off, count, base, lo_val, hi_val, d_out);
+    return cudaGetLastError();
+}
+
+cudaError_t set_pair(unsigned long long *d_out, uint64_t a, uint64_t b, cudaStream_t stream) {
+    set_pair_kernel<<<1, 32, 0, stream>>>(d_out, a, b);
     return cudaGetLastError();
 }
 

@@ -81,10 +81,11 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
     __syncthreads();
 
     // 2. other small primes, one thread per prime walking the CTA's m values
-    const uint64_t ns = min((uint64_t)*rd.sp_count, rd.sp_cap);
+    const uint64_t sp_begin = rd.sp_range[0];
+    const uint64_t ns = min((uint64_t)(rd.sp_range[1] - sp_begin), rd.sp_cap);
     const uint32_t mi_first = s_mi[0], mi_last = s_mi[nrows - 1];
     for (uint64_t i = threadIdx.x; i < ns; i += blockDim.x) {
-        const uint32_t p = rd.sp_base + rd.sp[i], r = rd.sr[i];
+        const uint32_t p = rd.sp_base + rd.sp[sp_begin + i], r = rd.sr[i];
         uint64_t m = job.mstart + mi_first;
         uint32_t mr = (uint32_t)(((m % p) * r) % p);
         uint32_t x0 = (sl % p + p - mr) % p;
