@@ -146,8 +146,25 @@ def run_reference(args, rank, world):
     """CPU reference arm: the oracle port of method2 on the host cores."""
     if rank != 0:
         return 0
-    job = WORKLOADS[args.workload]
     threads = os.cpu_count() or 1
+    if args.workload in ("batch64", "served"):
+        import workloads
+
+        jobs = workloads.mixed_jobs(64, seed=4)[:3]
+        _cpu_sample_jobs(jobs[:1], threads, 0.02)
+        r = _cpu_sample_jobs(jobs, threads)
+        line = {
+            "impl": "reference", "metric": "method2 sieve (m,p) pairs/s", "value": r["value"],
+            "unit": "pairs/s", "n_gpus": world, "steps": 1, "warmup": 1,
+            "ms_per_step": r["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32/u64 integer", "data": "synthetic",
+            "config": {"workload": args.workload, "jobs": "first 3 of the 64-job mix (seed 4)"},
+            "cpu_baseline": r,
+            "e2e": {"value": r["value"], "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return 0
+    job = WORKLOADS[args.workload]
     for _ in range(args.warmup):
         _cpu_sample(job, threads)
     secs, pairs, sample = 0.0, 0, ""
@@ -304,6 +321,238 @@ def run_gb300(args, rank, world, local):
     return 0
 
 
+def _pairs(res) -> int:
+    return int(res.rows) * int(res.primes)
+
+
+def _many_setup(args, rank, world, local):
+    import torch
+
+    import pgsieve
+    import workloads
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(local)
+    sieve = pgsieve.Sieve(local)
+    t = time.perf_counter()
+    sieve.reserve_table(4_000_000_000)  # the resident table every job draws from
+    table_s = time.perf_counter() - t
+    jobs = workloads.mixed_jobs(64, seed=4 + rank)  # each rank its own jobs
+    return torch, pgsieve, workloads, dist, sieve, jobs, table_s
+
+
+def _max_over_ranks(torch, dist, local, v: float) -> float:
+    if not dist:
+        return v
+    t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def _cpu_sample_jobs(jobs, threads: int, rows_fraction: float = 0.1) -> dict:
+    secs, pairs, parts = 0.0, 0, []
+    for j in jobs:
+        r = _cpu_sample(dict(p=j.p, d=j.d, mstart=j.mstart, minc=j.minc, sieve_length=j.sieve_length,
+                             max_prime=j.max_prime), threads, rows_fraction)
+        secs += r["seconds"]
+        pairs += r["pairs"]
+        parts.append(f"P={j.p} d={j.d} minc={max(1, int(j.minc * rows_fraction))} SL={j.sieve_length} "
+                     f"max_prime={j.max_prime}")
+    return {"value": pairs / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
+            "sample": f"first {rows_fraction:.0%} of the m of {len(jobs)} mix jobs: " + "; ".join(parts),
+            "seconds": round(secs, 2)}
+
+
+def run_batch(args, rank, world, local):
+    """64 mixed jobs: the batched path (one CUDA graph over 8 streams, shared
+    prime table) beside the plain path (each job alone, its own primes)."""
+    torch, pgsieve, workloads, dist, sieve, jobs, table_s = _many_setup(args, rank, world, local)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def barrier():
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+
+    # plain: every job through pgs_prepare/pgs_run, one after another
+    preps = [sieve.prepare(j) for j in jobs]
+    for p in preps:
+        p.run(False)
+    barrier()
+    ext = torch.cuda.ExternalStream(sieve.stream)
+    plain_ms = 0.0
+    plain_steps = max(1, min(args.steps, 2))
+    for _ in range(plain_steps):
+        with torch.cuda.stream(ext):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            for p in preps:
+                p.run(False)
+            e1.record(ext)
+        e1.synchronize()
+        plain_ms += e0.elapsed_time(e1)
+    plain_md5 = []
+    for p in preps:
+        plain_md5.append(hashlib.md5(p.fetch()).hexdigest())
+        p.close()
+    plain_ms = _max_over_ranks(torch, dist, local, plain_ms) / plain_steps
+
+    # batched: graph replay over the lanes
+    batch = sieve.batch(jobs, lanes=args.lanes)
+    for _ in range(args.warmup):
+        batch.run(graph=True)
+    barrier()
+    clocks = ClockSampler(local)
+    clocks.start()
+    step_ms = []
+    for _ in range(args.steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        step_ms.append(batch.run(graph=True))
+    barrier()
+    clock_info = clocks.stop()
+    total_ms = _max_over_ranks(torch, dist, local, sum(step_ms))
+    pairs = 0
+    bit_exact = True
+    for i in range(len(jobs)):
+        with batch.fetch_view(i) as v:
+            pairs += _pairs(v.res)
+            bit_exact &= hashlib.md5(v.bytes()).hexdigest() == plain_md5[i]
+    batch.close()
+    value = pairs * world * args.steps / (total_ms * 1e-3)
+
+    # end to end: pgs_method2_batch (tables up, every text down) per step
+    for v in sieve.method2_batch_views(jobs):  # warm the pinned-buffer pool
+        v.close()
+    barrier()
+    e2e_s = 0.0
+    out_bytes = 0
+    for _ in range(args.steps):
+        t = time.perf_counter()
+        views = sieve.method2_batch_views(jobs)  # every text is in host memory on return
+        e2e_s += time.perf_counter() - t
+        out_bytes = sum(len(v) for v in views)
+        for v in views:
+            v.close()
+    e2e_s = _max_over_ranks(torch, dist, local, e2e_s)
+    h2d = 0
+    for j in jobs:
+        pl = pgsieve.plan(j)
+        h2d += (4 * ((pl["k_bits"] + 31) // 32) + 4 * j.minc + 4 * (2 * j.sieve_length + 1)
+                + 4 * pl["valid_ms"] + 2 * j.sieve_length)
+    if rank != 0:
+        return 0
+    cpu = None
+    if world == 1 and not args.no_cpu:
+        cpu = _cpu_sample_jobs(jobs[:3], os.cpu_count() or 1)
+    line = {
+        "metric": "method2 sieve (m,p) pairs/s", "value": value, "unit": "pairs/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32/u64 integer", "data": "synthetic",
+        "config": {"workload": "batch64", "jobs": len(jobs), "seed": 4, "lanes": args.lanes,
+                   "mix": "P {503..3001}, d {1,210,2190,30030}, minc log-uniform 1e3..1e5, "
+                          "SL 5000..40000, max_prime log-uniform 1e8..4e9",
+                   "l2": "flushed between steps (256 MiB write); prime table 760 MB > L2",
+                   "parallelism": f"replicas x{world}"},
+        "plain_ms_per_batch": plain_ms, "plain_pairs_per_s": pairs * world / (plain_ms * 1e-3),
+        "batched_vs_plain": plain_ms / (total_ms / args.steps),
+        "table_setup_s": table_s, "bit_exact_vs_plain": bit_exact,
+        "e2e": {"value": pairs * world * args.steps / e2e_s, "unit": "pairs/s",
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(out_bytes),
+                "ms_per_step": e2e_s / args.steps * 1e3},
+        "cpu_baseline": cpu, "clocks": clock_info,
+    }
+    print(json.dumps(line), flush=True)
+    sieve.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def run_served(args, rank, world, local):
+    """1000 mixed requests, Poisson arrivals at 80% of the batched job rate,
+    admitted against a 150 GB device budget; p50/p99 latency."""
+    torch, pgsieve, workloads, dist, sieve, jobs64, table_s = _many_setup(args, rank, world, local)
+    import random
+
+    with sieve.batch(jobs64, lanes=args.lanes) as b:
+        b.run(graph=True)
+        rate = 0.8 * len(jobs64) / (b.run(graph=True) * 1e-3)
+    rng = random.Random(1000 + rank)
+    jobs = [workloads.mixed_job(rng) for _ in range(args.requests)]
+    arrivals = workloads.poisson_arrivals(len(jobs), rate, seed=7 + rank)
+    check = set(random.Random(3).sample(range(len(jobs)), min(48, len(jobs))))
+    want = {i: hashlib.md5(sieve.method2(jobs[i])).hexdigest() for i in check}
+    got = {}
+    pairs = 0
+    barrier_t = torch.cuda.synchronize
+    barrier_t()
+    if dist:
+        dist.barrier()
+    clocks = ClockSampler(local)
+    with sieve.server(hbm_budget=150 << 30, lanes=args.lanes) as srv:
+        tickets = [None] * len(jobs)
+        clocks.start()
+        t0 = time.perf_counter()
+
+        def submitter():
+            for i, (j, ta) in enumerate(zip(jobs, arrivals)):
+                dt = t0 + ta - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+                tickets[i] = srv.submit(j)
+
+        th = threading.Thread(target=submitter)
+        th.start()
+        lat = []
+        for i in range(len(jobs)):
+            while tickets[i] is None:
+                time.sleep(0.0002)
+            v, ms = srv.wait_view(tickets[i], timeout_ms=600_000)
+            with v:
+                pairs += _pairs(v.res)
+                if i in check:
+                    got[i] = hashlib.md5(v.bytes()).hexdigest()
+            lat.append(ms)
+        th.join()
+        wall = time.perf_counter() - t0
+        st = srv.stats()
+        clock_info = clocks.stop()
+    wall = _max_over_ranks(torch, dist, local, wall)
+    if rank != 0:
+        return 0
+    lat.sort()
+    line = {
+        "metric": "method2 sieve (m,p) pairs/s", "value": pairs * world / wall, "unit": "pairs/s",
+        "n_gpus": world, "steps": 1, "warmup": args.warmup, "ms_per_step": wall * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32/u64 integer", "data": "synthetic",
+        "config": {"workload": "served", "requests": len(jobs), "arrival_rate_per_s": rate,
+                   "hbm_budget_bytes": 150 << 30, "lanes": args.lanes,
+                   "parallelism": f"replicas x{world}"},
+        "jobs_per_s": len(jobs) * world / wall,
+        "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
+                       "mean": sum(lat) / len(lat), "max": lat[-1]},
+        "server": st, "bit_exact_sample": {"checked": len(check),
+                                           "equal": sum(got[i] == want[i] for i in check)},
+        "table_setup_s": table_s, "clocks": clock_info,
+        "e2e": {"value": pairs * world / wall, "unit": "pairs/s", "h2d_bytes_per_step": None,
+                "d2h_bytes_per_step": None},
+    }
+    print(json.dumps(line), flush=True)
+    sieve.close()
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
 def large_kernel_model_ops(spec, stats, plan) -> float:
     """Model of the large-prime phase's integer work (ops per job).
 
@@ -330,12 +579,16 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS))
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS) + ["batch64", "served"])
+    ap.add_argument("--lanes", type=int, default=8, help="streams of the batched/served paths")
+    ap.add_argument("--requests", type=int, default=1000, help="served requests")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
     ap.add_argument("--max-prime", type=int, default=0,
                     help="override the workload's max_prime (small profiling runs)")
     args = ap.parse_args()
     rank, world, local = _dist()
+    if args.workload in ("batch64", "served") and args.impl == "gb300":
+        return (run_batch if args.workload == "batch64" else run_served)(args, rank, world, local)
     if args.max_prime:
         WORKLOADS[args.workload] = dict(WORKLOADS[args.workload], max_prime=args.max_prime)
         args.workload_note = "max_prime overridden"

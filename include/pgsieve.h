@@ -133,6 +133,60 @@ typedef struct {
 } pgs_plan;
 int pgs_plan_job(const pgs_job *job, pgs_plan *out);
 
+/* ---- many jobs: batched and served ------------------------------------ */
+
+/*
+ * Prime table resident on the context: every prime up to `limit` (sorted,
+ * 2^30-wide windows) and the small primes the row phase needs, generated
+ * once and shared by every batched or served job.  Grows on demand.
+ */
+int pgs_table_reserve(pgs_ctx *ctx, uint64_t limit);
+
+/*
+ * Batched method2: many jobs of uneven P, d, minc, SL and max_prime at once.
+ * Jobs share the resident prime table and run concurrently on `lanes` CUDA
+ * streams (each with its own scratch); the whole batch is captured as one
+ * CUDA graph on its first pgs_batch_run and replayed afterwards.  Outputs are
+ * byte-identical to pgs_method2 for each job.
+ */
+typedef struct pgs_batch pgs_batch;
+int pgs_batch_prepare(pgs_ctx *ctx, const pgs_job *jobs, int n, int lanes, pgs_batch **out);
+/* Run every job; *ms receives the device time of the batch (may be NULL). */
+int pgs_batch_run(pgs_ctx *ctx, pgs_batch *b, int use_graph, double *ms);
+int pgs_batch_fetch(pgs_ctx *ctx, pgs_batch *b, int i, pgs_result *out);
+void pgs_batch_free(pgs_batch *b);
+/* Convenience: prepare, run once and fetch all n results into outs. */
+int pgs_method2_batch(pgs_ctx *ctx, const pgs_job *jobs, int n, pgs_result *outs);
+
+/*
+ * Served method2: a request loop.  Submitted jobs are admitted, in arrival
+ * order, as soon as a lane is free and their device footprint (bitset, lists,
+ * text and tables) fits under hbm_budget bytes; admitted jobs run
+ * concurrently and their results are copied back as each one finishes (a
+ * lane takes its next job as soon as its kernels are done; the copy-back
+ * runs on a separate thread and stream).
+ * While a server runs it owns the context: make no other calls on it.
+ */
+typedef struct pgs_server pgs_server;
+typedef struct {
+    uint64_t submitted, completed, failed;
+    double p50_ms, p99_ms, mean_ms, max_ms; /* submit-to-result latency */
+    double busy_s;                          /* first admission to last result */
+    uint64_t peak_bytes;                    /* largest admitted footprint sum */
+    uint64_t max_inflight;
+    double host_prep_s;  /* host time deriving, uploading and launching jobs */
+    double host_fetch_s; /* host time copying results back */
+} pgs_server_stats;
+int pgs_server_start(pgs_ctx *ctx, uint64_t hbm_budget, int lanes, pgs_server **out);
+int pgs_server_submit(pgs_server *srv, const pgs_job *job, uint64_t *ticket);
+/* Wait for a ticket's result (timeout_ms < 0: no limit).  Returns
+ * PGS_ETIMEOUT if it is not done in time, or the job's own status. */
+int pgs_server_wait(pgs_server *srv, uint64_t ticket, int timeout_ms, pgs_result *out,
+                    double *latency_ms);
+int pgs_server_stats_get(pgs_server *srv, pgs_server_stats *out);
+/* Finish every submitted job, stop the loop and free the server. */
+int pgs_server_stop(pgs_server *srv);
+
 /* ---- the reference's number-theory kernels, batched on the device ---- */
 
 /*

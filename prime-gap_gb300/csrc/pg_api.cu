@@ -54,6 +54,7 @@ void pgs_destroy(pgs_ctx *ctx) {
     ctx->win_t0.release();
     ctx->large_ctr.release();
     ctx->heavy.release();
+    batch_state_destroy(ctx);
     ctx->dpool.trim();
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
@@ -282,55 +283,7 @@ int pgs_fetch(pgs_ctx *ctx, pgs_prepared *pr, pgs_result *out) {
     if (!ctx || !pr || !out || !pr->ran) return PGS_EINVAL;
     std::lock_guard<std::mutex> g(ctx->mu);
     CK(cudaSetDevice(ctx->device));
-    cudaStream_t s = ctx->stream;
-    memset(out, 0, sizeof(*out));
-    HostJob &h = pr->hj;
-    std::vector<uint64_t> misc(3 + 2 * pr->windows.size());
-    CK(cudaMemcpyAsync(misc.data(), pr->misc.p, misc.size() * 8, cudaMemcpyDeviceToHost, s));
-    CK(cudaStreamSynchronize(s));
-    const uint64_t total = misc[0];
-    if (total > pr->text_cap) {
-        ctx->err = "text larger than its bound";
-        return PGS_ECUDA;
-    }
-    size_t cap = 0;
-    char *host = pinned_pool().get(total + 1, &cap);
-    if (!host) {
-        ctx->err = "cudaMallocHost failed";
-        return PGS_ENOMEM;
-    }
-    cudaEvent_t t0, t1;
-    CK(cudaEventCreate(&t0));
-    CK(cudaEventCreate(&t1));
-    CK(cudaEventRecord(t0, s));
-    if (total) CK(cudaMemcpyAsync(host, pr->text.p, total, cudaMemcpyDeviceToHost, s));
-    CK(cudaEventRecord(t1, s));
-    CK(cudaStreamSynchronize(s));
-    host[total] = 0;
-    float ms_d2h = 0;
-    cudaEventElapsedTime(&ms_d2h, t0, t1);
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
-
-    out->text = host;
-    out->text_len = total;
-    out->internal = new PinnedOwner{cap};
-    out->rows = h.valid_mi.size();
-    uint64_t primes = h.primes_to_P + misc[2];
-    for (size_t w = 0; w < pr->windows.size(); w++) primes += misc[4 + 2 * w];
-    out->primes = primes;
-    out->prime_limit = h.prime_limit;
-    out->launches = pr->launches;
-    out->ms_stage[PGS_STAGE_SETUP] = pr->ms_setup;
-    out->ms_stage[PGS_STAGE_D2H] = ms_d2h;
-    for (auto &sp : pr->spans) {
-        float ms = 0;
-        if (sp.second.first < 0 || sp.second.second < 0) continue;
-        cudaEventElapsedTime(&ms, pr->events[sp.second.first], pr->events[sp.second.second]);
-        if (sp.first < 0) out->ms_total = ms;
-        else out->ms_stage[sp.first] += ms;
-    }
-    return PGS_OK;
+    return fetch_job(ctx, pr, ctx->stream, out);
 }
 
 int pgs_stage_ms(pgs_ctx *ctx, pgs_prepared *pr, double *out, double *total) {

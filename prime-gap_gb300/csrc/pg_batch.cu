@@ -1,0 +1,791 @@
+// Batched and served method2 over a prime table resident on the context.
+//
+// The plain path (pg_api.cu) sieves its own primes for every job.  Here all
+// jobs share one table -- sorted primes in 2^30-wide windows plus the small
+// primes of the row phase -- generated once and kept in HBM (every prime up to
+// 4e9 is 760 MB as u32 offsets).  A job then costs K mod p, the large-prime
+// walk and its rows only; it finds its primes by a device binary search
+// (pg::find_range), so nothing waits on the host.
+//
+// Jobs run on lanes: CUDA streams with their own scratch (walk steps and
+// starts, heavy-prime list).  A batch assigns its jobs to lanes by estimated
+// cost (longest first onto the least-loaded lane) and is captured once as a
+// CUDA graph spanning all lanes.  A server admits requests in arrival order
+// as lanes free up and their device footprint fits a byte budget, and copies
+// each result back as its lane's completion event fires.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <thread>
+
+#include "pg_host.h"
+
+using namespace pgh;
+
+struct TableWindow {
+    uint64_t lo = 0, hi = 0, count = 0;
+    DevBuf off;  // sorted primes as offsets from lo
+};
+
+struct PrimeTable {
+    uint64_t small_limit = 0;  // sorted primes 3..small_limit in `small`
+    DevBuf small;
+    std::vector<uint32_t> small_host;
+    std::vector<TableWindow *> windows;  // window k covers [max(3, k*2^30), (k+1)*2^30 - 1]
+    uint64_t max_count = 0;
+    ~PrimeTable() {
+        for (auto *w : windows) {
+            w->off.release();
+            delete w;
+        }
+        small.release();
+    }
+};
+
+struct Lane {
+    cudaStream_t stream = nullptr;
+    DevBuf r, t0, ctr, heavy;
+    ~Lane() {
+        r.release();
+        t0.release();
+        ctr.release();
+        heavy.release();
+        if (stream) cudaStreamDestroy(stream);
+    }
+};
+
+namespace {
+
+constexpr uint64_t kSmallMin = 1ull << 22;
+
+double now_s() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch()).count();
+}
+
+// Extend the table to every prime <= limit and small primes <= small_need.
+int table_extend(pgs_ctx *ctx, uint64_t limit, uint64_t small_need, cudaStream_t s) {
+    if (!ctx->table) ctx->table = new PrimeTable();
+    PrimeTable &t = *ctx->table;
+    const uint64_t k_last = limit / kWindowSpan;
+    const bool grow_small = small_need > t.small_limit;
+    const uint64_t small_target = grow_small ? std::max(small_need, kSmallMin) : t.small_limit;
+    if (!grow_small && t.windows.size() > k_last) return PGS_OK;
+    const uint64_t cover = std::max((k_last + 1) * kWindowSpan - 1, small_target);
+    CK(pg::base_primes_build(ctx->base, cover, s));
+    struct Scratch {
+        DevBuf tmp, cnt;
+        ~Scratch() {
+            tmp.release();
+            cnt.release();
+        }
+    } sc;
+    DevBuf &tmp = sc.tmp, &cnt = sc.cnt;
+    tmp.pool = cnt.pool = &ctx->dpool;
+    CK(cnt.ensure(8));
+    if (grow_small) {
+        // jobs in flight may read the old list: let them finish first
+        for (Lane *l : ctx->lanes) CK(cudaStreamSynchronize(l->stream));
+        const uint64_t cap = pg::prime_count_bound(0, small_target) + 16;
+        CK(t.small.ensure(cap * 4));
+        CK(tmp.ensure(pg::sieve_sorted_tmp_bytes(0, small_target)));
+        CK(pg::sieve_window_sorted(ctx->base, 0, small_target, t.small.as<uint32_t>(), cap,
+                                   cnt.as<unsigned long long>(), tmp.p, s));
+        uint64_t n = 0;
+        CK(cudaMemcpyAsync(&n, cnt.p, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        t.small_host.resize(n);
+        if (n) CK(cudaMemcpy(t.small_host.data(), t.small.p, n * 4, cudaMemcpyDeviceToHost));
+        t.small_limit = small_target;
+    }
+    for (uint64_t k = t.windows.size(); k <= k_last; k++) {
+        auto *w = new TableWindow();
+        w->lo = k == 0 ? 3 : k * kWindowSpan;
+        w->hi = (k + 1) * kWindowSpan - 1;
+        const uint64_t cap = pg::prime_count_bound(w->lo, w->hi) + 16;
+        cudaError_t e = w->off.ensure(cap * 4);
+        if (e == cudaSuccess) e = tmp.ensure(pg::sieve_sorted_tmp_bytes(w->lo, w->hi));
+        if (e == cudaSuccess)
+            e = pg::sieve_window_sorted(ctx->base, w->lo, w->hi, w->off.as<uint32_t>(), cap,
+                                        cnt.as<unsigned long long>(), tmp.p, s);
+        uint64_t n = 0;
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&n, cnt.p, 8, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            w->off.release();
+            delete w;
+            return fail(ctx, e, "table window");
+        }
+        w->count = n;
+        t.max_count = std::max(t.max_count, n);
+        t.windows.push_back(w);
+    }
+    return PGS_OK;
+}
+
+// Size an idle lane's scratch for the largest table window.
+int lane_buffers(pgs_ctx *ctx, Lane *l) {
+    const uint64_t need = ctx->table ? ctx->table->max_count : 0;
+    CK(l->r.ensure(need * 8 + 8));
+    CK(l->t0.ensure(need * 8 + 8));
+    CK(l->ctr.ensure(2 * sizeof(unsigned long long)));
+    CK(l->heavy.ensure((size_t)pg::heavy_capacity() * pg::kHeavyPrimeBytes));
+    return PGS_OK;
+}
+
+int ensure_lanes(pgs_ctx *ctx, int n) {
+    while ((int)ctx->lanes.size() < n) {
+        auto *l = new Lane();
+        cudaError_t e = cudaStreamCreateWithFlags(&l->stream, cudaStreamNonBlocking);
+        if (e != cudaSuccess) {
+            delete l;
+            return fail(ctx, e, "lane stream");
+        }
+        ctx->lanes.push_back(l);
+    }
+    for (int i = 0; i < n; i++) {
+        int rc = lane_buffers(ctx, ctx->lanes[i]);
+        if (rc) return rc;
+    }
+    return PGS_OK;
+}
+
+// Device bytes a job will hold (its tables and work buffers), from its
+// derived parameters.
+uint64_t job_footprint(const HostJob &h) {
+    const uint64_t rows = h.valid_mi.size();
+    const uint64_t mmax = h.job.mstart + h.job.minc;
+    const uint64_t per_row = ndigits(mmax) + 2ull * ndigits(h.H) + 16;
+    const uint64_t per_entry = h.job.compression == 1 ? 2 : 2 + ndigits(h.job.sieve_length);
+    uint64_t b = rows * (per_row + 2ull * h.H * per_entry);     // text
+    b += rows * h.pitch * 4ull + rows * 2ull * std::max<uint32_t>(h.H, 1) * 4;  // bitset, lists
+    b += rows * (8 + 8 + 8 + 4);                                // counts, bytes, offsets, valid_mi
+    b += h.job.minc * 4 + (2ull * h.job.sieve_length + 1) * 4;  // row_of_mi, col_of_x
+    return b;
+}
+
+// `derived`, when given, is the job's HostJob from derive(); it is moved in.
+int prepare_table_job(pgs_ctx *ctx, const pgs_job &job, cudaStream_t s, pgs_prepared **out,
+                      HostJob *derived = nullptr) {
+    *out = nullptr;
+    auto *pr = new pgs_prepared();
+    pr->ctx = ctx;
+    pr->table_mode = true;
+    for (DevBuf *b : pr->all()) b->pool = &ctx->dpool;
+    if (derived) {
+        pr->hj = std::move(*derived);
+    } else {
+        int rc = derive(job, pr->hj, ctx->err, true);
+        if (rc != PGS_OK) {
+            delete pr;
+            return rc;
+        }
+    }
+    HostJob &h = pr->hj;
+    PrimeTable &t = *ctx->table;
+    const uint64_t rows = h.valid_mi.size();
+    const uint64_t shi = std::min<uint64_t>(h.s1, h.prime_limit);
+    if (shi > t.small_limit || h.prime_limit / kWindowSpan >= t.windows.size()) {
+        ctx->err = "prime table does not cover the job";
+        delete pr;
+        return PGS_EINVAL;
+    }
+    // small primes (P, min(S1, limit)]: a contiguous run of the sorted table
+    pr->tbl_a = std::upper_bound(t.small_host.begin(), t.small_host.end(), h.job.p) -
+                t.small_host.begin();
+    pr->tbl_b = std::upper_bound(t.small_host.begin(), t.small_host.end(), (uint32_t)shi) -
+                t.small_host.begin();
+    if (pr->tbl_b < pr->tbl_a) pr->tbl_b = pr->tbl_a;
+    pr->sp_bound = pr->tbl_b - pr->tbl_a;
+    for (size_t k = 0; k < t.windows.size(); k++)
+        if (h.prime_limit > h.s1 && t.windows[k]->hi > h.s1 && t.windows[k]->lo <= h.prime_limit)
+            pr->tbl_windows.push_back((int)k);
+
+    cudaError_t e = cudaSuccess;
+    auto up = [&](DevBuf &b, auto &v) {
+        if (e == cudaSuccess) e = upload(b, v, s);
+    };
+    up(pr->klimbs, h.klimbs);
+    up(pr->row_of_mi, h.row_of_mi);
+    up(pr->col_of_x, h.col_of_x);
+    up(pr->valid_mi, h.valid_mi);
+    up(pr->dist, h.dist);
+    up(pr->dq, h.dq);
+    up(pr->mmask, h.mmask);
+    up(pr->xmask, h.xmask);
+    auto need = [&](DevBuf &b, size_t n) {
+        if (e == cudaSuccess) e = b.ensure(n);
+    };
+    need(pr->dr, std::max<size_t>(1, h.dq.size()) * 4);
+    need(pr->comp, rows * h.pitch * 4ull);
+    need(pr->sr, pr->sp_bound * 4 + 4);
+    need(pr->sp_t0, pr->sp_bound * 4 + 4);
+    need(pr->lists, rows * 2ull * std::max<uint32_t>(h.H, 1) * 4);
+    need(pr->counts, rows * 2ull * 4);
+    need(pr->row_bytes, rows * 8ull);
+    need(pr->offsets, rows * 8ull);
+    need(pr->scan_tmp, pg::scan_tmp_words(rows) * 8);
+    need(pr->misc, (1 + 2 * job_ranges(pr)) * 8);
+    const uint64_t mmax = h.job.mstart + h.job.minc;
+    const uint64_t per_row = ndigits(mmax) + 2ull * ndigits(h.H) + 16;
+    const uint64_t per_entry = h.job.compression == 1 ? 2 : 2 + ndigits(h.job.sieve_length);
+    pr->text_cap = rows * (per_row + 2ull * h.H * per_entry) + 64;
+    need(pr->text, pr->text_cap);
+    if (e != cudaSuccess) {
+        delete pr;
+        return fail(ctx, e, "prepare batched job");
+    }
+    size_t fp = 0;
+    for (DevBuf *b : pr->all()) fp += b->n;
+    pr->footprint = fp;
+    *out = pr;
+    return PGS_OK;
+}
+
+// All kernels of one job on one lane (asynchronous, capturable).
+int run_table_job(pgs_ctx *ctx, pgs_prepared *pr, Lane *lane) {
+    const cudaStream_t s = lane->stream;
+    HostJob &h = pr->hj;
+    PrimeTable &t = *ctx->table;
+    const uint64_t rows = h.valid_mi.size();
+    const pg::JobDev job = job_dev(pr);
+    pg::RowsDev rd = rows_dev(pr);
+    unsigned long long *misc = pr->misc.as<unsigned long long>();
+    rd.sp = t.small.as<uint32_t>();
+    rd.sp_base = 0;
+    rd.sp_range = misc + 1;
+    rd.sp_cap = pr->sp_bound;
+    const int nl = (int)h.klimbs.size();
+    uint64_t launches = 0;
+    CK(cudaMemsetAsync(pr->comp.p, 0, rows * h.pitch * 4ull, s));
+    CK(cudaMemsetAsync(pr->misc.p, 0, (1 + 2 * job_ranges(pr)) * 8, s));
+    CK(pg::set_pair(misc + 1, pr->tbl_a, pr->tbl_b, s));
+    launches++;
+    if (pr->sp_bound) {
+        CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, 0, t.small.as<uint32_t>(), misc + 1,
+                           pr->sp_bound, nullptr, pr->sr.p, pr->sp_t0.p, false, s));
+        launches++;
+    }
+    if (!h.dq.empty()) {
+        CK(pg::kmod_list32(pr->klimbs.as<uint32_t>(), nl, pr->dq.as<uint32_t>(),
+                           (uint32_t)h.dq.size(), pr->dr.as<uint32_t>(), s));
+        launches++;
+    }
+    const pg::LargeScratch scratch{lane->ctr.as<unsigned long long>(), lane->heavy.as<pg::HeavyPrime>(),
+                                   pg::heavy_capacity()};
+    for (size_t i = 0; i < pr->tbl_windows.size(); i++) {
+        const TableWindow &w = *t.windows[pr->tbl_windows[i]];
+        unsigned long long *rng = misc + 3 + 2 * i;
+        const bool wide = w.lo >= (1ull << 32);
+        CK(pg::find_range(w.off.as<uint32_t>(), w.count, w.lo, h.s1 + 1, h.prime_limit, rng, s));
+        CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, w.lo, w.off.as<uint32_t>(), rng, w.count,
+                           &h.walk, lane->r.p, lane->t0.p, wide, s));
+        CK(pg::large_window(job, w.lo, w.off.as<uint32_t>(), rng, w.count, lane->r.p, lane->t0.p, wide,
+                            pr->mmask.as<uint32_t>(), pr->xmask.as<uint32_t>(), scratch, s));
+        launches += 4;
+    }
+    CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression), s));
+    CK(pg::scan_u64(pr->row_bytes.as<uint64_t>(), pr->offsets.as<uint64_t>(), pr->misc.as<uint64_t>(),
+                    rows, pr->scan_tmp.as<uint64_t>(), s));
+    CK(pg::format_rows(rd, pr->offsets.as<uint64_t>(), pr->text.as<char>(), s));
+    launches += 5;
+    pr->launches = launches;
+    pr->ran = true;
+    return PGS_OK;
+}
+
+uint64_t job_cost(const HostJob &h) {
+    const double lim = (double)h.prime_limit;
+    const double primes = lim / std::log(std::max(lim, 3.0));
+    return (uint64_t)(primes * ((double)h.klimbs.size() + 150.0) +
+                      (double)h.valid_mi.size() * h.H * 2.0);
+}
+
+}  // namespace
+
+struct pgs_batch {
+    pgs_ctx *ctx = nullptr;
+    std::vector<pgs_prepared *> jobs;
+    std::vector<int> lane_of;
+    int nlanes = 1;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaEvent_t t0 = nullptr, t1 = nullptr, fork = nullptr;
+    std::vector<cudaEvent_t> joins;
+};
+
+namespace {
+
+int launch_batch(pgs_ctx *ctx, pgs_batch *b) {
+    Lane *l0 = ctx->lanes[0];
+    CK(cudaEventRecord(b->fork, l0->stream));
+    for (int l = 1; l < b->nlanes; l++) CK(cudaStreamWaitEvent(ctx->lanes[l]->stream, b->fork, 0));
+    for (size_t j = 0; j < b->jobs.size(); j++) {
+        int rc = run_table_job(ctx, b->jobs[j], ctx->lanes[b->lane_of[j]]);
+        if (rc) return rc;
+    }
+    for (int l = 1; l < b->nlanes; l++) {
+        CK(cudaEventRecord(b->joins[l], ctx->lanes[l]->stream));
+        CK(cudaStreamWaitEvent(l0->stream, b->joins[l], 0));
+    }
+    return PGS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pgs_table_reserve(pgs_ctx *ctx, uint64_t limit) {
+    if (!ctx || limit > 40000000000000ull) return PGS_EINVAL;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    return table_extend(ctx, limit, kSmallMin, ctx->stream);
+}
+
+int pgs_batch_prepare(pgs_ctx *ctx, const pgs_job *jobs, int n, int lanes, pgs_batch **out) {
+    if (!ctx || !jobs || n <= 0 || !out) return PGS_EINVAL;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    *out = nullptr;
+    // cover every job: large primes up to the largest limit, small up to the largest S1
+    uint64_t limit = 3, small = kSmallMin;
+    for (int i = 0; i < n; i++) {
+        HostJob h;
+        int rc = derive(jobs[i], h, ctx->err, false);
+        if (rc) return rc;
+        limit = std::max(limit, h.prime_limit);
+        small = std::max(small, std::min<uint64_t>(h.s1, h.prime_limit));
+    }
+    int rc = table_extend(ctx, limit, small, ctx->stream);
+    if (rc) return rc;
+    const int L = std::max(1, std::min(lanes, n));
+    rc = ensure_lanes(ctx, L);
+    if (rc) return rc;
+    auto *b = new pgs_batch();
+    b->ctx = ctx;
+    b->nlanes = L;
+    std::vector<uint64_t> cost;
+    for (int i = 0; i < n; i++) {
+        pgs_prepared *pr = nullptr;
+        rc = prepare_table_job(ctx, jobs[i], ctx->lanes[i % L]->stream, &pr);
+        if (rc) {
+            pgs_batch_free(b);
+            return rc;
+        }
+        b->jobs.push_back(pr);
+        cost.push_back(job_cost(pr->hj));
+    }
+    // longest job first onto the least-loaded lane
+    std::vector<int> order(n);
+    for (int i = 0; i < n; i++) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](int a, int c) { return cost[a] > cost[c]; });
+    std::vector<uint64_t> load(L, 0);
+    b->lane_of.assign(n, 0);
+    for (int i : order) {
+        int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[best] += cost[i];
+        b->lane_of[i] = best;
+    }
+    CK(cudaEventCreate(&b->t0));
+    CK(cudaEventCreate(&b->t1));
+    CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    b->joins.assign(L, nullptr);
+    for (int l = 1; l < L; l++) CK(cudaEventCreateWithFlags(&b->joins[l], cudaEventDisableTiming));
+    for (int l = 0; l < L; l++) CK(cudaStreamSynchronize(ctx->lanes[l]->stream));
+    *out = b;
+    return PGS_OK;
+}
+
+int pgs_batch_run(pgs_ctx *ctx, pgs_batch *b, int use_graph, double *ms) {
+    if (!ctx || !b || b->ctx != ctx) return PGS_EINVAL;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    Lane *l0 = ctx->lanes[0];
+    if (use_graph && !b->exec) {
+        CK(cudaStreamBeginCapture(l0->stream, cudaStreamCaptureModeRelaxed));
+        int rc = launch_batch(ctx, b);
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamEndCapture(l0->stream, &graph);
+        if (rc) {
+            if (graph) cudaGraphDestroy(graph);
+            return rc;
+        }
+        CK(e);
+        b->graph = graph;
+        CK(cudaGraphInstantiate(&b->exec, b->graph, 0));
+    }
+    CK(cudaEventRecord(b->t0, l0->stream));
+    if (use_graph) {
+        CK(cudaGraphLaunch(b->exec, l0->stream));
+    } else {
+        int rc = launch_batch(ctx, b);
+        if (rc) return rc;
+    }
+    CK(cudaEventRecord(b->t1, l0->stream));
+    CK(cudaEventSynchronize(b->t1));
+    float t = 0;
+    CK(cudaEventElapsedTime(&t, b->t0, b->t1));
+    if (ms) *ms = t;
+    return PGS_OK;
+}
+
+int pgs_batch_fetch(pgs_ctx *ctx, pgs_batch *b, int i, pgs_result *out) {
+    if (!ctx || !b || !out || i < 0 || i >= (int)b->jobs.size()) return PGS_EINVAL;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    if (!b->jobs[i]->ran) return PGS_EINVAL;
+    return fetch_job(ctx, b->jobs[i], ctx->lanes[b->lane_of[i]]->stream, out);
+}
+
+void pgs_batch_free(pgs_batch *b) {
+    if (!b) return;
+    if (b->ctx) {
+        cudaSetDevice(b->ctx->device);
+        for (Lane *l : b->ctx->lanes) cudaStreamSynchronize(l->stream);
+    }
+    if (b->exec) cudaGraphExecDestroy(b->exec);
+    if (b->graph) cudaGraphDestroy(b->graph);
+    if (b->t0) cudaEventDestroy(b->t0);
+    if (b->t1) cudaEventDestroy(b->t1);
+    if (b->fork) cudaEventDestroy(b->fork);
+    for (auto e : b->joins)
+        if (e) cudaEventDestroy(e);
+    for (auto *pr : b->jobs) delete pr;
+    delete b;
+}
+
+int pgs_method2_batch(pgs_ctx *ctx, const pgs_job *jobs, int n, pgs_result *outs) {
+    if (!outs) return PGS_EINVAL;
+    pgs_batch *b = nullptr;
+    int rc = pgs_batch_prepare(ctx, jobs, n, 8, &b);
+    if (rc) return rc;
+    rc = pgs_batch_run(ctx, b, 0, nullptr);
+    for (int i = 0; rc == PGS_OK && i < n; i++) rc = pgs_batch_fetch(ctx, b, i, &outs[i]);
+    pgs_batch_free(b);
+    return rc;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// server
+//
+// Two threads.  The dispatcher admits requests in arrival order: it derives
+// the head job (once), waits until a lane is free and the job's footprint
+// fits the budget, uploads its tables and launches its kernels on the lane,
+// then records the lane's event.  The completer polls the lanes' events;
+// when a job's kernels are done it frees the lane at once (the job's text
+// lives in the job's own buffers, not in lane scratch) and copies the text
+// back on its own stream, then releases the job's memory from the budget.
+
+namespace {
+
+struct Request {
+    uint64_t ticket = 0;
+    pgs_job job{};
+    double t_submit = 0, latency_ms = 0;
+    int status = 1;  // 1 pending/running, else a PGS_ status
+    pgs_result res{};
+    pgs_prepared *pr = nullptr;
+    uint64_t footprint = 0;
+    HostJob *hj = nullptr;  // derived once, at the head of the queue
+    int derive_rc = 1;
+    ~Request() { delete hj; }
+};
+
+}  // namespace
+
+struct pgs_server {
+    pgs_ctx *ctx = nullptr;
+    uint64_t budget = 0;
+    int nlanes = 1;
+    std::mutex mu;
+    std::condition_variable cv_done;
+    std::deque<Request *> pending;
+    std::map<uint64_t, Request *> reqs;
+    std::vector<Request *> lane_req;   // job whose kernels run on the lane
+    std::vector<cudaEvent_t> lane_done;
+    cudaStream_t fetch_stream = nullptr;
+    uint64_t next_ticket = 1, in_use = 0, running = 0, fetching = 0;
+    bool stopping = false, dispatcher_done = false;
+    std::thread dispatcher, completer;
+    std::string err;
+    // statistics
+    std::vector<double> latencies;
+    uint64_t submitted = 0, completed = 0, failed = 0, peak_bytes = 0, max_inflight = 0;
+    double t_first = -1, t_last = 0, prep_s = 0, fetch_s = 0;
+};
+
+namespace {
+
+void complete(pgs_server *srv, Request *r, int status) {
+    const double t0 = now_s();
+    if (status == PGS_OK) status = fetch_job(srv->ctx, r->pr, srv->fetch_stream, &r->res);
+    delete r->pr;
+    r->pr = nullptr;
+    const double t = now_s();
+    std::lock_guard<std::mutex> g(srv->mu);
+    srv->fetch_s += t - t0;
+    r->latency_ms = (t - r->t_submit) * 1e3;
+    r->status = status;
+    srv->in_use -= r->footprint;
+    srv->fetching--;
+    srv->t_last = t;
+    if (status == PGS_OK) {
+        srv->completed++;
+        srv->latencies.push_back(r->latency_ms);
+    } else {
+        srv->failed++;
+    }
+    srv->cv_done.notify_all();
+}
+
+void complete_loop(pgs_server *srv) {
+    cudaSetDevice(srv->ctx->device);
+    for (;;) {
+        bool idle = true;
+        for (int l = 0; l < srv->nlanes; l++) {
+            Request *r;
+            {
+                std::lock_guard<std::mutex> g(srv->mu);
+                r = srv->lane_req[l];
+            }
+            if (!r) continue;
+            cudaError_t q = cudaEventQuery(srv->lane_done[l]);
+            if (q == cudaErrorNotReady) continue;
+            {
+                std::lock_guard<std::mutex> g(srv->mu);
+                srv->lane_req[l] = nullptr;  // the lane takes new work now
+                srv->running--;
+                srv->fetching++;
+            }
+            complete(srv, r, q == cudaSuccess ? PGS_OK : PGS_ECUDA);
+            idle = false;
+        }
+        {
+            std::lock_guard<std::mutex> g(srv->mu);
+            if (srv->dispatcher_done && srv->running == 0) return;
+        }
+        if (idle) std::this_thread::sleep_for(std::chrono::microseconds(20));
+    }
+}
+
+void dispatch_loop(pgs_server *srv) {
+    pgs_ctx *ctx = srv->ctx;
+    cudaSetDevice(ctx->device);
+    for (;;) {
+        Request *r = nullptr;
+        int lane = -1;
+        {
+            std::lock_guard<std::mutex> g(srv->mu);
+            if (srv->pending.empty()) {
+                if (srv->stopping) {
+                    srv->dispatcher_done = true;
+                    return;
+                }
+            } else {
+                r = srv->pending.front();
+                for (int l = 0; l < srv->nlanes; l++)
+                    if (!srv->lane_req[l]) {
+                        lane = l;
+                        break;
+                    }
+            }
+        }
+        if (!r) {
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+            continue;
+        }
+        const double t0 = now_s();
+        if (r->derive_rc == 1) {  // derive the head while lanes are busy
+            r->hj = new HostJob();
+            r->derive_rc = derive(r->job, *r->hj, srv->err, true);
+            r->footprint = r->derive_rc == PGS_OK ? job_footprint(*r->hj) : 0;
+        }
+        int rc = r->derive_rc;
+        bool admit = rc != PGS_OK;  // failures leave the queue at once
+        if (rc == PGS_OK && lane >= 0) {
+            std::lock_guard<std::mutex> g(srv->mu);
+            // the head waits while it does not fit (unless nothing holds memory)
+            admit = srv->in_use == 0 || srv->in_use + r->footprint <= srv->budget;
+        }
+        if (!admit) {
+            std::this_thread::sleep_for(std::chrono::microseconds(20));
+            continue;
+        }
+        {
+            std::lock_guard<std::mutex> g(srv->mu);
+            srv->pending.pop_front();
+            if (rc == PGS_OK) {
+                srv->in_use += r->footprint;
+                srv->peak_bytes = std::max(srv->peak_bytes, srv->in_use);
+            }
+        }
+        if (rc == PGS_OK) {
+            HostJob &h = *r->hj;
+            Lane *L = ctx->lanes[lane];
+            rc = table_extend(ctx, h.prime_limit, std::min<uint64_t>(h.s1, h.prime_limit), L->stream);
+            if (rc == PGS_OK) rc = lane_buffers(ctx, L);
+            if (rc == PGS_OK) rc = prepare_table_job(ctx, r->job, L->stream, &r->pr, r->hj);
+            if (rc == PGS_OK) rc = run_table_job(ctx, r->pr, L);
+            if (rc == PGS_OK && cudaEventRecord(srv->lane_done[lane], L->stream) != cudaSuccess)
+                rc = PGS_ECUDA;
+        }
+        std::lock_guard<std::mutex> g(srv->mu);
+        srv->prep_s += now_s() - t0;
+        if (rc != PGS_OK) {
+            delete r->pr;
+            r->pr = nullptr;
+            if (r->derive_rc == PGS_OK) srv->in_use -= r->footprint;
+            r->status = rc;
+            srv->failed++;
+            srv->cv_done.notify_all();
+            continue;
+        }
+        srv->lane_req[lane] = r;
+        srv->running++;
+        srv->max_inflight = std::max(srv->max_inflight, srv->running + srv->fetching);
+        if (srv->t_first < 0) srv->t_first = now_s();
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int pgs_server_start(pgs_ctx *ctx, uint64_t hbm_budget, int lanes, pgs_server **out) {
+    if (!ctx || !out || lanes <= 0) return PGS_EINVAL;
+    *out = nullptr;
+    {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        CK(cudaSetDevice(ctx->device));
+        int rc = table_extend(ctx, 3, kSmallMin, ctx->stream);
+        if (rc) return rc;
+        rc = ensure_lanes(ctx, lanes);
+        if (rc) return rc;
+    }
+    auto *srv = new pgs_server();
+    srv->ctx = ctx;
+    srv->budget = hbm_budget;
+    srv->nlanes = lanes;
+    srv->lane_req.assign(lanes, nullptr);
+    srv->lane_done.assign(lanes, nullptr);
+    cudaError_t e = cudaStreamCreateWithFlags(&srv->fetch_stream, cudaStreamNonBlocking);
+    for (int l = 0; l < lanes && e == cudaSuccess; l++)
+        e = cudaEventCreateWithFlags(&srv->lane_done[l], cudaEventDisableTiming);
+    if (e != cudaSuccess) {
+        for (auto ev : srv->lane_done)
+            if (ev) cudaEventDestroy(ev);
+        if (srv->fetch_stream) cudaStreamDestroy(srv->fetch_stream);
+        delete srv;
+        return fail(ctx, e, "server start");
+    }
+    srv->dispatcher = std::thread(dispatch_loop, srv);
+    srv->completer = std::thread(complete_loop, srv);
+    *out = srv;
+    return PGS_OK;
+}
+
+int pgs_server_submit(pgs_server *srv, const pgs_job *job, uint64_t *ticket) {
+    if (!srv || !job) return PGS_EINVAL;
+    auto *r = new Request();
+    r->job = *job;
+    r->t_submit = now_s();
+    std::lock_guard<std::mutex> g(srv->mu);
+    if (srv->stopping) {
+        delete r;
+        return PGS_EINVAL;
+    }
+    r->ticket = srv->next_ticket++;
+    srv->reqs[r->ticket] = r;
+    srv->pending.push_back(r);
+    srv->submitted++;
+    if (ticket) *ticket = r->ticket;
+    return PGS_OK;
+}
+
+int pgs_server_wait(pgs_server *srv, uint64_t ticket, int timeout_ms, pgs_result *out,
+                    double *latency_ms) {
+    if (!srv || !out) return PGS_EINVAL;
+    std::unique_lock<std::mutex> lk(srv->mu);
+    auto it = srv->reqs.find(ticket);
+    if (it == srv->reqs.end()) return PGS_EINVAL;
+    Request *r = it->second;
+    auto done = [&] { return r->status != 1; };
+    if (timeout_ms < 0) {
+        srv->cv_done.wait(lk, done);
+    } else if (!srv->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), done)) {
+        return PGS_ETIMEOUT;
+    }
+    const int status = r->status;
+    *out = r->res;
+    if (latency_ms) *latency_ms = r->latency_ms;
+    srv->reqs.erase(it);
+    delete r;
+    return status;
+}
+
+int pgs_server_stats_get(pgs_server *srv, pgs_server_stats *out) {
+    if (!srv || !out) return PGS_EINVAL;
+    std::lock_guard<std::mutex> g(srv->mu);
+    memset(out, 0, sizeof(*out));
+    out->submitted = srv->submitted;
+    out->completed = srv->completed;
+    out->failed = srv->failed;
+    out->peak_bytes = srv->peak_bytes;
+    out->max_inflight = srv->max_inflight;
+    out->host_prep_s = srv->prep_s;
+    out->host_fetch_s = srv->fetch_s;
+    if (!srv->latencies.empty()) {
+        std::vector<double> v = srv->latencies;
+        std::sort(v.begin(), v.end());
+        auto q = [&](double f) { return v[std::min(v.size() - 1, (size_t)(f * (v.size() - 1) + 0.5))]; };
+        out->p50_ms = q(0.50);
+        out->p99_ms = q(0.99);
+        out->max_ms = v.back();
+        double s = 0;
+        for (double x : v) s += x;
+        out->mean_ms = s / v.size();
+    }
+    out->busy_s = srv->t_first >= 0 ? srv->t_last - srv->t_first : 0;
+    return PGS_OK;
+}
+
+int pgs_server_stop(pgs_server *srv) {
+    if (!srv) return PGS_EINVAL;
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        srv->stopping = true;
+    }
+    if (srv->dispatcher.joinable()) srv->dispatcher.join();
+    if (srv->completer.joinable()) srv->completer.join();
+    for (auto &kv : srv->reqs) {
+        pgs_result_free(&kv.second->res);
+        delete kv.second->pr;
+        delete kv.second;
+    }
+    for (auto e : srv->lane_done)
+        if (e) cudaEventDestroy(e);
+    if (srv->fetch_stream) cudaStreamDestroy(srv->fetch_stream);
+    delete srv;
+    return PGS_OK;
+}
+
+}  // extern "C"
+
+namespace pgh {
+
+void batch_state_destroy(pgs_ctx *ctx) {
+    for (Lane *l : ctx->lanes) {
+        cudaStreamSynchronize(l->stream);
+        delete l;
+    }
+    ctx->lanes.clear();
+    delete ctx->table;
+    ctx->table = nullptr;
+}
+
+}  // namespace pgh

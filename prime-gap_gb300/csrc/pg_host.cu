@@ -282,4 +282,61 @@ uint32_t rows_per_block(uint32_t nb, int compression) {
     return r;
 }
 
+size_t job_ranges(const pgs_prepared *pr) {
+    return 1 + (pr->table_mode ? pr->tbl_windows.size() : pr->windows.size());
+}
+
+int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out) {
+    memset(out, 0, sizeof(*out));
+    const HostJob &h = pr->hj;
+    // misc: [0] text bytes, then {begin, end} pairs: small primes, then windows
+    const size_t nr = job_ranges(pr);
+    std::vector<uint64_t> misc(1 + 2 * nr);
+    CK(cudaMemcpyAsync(misc.data(), pr->misc.p, misc.size() * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    const uint64_t total = misc[0];
+    if (total > pr->text_cap) {
+        ctx->err = "text larger than its bound";
+        return PGS_ECUDA;
+    }
+    size_t cap = 0;
+    char *host = pinned_pool().get(total + 1, &cap);
+    if (!host) {
+        ctx->err = "cudaMallocHost failed";
+        return PGS_ENOMEM;
+    }
+    cudaEvent_t t0, t1;
+    CK(cudaEventCreate(&t0));
+    CK(cudaEventCreate(&t1));
+    CK(cudaEventRecord(t0, s));
+    if (total) CK(cudaMemcpyAsync(host, pr->text.p, total, cudaMemcpyDeviceToHost, s));
+    CK(cudaEventRecord(t1, s));
+    CK(cudaStreamSynchronize(s));
+    host[total] = 0;
+    float ms_d2h = 0;
+    cudaEventElapsedTime(&ms_d2h, t0, t1);
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+
+    out->text = host;
+    out->text_len = total;
+    out->internal = new PinnedOwner{cap};
+    out->rows = h.valid_mi.size();
+    uint64_t primes = h.primes_to_P;
+    for (size_t i = 0; i < nr; i++) primes += misc[2 + 2 * i] - misc[1 + 2 * i];
+    out->primes = primes;
+    out->prime_limit = h.prime_limit;
+    out->launches = pr->launches;
+    out->ms_stage[PGS_STAGE_SETUP] = pr->ms_setup;
+    out->ms_stage[PGS_STAGE_D2H] = ms_d2h;
+    for (auto &sp : pr->spans) {
+        float ms = 0;
+        if (sp.second.first < 0 || sp.second.second < 0) continue;
+        cudaEventElapsedTime(&ms, pr->events[sp.second.first], pr->events[sp.second.second]);
+        if (sp.first < 0) out->ms_total = ms;
+        else out->ms_stage[sp.first] += ms;
+    }
+    return PGS_OK;
+}
+
 }  // namespace pgh

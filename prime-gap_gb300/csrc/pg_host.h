@@ -163,6 +163,9 @@ struct pgs_ctx {
     pg::BasePrimes base;
     pgh::DevBuf win_off, win_r, win_t0, large_ctr, heavy;
     pgh::DevicePool dpool;
+    // batched / served paths (pg_batch.cu)
+    PrimeTable *table = nullptr;
+    std::vector<Lane *> lanes;
 };
 
 struct pgs_prepared {
@@ -171,6 +174,12 @@ struct pgs_prepared {
     std::vector<pgh::Window> windows;
     uint64_t sp_lo = 0, sp_hi = 0, sp_bound = 0;
     uint64_t text_cap = 0;
+    // resident-table jobs (pg_batch.cu): small primes are table entries
+    // [tbl_a, tbl_b), large primes come from the table windows listed
+    bool table_mode = false;
+    uint64_t tbl_a = 0, tbl_b = 0;
+    std::vector<int> tbl_windows;
+    size_t footprint = 0;  // device bytes held by this job
     uint64_t win_bound = 0;
     pgh::DevBuf klimbs, row_of_mi, col_of_x, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0, mmask, xmask;
     pgh::DevBuf lists, counts, row_bytes, offsets, scan_tmp, misc, text;
@@ -210,5 +219,12 @@ cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t s) {
 pg::JobDev job_dev(pgs_prepared *pr);
 pg::RowsDev rows_dev(pgs_prepared *pr);
 uint32_t rows_per_block(uint32_t nb, int compression);
+
+// Copy a finished job's text to pinned host memory (no context lock).
+int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out);
+// Number of {begin, end} prime ranges in a prepared job's misc buffer.
+size_t job_ranges(const pgs_prepared *pr);
+// Free the resident prime table and the lanes (pg_batch.cu).
+void batch_state_destroy(pgs_ctx *ctx);
 
 }  // namespace pgh

@@ -73,6 +73,23 @@ class Plan(ctypes.Structure):
     ]
 
 
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("submitted", ctypes.c_uint64),
+        ("completed", ctypes.c_uint64),
+        ("failed", ctypes.c_uint64),
+        ("p50_ms", ctypes.c_double),
+        ("p99_ms", ctypes.c_double),
+        ("mean_ms", ctypes.c_double),
+        ("max_ms", ctypes.c_double),
+        ("busy_s", ctypes.c_double),
+        ("peak_bytes", ctypes.c_uint64),
+        ("max_inflight", ctypes.c_uint64),
+        ("host_prep_s", ctypes.c_double),
+        ("host_fetch_s", ctypes.c_double),
+    ]
+
+
 @dataclass
 class JobSpec:
     """Config fields of one method2 job; max_prime is absolute."""
@@ -124,6 +141,22 @@ _SIGNATURES = {
     "pgs_large_hits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                       ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _u32p,
                                       _u64p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "pgs_table_reserve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
+    "pgs_batch_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_int, ctypes.c_int,
+                                         ctypes.POINTER(ctypes.c_void_p)]),
+    "pgs_batch_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_double)]),
+    "pgs_batch_fetch": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Result)]),
+    "pgs_batch_free": (None, [ctypes.c_void_p]),
+    "pgs_method2_batch": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_int,
+                                         ctypes.POINTER(Result)]),
+    "pgs_server_start": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    "pgs_server_submit": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), _u64p]),
+    "pgs_server_wait": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(Result),
+                                       ctypes.POINTER(ctypes.c_double)]),
+    "pgs_server_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStats)]),
+    "pgs_server_stop": (ctypes.c_int, [ctypes.c_void_p]),
 }
 
 _lib: ctypes.CDLL | None = None
@@ -237,6 +270,37 @@ class Sieve:
         self._check(self.lib.pgs_prepare(self.h, ctypes.byref(job.c()), ctypes.byref(h)))
         return Prepared(self, h)
 
+    def reserve_table(self, limit: int) -> None:
+        """Generate (once) the resident prime table up to ``limit``."""
+        self._check(self.lib.pgs_table_reserve(self.h, limit))
+
+    def batch(self, jobs: list[JobSpec], lanes: int = 8) -> "Batch":
+        """Prepare many jobs over the resident prime table (pgs_batch_prepare)."""
+        arr = (Job * len(jobs))(*[j.c() for j in jobs])
+        h = ctypes.c_void_p()
+        self._check(self.lib.pgs_batch_prepare(self.h, arr, len(jobs), lanes, ctypes.byref(h)))
+        return Batch(self, h, len(jobs))
+
+    def method2_batch(self, jobs: list[JobSpec]) -> list[bytes]:
+        out = []
+        for v in self.method2_batch_views(jobs):
+            with v:
+                out.append(v.bytes())
+        return out
+
+    def method2_batch_views(self, jobs: list[JobSpec]) -> list["ResultView"]:
+        """pgs_method2_batch without copies: one view per job (close each)."""
+        arr = (Job * len(jobs))(*[j.c() for j in jobs])
+        res = (Result * len(jobs))()
+        self._check(self.lib.pgs_method2_batch(self.h, arr, len(jobs), res))
+        return [ResultView(self.lib, r) for r in res]
+
+    def server(self, hbm_budget: int, lanes: int = 8) -> "Server":
+        """Start the request server on this context (pgs_server_start)."""
+        h = ctypes.c_void_p()
+        self._check(self.lib.pgs_server_start(self.h, hbm_budget, lanes, ctypes.byref(h)))
+        return Server(self, h)
+
     def int_peak(self) -> float:
         """Measured 32-bit IMAD issue rate (per second)."""
         v = ctypes.c_double()
@@ -337,6 +401,82 @@ class Prepared:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class Batch:
+    """Jobs prepared over the resident prime table; run as one CUDA graph."""
+
+    def __init__(self, sieve: Sieve, h: ctypes.c_void_p, n: int):
+        self.sieve, self.h, self.n = sieve, h, n
+
+    def run(self, graph: bool = True) -> float:
+        """Run every job; returns the batch's device time in ms."""
+        ms = ctypes.c_double()
+        self.sieve._check(self.sieve.lib.pgs_batch_run(self.sieve.h, self.h, int(graph), ctypes.byref(ms)))
+        return ms.value
+
+    def fetch_view(self, i: int) -> ResultView:
+        res = Result()
+        self.sieve._check(self.sieve.lib.pgs_batch_fetch(self.sieve.h, self.h, i, ctypes.byref(res)))
+        return ResultView(self.sieve.lib, res)
+
+    def fetch(self, i: int) -> bytes:
+        with self.fetch_view(i) as v:
+            return v.bytes()
+
+    def close(self) -> None:
+        if self.h:
+            self.sieve.lib.pgs_batch_free(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+
+class Server:
+    """Request server: jobs admitted in arrival order within an HBM budget."""
+
+    def __init__(self, sieve: Sieve, h: ctypes.c_void_p):
+        self.sieve, self.h = sieve, h
+
+    def submit(self, job: JobSpec) -> int:
+        t = ctypes.c_uint64()
+        rc = self.sieve.lib.pgs_server_submit(self.h, ctypes.byref(job.c()), ctypes.byref(t))
+        if rc != PGS_OK:
+            raise PgsError(rc, "submit refused")
+        return t.value
+
+    def wait_view(self, ticket: int, timeout_ms: int = -1) -> tuple[ResultView, float]:
+        res = Result()
+        lat = ctypes.c_double()
+        rc = self.sieve.lib.pgs_server_wait(self.h, ticket, timeout_ms, ctypes.byref(res), ctypes.byref(lat))
+        if rc != PGS_OK:
+            raise PgsError(rc, self.sieve.lib.pgs_last_error(self.sieve.h).decode(errors="replace"))
+        return ResultView(self.sieve.lib, res), lat.value
+
+    def wait(self, ticket: int, timeout_ms: int = -1) -> tuple[bytes, float]:
+        v, lat = self.wait_view(ticket, timeout_ms)
+        with v:
+            return v.bytes(), lat
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self.sieve._check(self.sieve.lib.pgs_server_stats_get(self.h, ctypes.byref(st)))
+        return {f: getattr(st, f) for f, _ in ServerStats._fields_}
+
+    def stop(self) -> None:
+        if self.h:
+            self.sieve.lib.pgs_server_stop(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.stop()
 
 
 def _result_stats(res: Result) -> dict:

@@ -15,7 +15,9 @@ SYMBOLS = [
     "pgs_create", "pgs_destroy", "pgs_last_error", "pgs_set_stream", "pgs_get_stream",
     "pgs_method2", "pgs_result_free", "pgs_prepare", "pgs_run", "pgs_fetch", "pgs_prepared_free",
     "pgs_plan_job", "pgs_stage_ms", "pgs_int_peak", "pgs_primes", "pgs_k_mod_p", "pgs_modulo_search", "pgs_large_hits",
-    "pgs_version",
+    "pgs_version", "pgs_table_reserve", "pgs_batch_prepare", "pgs_batch_run", "pgs_batch_fetch",
+    "pgs_batch_free", "pgs_method2_batch", "pgs_server_start", "pgs_server_submit", "pgs_server_wait",
+    "pgs_server_stats_get", "pgs_server_stop",
 ]
 
 
