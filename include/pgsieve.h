@@ -215,6 +215,29 @@ int pgs_large_hits(pgs_ctx *ctx, uint64_t M, uint32_t max_mi, uint32_t SL, uint6
                    uint64_t base_r, uint32_t *mi_out, uint64_t *mod_out, size_t cap,
                    size_t *count);
 
+/*
+ * pgs_large_hits that allocates nothing.  No counterpart in the reference.
+ *
+ * Same arguments, results and errors as pgs_large_hits, but the device hit
+ * lists and counter live in a fixed file-scope device buffer instead of
+ * per-call cudaMalloc/cudaFree.  For callers that must not allocate: a
+ * query made on a second context while a batch or server keeps kernels in
+ * flight on the same device (cudaFree waits for the whole device to go idle,
+ * so every pgs_large_hits call would stall behind, and hold up, those jobs),
+ * and callers running at their device-memory budget.
+ *
+ * Limit: cap <= 65536 hits per call; a larger cap returns PGS_EINVAL.  The
+ * count written may still exceed cap (only cap pairs are written).
+ * The buffer's address is looked up once per device on the first call
+ * (cudaGetSymbolAddress, which may load the module): make that first call
+ * before any stream capture on the device.  The buffer is shared by every
+ * context on a device: calls that overlap in time race on it, so serialise
+ * them (calls on one context are serialised by the context).
+ */
+int pgs_large_hits_static(pgs_ctx *ctx, uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t prime,
+                          uint64_t base_r, uint32_t *mi_out, uint64_t *mod_out, size_t cap,
+                          size_t *count);
+
 /* Library version string. */
 const char *pgs_version(void);
 

@@ -141,6 +141,9 @@ _SIGNATURES = {
     "pgs_large_hits": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                       ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _u32p,
                                       _u64p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "pgs_large_hits_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
+                                             ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _u32p,
+                                             _u64p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
     "pgs_table_reserve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "pgs_batch_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_void_p)]),
