@@ -83,6 +83,15 @@ PG_HD uint32_t redc32(uint64_t t, uint32_t p, uint32_t pinv) {
     return (uint32_t)(hi >= p ? hi - p : hi);
 }
 
+// R^2 mod p (R = 2^32) from r1 = R mod p without a 64-bit division: x = 2^33
+// mod p (one doubling), then five Montgomery squarings, each sending the
+// power e of x = 2^e to 2e - 32: 33 -> 34 -> 36 -> 40 -> 48 -> 64.
+PG_HD uint32_t r2_from_r1(uint32_t r1, uint32_t p, uint32_t pinv) {
+    uint32_t x = r1 >= p - r1 ? r1 - (p - r1) : r1 + r1;
+    for (int i = 0; i < 5; i++) x = redc32((uint64_t)x * x, p, pinv);
+    return x;
+}
+
 // Montgomery reduction, R = 2^64, of the 128-bit value (hi:lo) < p*2^64;
 // p < 2^63.  Result in [0, p).
 PG_HD uint64_t redc64(uint64_t hi, uint64_t lo, uint64_t p, uint64_t pinv) {
@@ -103,7 +112,7 @@ PG_HD uint32_t kmod32(const uint32_t *limbs, int n, uint32_t p, uint32_t &pinv_o
                       uint32_t &r2_out) {
     const uint32_t pinv = neg_inv32(p);
     const uint32_t r1 = (0u - p) % p;                          // 2^32 mod p
-    const uint32_t r2 = (uint32_t)(((uint64_t)r1 * r1) % p);  // 2^64 mod p
+    const uint32_t r2 = r2_from_r1(r1, p, pinv);               // 2^64 mod p
     uint32_t u = 0;
     if (p < 0x80000000u) {
         for (int i = n - 1; i >= 0; i--) u = redc32_lazy((uint64_t)u * r2 + limbs[i], p, pinv);
@@ -127,7 +136,7 @@ PG_HD void kmod32_multi(const uint32_t *limbs, int n, const uint32_t *p, uint32_
     for (int k = 0; k < NP; k++) {
         pinv[k] = neg_inv32(p[k]);
         const uint32_t r1 = (0u - p[k]) % p[k];
-        r2[k] = (uint32_t)(((uint64_t)r1 * r1) % p[k]);
+        r2[k] = r2_from_r1(r1, p[k], pinv[k]);
         u[k] = 0;
         lazy = lazy && p[k] < 0x80000000u;
     }
@@ -162,11 +171,70 @@ PG_HD uint32_t start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p, uint32_t
     return (uint32_t)(t >= p ? t - p : t);
 }
 
+// ---------------------------------------------------------------------------
+// K mod p, least significant limb first: W <- REDC(W + limb) leaves
+// W = K * R^-n after n limbs (each step multiplies what came before by R^-1),
+// and REDC(W * R^(n+1)) = K mod p.  A step is one add and one REDC (two
+// multiplies) instead of the most-significant-first step's three; R^(n+1) mod p
+// costs ~log2(n) Montgomery squarings per prime, shared work for long K.
+
+// (W + l) * 2^-32 mod p, result <= p + 1, for W <= p + 1, p < 2^32 - 4.
+PG_HD uint32_t redc32_add(uint32_t W, uint32_t l, uint32_t p, uint32_t pinv) {
+    const uint64_t x = (uint64_t)W + l;  // < 2^33
+    const uint32_t xl = (uint32_t)x;
+    const uint32_t m = xl * pinv;
+#if defined(__CUDA_ARCH__)
+    const uint32_t h = __umulhi(m, p);
+#else
+    const uint32_t h = (uint32_t)(((uint64_t)m * p) >> 32);
+#endif
+    return (uint32_t)(x >> 32) + h + (xl != 0u);
+}
+
+// R^(e+1) mod p (R = 2^32): Montgomery power of R (whose Montgomery form is
+// r2 = R^2 mod p), starting from the Montgomery form of 1 (r1 = R mod p).
+PG_HD uint32_t mont_rpow32(uint32_t e, uint32_t p, uint32_t pinv, uint32_t r1, uint32_t r2) {
+    uint32_t acc = r1, b = r2;
+    while (e) {
+        if (e & 1u) acc = redc32((uint64_t)acc * b, p, pinv);
+        e >>= 1;
+        if (e) b = redc32((uint64_t)b * b, p, pinv);
+    }
+    return acc;
+}
+
+// NP primes (odd, 3 <= p < 2^32 - 4) at once, least significant limb first.
+// Also returns pinv and r2 = 2^64 mod p of each prime.
+template <int NP>
+PG_HD void kmod32_lsb_multi(const uint32_t *limbs, int n, const uint32_t *p, uint32_t *r,
+                            uint32_t *pinv, uint32_t *r2) {
+    uint32_t W[NP], r1[NP];
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        pinv[k] = neg_inv32(p[k]);
+        r1[k] = (0u - p[k]) % p[k];
+        r2[k] = r2_from_r1(r1[k], p[k], pinv[k]);
+        W[k] = 0;
+    }
+    for (int i = 0; i < n; i++) {
+        const uint32_t l = limbs[i];
+#pragma unroll
+        for (int k = 0; k < NP; k++) W[k] = redc32_add(W[k], l, p[k], pinv[k]);
+    }
+#pragma unroll
+    for (int k = 0; k < NP; k++) {
+        const uint32_t X = mont_rpow32((uint32_t)n, p[k], pinv[k], r1[k], r2[k]);
+        r[k] = redc32((uint64_t)W[k] * X, p[k], pinv[k]);  // W * X < (p + 2) * p < p * 2^32
+    }
+}
+
 // Odd primes 2^31 <= p < 2^46 (and any odd p >= 3 below that): R = 2^64.
-PG_HD uint64_t kmod64(const uint32_t *limbs, int n, uint64_t p) {
+PG_HD uint64_t kmod64(const uint32_t *limbs, int n, uint64_t p, uint64_t *pinv_out = nullptr,
+                      uint64_t *r2_out = nullptr) {
     const uint64_t pinv = neg_inv64(p);
     const uint64_t r1 = (0ull - p) % p;                             // 2^64 mod p
     const uint64_t r2 = mulmod_u64(r1, r1, p, 1.0 / (double)p);  // 2^128 mod p
+    if (pinv_out) *pinv_out = pinv, *r2_out = r2;
     uint64_t u = 0;
     const int nw = (n + 1) / 2;
     for (int i = nw - 1; i >= 0; i--) {
@@ -179,6 +247,45 @@ PG_HD uint64_t kmod64(const uint32_t *limbs, int n, uint64_t p) {
         u = redc64(hi, lo2, p, pinv);
     }
     return redc64(umulhi64(u, r2), u * r2, p, pinv);
+}
+
+// REDC of the 65-bit value c*2^64 + lo (R = 2^64), result < p + 2 for
+// c*2^64 + lo < 2^64 + p*2^64.
+PG_HD uint64_t redc64_add(uint64_t W, uint64_t w, uint64_t p, uint64_t pinv) {
+    const uint64_t lo = W + w;
+    const uint64_t c = lo < W;
+    const uint64_t m = lo * pinv;
+    return c + umulhi64(m, p) + (lo != 0);
+}
+
+// Montgomery product for R = 2^64, inputs < p < 2^63, result < p.
+PG_HD uint64_t montmul64(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv) {
+    return redc64(umulhi64(a, b), a * b, p, pinv);
+}
+
+// kmod64 least significant 64-bit word first: W <- REDC(W + word), then
+// K mod p = REDC(W * R^(nw+1)).  Odd p < 2^46.
+PG_HD uint64_t kmod64_lsb(const uint32_t *limbs, int n, uint64_t p, uint64_t *pinv_out = nullptr,
+                          uint64_t *r2_out = nullptr) {
+    const uint64_t pinv = neg_inv64(p);
+    const uint64_t r1 = (0ull - p) % p;                          // 2^64 mod p
+    const uint64_t r2 = mulmod_u64(r1, r1, p, 1.0 / (double)p);  // 2^128 mod p
+    if (pinv_out) *pinv_out = pinv, *r2_out = r2;
+    const int nw = (n + 1) / 2;
+    uint64_t W = 0;
+    for (int i = 0; i < nw; i++) {
+        uint64_t w = limbs[2 * i];
+        if (2 * i + 1 < n) w |= (uint64_t)limbs[2 * i + 1] << 32;
+        W = redc64_add(W, w, p, pinv);
+    }
+    uint64_t acc = r1, b = r2;
+    for (uint32_t e = (uint32_t)nw; e;) {
+        if (e & 1u) acc = montmul64(acc, b, p, pinv);
+        e >>= 1;
+        if (e) b = montmul64(b, b, p, pinv);
+    }
+    if (W >= p) W -= p;  // W < p + 2
+    return montmul64(W, acc, p, pinv);
 }
 
 // ---------------------------------------------------------------------------
@@ -407,6 +514,36 @@ PG_HD uint32_t half_mod(uint32_t r, uint32_t p) {
 }
 PG_HD uint64_t half_mod(uint64_t r, uint64_t p) { return (r & 1u) ? ((r + p) >> 1) : (r >> 1); }
 
+// Step and start residue of a prime's parity-reduced walk from r = K mod p:
+// step = r/2 (d odd) or r (d even); t0 = (step' * m0 + c) mod p with
+// step' = r/2 and c = c_add (+ (p+1)/2 when d is odd).  r2 = 2^64 mod p
+// (32-bit primes only; it comes with K mod p).
+// kmul != 1: r is K' mod p for K = K' * kmul; K mod p = REDC(REDC(r * kmul) * r2).
+PG_HD void walk_start(const WalkParams &wk, uint32_t p, uint32_t r, uint32_t r2, uint32_t &step,
+                      uint32_t &t0, uint32_t kmul = 1) {
+    const uint32_t pinv = neg_inv32(p);
+    if (kmul != 1) r = redc32((uint64_t)redc32((uint64_t)r * kmul, p, pinv) * r2, p, pinv);
+    const uint32_t rh = half_mod(r, p);
+    const uint32_t c = wk.c_add + (wk.odd_d ? (p >> 1) + 1 : 0u);
+    step = wk.odd_d ? rh : r;
+    t0 = start32(rh, wk.m0, c, p, pinv, r2);
+}
+// 64-bit primes (p < 2^46, any m0): with pinv = -p^-1 mod 2^64 and
+// r2 = 2^128 mod p, t0 = REDC(REDC(m0 * r2) * rh) + c = m0 * rh + c mod p,
+// with no division.
+PG_HD void walk_start(const WalkParams &wk, uint64_t p, uint64_t r, uint64_t pinv, uint64_t r2,
+                      uint64_t &step, uint64_t &t0, uint32_t kmul = 1) {
+    if (kmul != 1) r = montmul64(montmul64(r, kmul, p, pinv), r2, p, pinv);
+    const uint64_t rh = half_mod(r, p);
+    const uint64_t c = wk.c_add + (wk.odd_d ? (p >> 1) + 1 : 0ull);
+    const uint64_t m0R = montmul64(wk.m0, r2, p, pinv);  // m0 * 2^64 mod p
+    uint64_t t = montmul64(m0R, rh, p, pinv) + c;
+    if (t >= p) t -= p;
+    step = wk.odd_d ? rh : r;
+    t0 = t;
+}
+
+
 // ---------------------------------------------------------------------------
 // first entry and three-gap data in one continued-fraction pass
 //
@@ -427,44 +564,46 @@ struct Entry {
     ThreeGap<T> g;
 };
 
+// One code path for both orientations (no divergence inside a warp): the
+// level with the larger gap `big` (up if up > dn, else dn) loses q copies of
+// the smaller gap `small`, and its m-step gains q copies of the other's.
+// The entry point moves as follows, with f = ceil((big - y) / small) for
+// y < big (else 0):
+//   up > dn: level i of the batch enters [0, up - i*dn): y -= dn whenever
+//            y >= up - i*dn, which, once true, stays true: q - f subtractions;
+//   up <= dn: level i enters [0, dn - i*up) with one wrap y -= dn - i*up at
+//            the first level where y >= dn - i*up, i = f (after it y < up).
+// t only grows, and the first hit comes no earlier than the first entry into
+// the current circle, so once t >= t_lim the search stops (no hit below
+// t_lim): the caller sees t >= t_lim.
 template <typename T>
-PG_HD Entry<T> first_entry(T p, T a, T w, T y0) {
+PG_HD Entry<T> first_entry(T p, T a, T w, T y0, uint64_t t_lim = ~0ull) {
     T kp = 1, up = a, kn = 1, dn = p - a;
     T y = y0;
     uint64_t t = 0;
     for (int pass = 0; pass < 256 && (up >= w || dn >= w); pass++) {
-        if (up > dn) {
-            // subtract dn until up < w or up <= dn: q = ceil((up - max(w-1, dn)) / dn)
-            const T lim = (w - 1) > dn ? (w - 1) : dn;
-            T q = (up - lim + dn - 1) / dn;
-            if (q == 0) break;
-            // level i of the batch enters [0, up - i*dn): y -= dn whenever
-            // y >= up - i*dn, which, once true, stays true for later levels
-            T s;
-            if (y >= up) {
-                s = q;
-            } else {
-                T f = (up - y + dn - 1) / dn;
-                s = f < q ? q - f : 0;
-            }
-            y -= s * dn;
-            t += (uint64_t)s * kn;
-            up -= q * dn;
-            kp += q * kn;
-        } else {
-            const T lim = (w - 1) > up ? (w - 1) : up;
-            T q = (dn - lim + up - 1) / up;
-            if (q == 0) break;
-            // level i enters [0, dn - i*up) with one wrap y -= dn - i*up at the
-            // first level where y >= dn - i*up (after it y < up: no more)
-            T i = y >= dn ? 0 : (dn - y + up - 1) / up;
-            if (i < q) {
-                y -= dn - i * up;
-                t += kn + (uint64_t)i * kp;
-            }
-            dn -= q * up;
-            kn += q * kp;
+        const bool A = up > dn;
+        T big = A ? up : dn;
+        const T small = A ? dn : up;
+        T kbig = A ? kp : kn;
+        const T ksmall = A ? kn : kp;
+        const T lim = (w - 1) > small ? (w - 1) : small;
+        const T q = (big - lim + small - 1) / small;
+        if (q == 0) break;
+        const T f = y >= big ? (T)0 : (big - y + small - 1) / small;
+        if (f < q) {
+            const T dy = A ? (q - f) * small : big - f * small;
+            const uint64_t dt = A ? (uint64_t)(q - f) * ksmall : (uint64_t)kbig + (uint64_t)f * ksmall;
+            y -= dy;
+            t += dt;
         }
+        big -= q * small;
+        kbig += q * ksmall;
+        up = A ? big : small;
+        dn = A ? small : big;
+        kp = A ? kbig : ksmall;
+        kn = A ? ksmall : kbig;
+        if (t >= t_lim) return {t, y, {kp, up, kn, dn}};
     }
     if (y >= w) {  // last level: [0, up + dn) -> [0, w) by one wrap
         y -= dn;

@@ -14,6 +14,7 @@
 // as lanes free up and their device footprint fits a byte budget, and copies
 // each result back as its lane's completion event fires.
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <cmath>
 #include <condition_variable>
@@ -245,56 +246,129 @@ int prepare_table_job(pgs_ctx *ctx, const pgs_job &job, cudaStream_t s, pgs_prep
     return PGS_OK;
 }
 
-// All kernels of one job on one lane (asynchronous, capturable).
-int run_table_job(pgs_ctx *ctx, pgs_prepared *pr, Lane *lane) {
+// A group of jobs with the same P: their K = P#/d are all multiples of
+// K' = P#/L, L = lcm of their d, so one K' mod p pass per prime window serves
+// every job, each scaling it by L/d (two Montgomery products) as its walk
+// starts.  A group of one job uses its own K and walk-start mode.
+struct GroupPlan {
+    std::vector<int> jobs;          // indices into the batch
+    std::vector<uint32_t> klimbs;   // K' (groups of two or more)
+    std::vector<uint32_t> kmul;     // L/d per job
+    uint64_t cost = 0;
+    int lane = 0;
+};
+
+// Kernels of one group on one lane, asynchronous and capturable: each job's
+// setup (small primes, primes of d), then per table window one K' mod p pass
+// over the hull of the jobs' prime ranges and every job's large-prime kernel
+// reading from it, then each job's rows and text.  d_urange: 2 words per
+// window of the hull; d_klimbs: K' on the device (both unused for one job).
+int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
+              unsigned long long *d_urange, const uint32_t *d_klimbs = nullptr, int nl_shared = 0,
+              const std::vector<uint32_t> &kmul = {}) {
     const cudaStream_t s = lane->stream;
-    HostJob &h = pr->hj;
     PrimeTable &t = *ctx->table;
-    const uint64_t rows = h.valid_mi.size();
-    const pg::JobDev job = job_dev(pr);
-    pg::RowsDev rd = rows_dev(pr);
-    unsigned long long *misc = pr->misc.as<unsigned long long>();
-    rd.sp = t.small.as<uint32_t>();
-    rd.sp_base = 0;
-    rd.sp_range = misc + 1;
-    rd.sp_cap = pr->sp_bound;
-    const int nl = (int)h.klimbs.size();
-    uint64_t launches = 0;
-    CK(cudaMemsetAsync(pr->comp.p, 0, rows * h.pitch * 4ull, s));
-    CK(cudaMemsetAsync(pr->misc.p, 0, (1 + 2 * job_ranges(pr)) * 8, s));
-    CK(pg::set_pair(misc + 1, pr->tbl_a, pr->tbl_b, s));
-    launches++;
-    if (pr->sp_bound) {
-        CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, 0, t.small.as<uint32_t>(), misc + 1,
-                           pr->sp_bound, nullptr, pr->sr.p, pr->sp_t0.p, false, s));
-        launches++;
-    }
-    if (!h.dq.empty()) {
-        CK(pg::kmod_list32(pr->klimbs.as<uint32_t>(), nl, pr->dq.as<uint32_t>(),
-                           (uint32_t)h.dq.size(), pr->dr.as<uint32_t>(), s));
-        launches++;
-    }
     const pg::LargeScratch scratch{lane->ctr.as<unsigned long long>(), lane->heavy.as<pg::HeavyPrime>(),
                                    pg::heavy_capacity()};
-    for (size_t i = 0; i < pr->tbl_windows.size(); i++) {
-        const TableWindow &w = *t.windows[pr->tbl_windows[i]];
-        unsigned long long *rng = misc + 3 + 2 * i;
-        const bool wide = w.lo >= (1ull << 32);
-        CK(pg::find_range(w.off.as<uint32_t>(), w.count, w.lo, h.s1 + 1, h.prime_limit, rng, s));
-        CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, w.lo, w.off.as<uint32_t>(), rng, w.count,
-                           &h.walk, lane->r.p, lane->t0.p, wide, s));
-        CK(pg::large_window(job, w.lo, w.off.as<uint32_t>(), rng, w.count, lane->r.p, lane->t0.p, wide,
-                            pr->mmask.as<uint32_t>(), pr->xmask.as<uint32_t>(), scratch, s));
-        launches += 4;
+    uint64_t lo_val = ~0ull, hi_val = 0;
+    std::vector<int> windows;
+    for (pgs_prepared *pr : jobs) {
+        HostJob &h = pr->hj;
+        const uint64_t rows = h.valid_mi.size();
+        unsigned long long *misc = pr->misc.as<unsigned long long>();
+        const int nl = (int)h.klimbs.size();
+        pr->launches = 0;
+        CK(cudaMemsetAsync(pr->comp.p, 0, rows * h.pitch * 4ull, s));
+        CK(cudaMemsetAsync(pr->misc.p, 0, (1 + 2 * job_ranges(pr)) * 8, s));
+        CK(pg::set_pair(misc + 1, pr->tbl_a, pr->tbl_b, s));
+        pr->launches++;
+        if (pr->sp_bound) {
+            CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, 0, t.small.as<uint32_t>(), misc + 1,
+                               pr->sp_bound, nullptr, pr->sr.p, nullptr, false, s));
+            pr->launches++;
+        }
+        if (!h.dq.empty()) {
+            CK(pg::kmod_list32(pr->klimbs.as<uint32_t>(), nl, pr->dq.as<uint32_t>(),
+                               (uint32_t)h.dq.size(), pr->dr.as<uint32_t>(), s));
+            pr->launches++;
+        }
+        if (!pr->tbl_windows.empty()) {
+            lo_val = std::min(lo_val, h.s1 + 1);
+            hi_val = std::max(hi_val, h.prime_limit);
+        }
+        windows.insert(windows.end(), pr->tbl_windows.begin(), pr->tbl_windows.end());
     }
-    CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression), s));
-    CK(pg::scan_u64(pr->row_bytes.as<uint64_t>(), pr->offsets.as<uint64_t>(), pr->misc.as<uint64_t>(),
-                    rows, pr->scan_tmp.as<uint64_t>(), s));
-    CK(pg::format_rows(rd, pr->offsets.as<uint64_t>(), pr->text.as<char>(), s));
-    launches += 5;
-    pr->launches = launches;
-    pr->ran = true;
+    std::sort(windows.begin(), windows.end());
+    windows.erase(std::unique(windows.begin(), windows.end()), windows.end());
+    const bool shared = jobs.size() > 1;
+    for (size_t u = 0; u < windows.size(); u++) {
+        const TableWindow &w = *t.windows[windows[u]];
+        const bool wide = w.lo >= (1ull << 32);
+        // the jobs that sieve with this window, and their range slots
+        std::vector<std::pair<pgs_prepared *, size_t>> users;
+        std::vector<uint32_t> user_kmul;
+        for (size_t j = 0; j < jobs.size(); j++)
+            for (size_t i = 0; i < jobs[j]->tbl_windows.size(); i++)
+                if (jobs[j]->tbl_windows[i] == windows[u]) {
+                    users.push_back({jobs[j], i});
+                    user_kmul.push_back(shared ? kmul[j] : 1u);
+                }
+        pgs_prepared *lead = users.front().first;
+        unsigned long long *rr;
+        if (shared) {
+            rr = d_urange + 2 * u;
+            CK(pg::find_range(w.off.as<uint32_t>(), w.count, w.lo, lo_val, hi_val, rr, s));
+        } else {
+            rr = lead->misc.as<unsigned long long>() + 3 + 2 * users.front().second;
+            CK(pg::find_range(w.off.as<uint32_t>(), w.count, w.lo, lead->hj.s1 + 1, lead->hj.prime_limit,
+                              rr, s));
+        }
+        // one job: its walk step and start; a group: K' mod p, each job starts its own walk
+        if (shared)
+            CK(pg::kmod_window(d_klimbs, nl_shared, w.lo, w.off.as<uint32_t>(), rr, w.count, nullptr,
+                               lane->r.p, lane->t0.p, wide, s));
+        else
+            CK(pg::kmod_window(lead->klimbs.as<uint32_t>(), (int)lead->hj.klimbs.size(), w.lo,
+                               w.off.as<uint32_t>(), rr, w.count, &lead->hj.walk, lane->r.p, lane->t0.p,
+                               wide, s));
+        lead->launches += 2;
+        for (size_t k = 0; k < users.size(); k++) {
+            const auto &ui = users[k];
+            pgs_prepared *pr = ui.first;
+            pg::JobDev jd = job_dev(pr);
+            jd.kmul = user_kmul[k];
+            unsigned long long *rng = pr->misc.as<unsigned long long>() + 3 + 2 * ui.second;
+            if (shared) {
+                CK(pg::find_range(w.off.as<uint32_t>(), w.count, w.lo, pr->hj.s1 + 1, pr->hj.prime_limit,
+                                  rng, s));
+                pr->launches++;
+            }
+            CK(pg::large_window(jd, w.lo, w.off.as<uint32_t>(), rng, w.count, lane->r.p,
+                                lane->t0.p, rr, wide, shared, pr->mmask.as<uint32_t>(),
+                                pr->xmask.as<uint32_t>(), scratch, s));
+            pr->launches += 2;
+        }
+    }
+    for (pgs_prepared *pr : jobs) {
+        HostJob &h = pr->hj;
+        const uint64_t rows = h.valid_mi.size();
+        pg::RowsDev rd = rows_dev(pr);
+        rd.sp = t.small.as<uint32_t>();
+        rd.sp_base = 0;
+        rd.sp_range = pr->misc.as<unsigned long long>() + 1;
+        rd.sp_cap = pr->sp_bound;
+        CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression), s));
+        CK(pg::scan_u64(pr->row_bytes.as<uint64_t>(), pr->offsets.as<uint64_t>(), pr->misc.as<uint64_t>(),
+                        rows, pr->scan_tmp.as<uint64_t>(), s));
+        CK(pg::format_rows(rd, pr->offsets.as<uint64_t>(), pr->text.as<char>(), s));
+        pr->launches += 5;
+        pr->ran = true;
+    }
     return PGS_OK;
+}
+
+int run_table_job(pgs_ctx *ctx, pgs_prepared *pr, Lane *lane) {
+    return run_group(ctx, std::vector<pgs_prepared *>{pr}, lane, nullptr);
 }
 
 uint64_t job_cost(const HostJob &h) {
@@ -306,10 +380,127 @@ uint64_t job_cost(const HostJob &h) {
 
 }  // namespace
 
+namespace {
+
+// derive() for many jobs on up to 8 host threads.  Returns the first failing
+// job's status (and its message in err).
+int derive_all(const pgs_job *jobs, int n, std::vector<HostJob> &out, bool tables, std::string &err) {
+    out.assign(n, HostJob());
+    std::vector<int> rc(n, PGS_OK);
+    std::vector<std::string> msg(n);
+    std::atomic<int> next{0};
+    auto work = [&] {
+        for (int i; (i = next.fetch_add(1)) < n;) rc[i] = derive(jobs[i], out[i], msg[i], tables);
+    };
+    const int T = std::max(1, std::min({8, n, (int)std::thread::hardware_concurrency()}));
+    std::vector<std::thread> pool;
+    for (int t = 1; t < T; t++) pool.emplace_back(work);
+    work();
+    for (auto &t : pool) t.join();
+    for (int i = 0; i < n; i++)
+        if (rc[i] != PGS_OK) {
+            err = msg[i];
+            return rc[i];
+        }
+    return PGS_OK;
+}
+
+// P#/L as 32-bit limbs, for L a product of distinct primes <= P.
+std::vector<uint32_t> primorial_quotient(uint32_t P, uint64_t L) {
+    std::vector<uint32_t> limbs{1};
+    for (uint32_t q : primes_upto(P)) {
+        if (L % q == 0) continue;
+        uint64_t carry = 0;
+        for (auto &l : limbs) {
+            const uint64_t t = (uint64_t)l * q + carry;
+            l = (uint32_t)t;
+            carry = t >> 32;
+        }
+        if (carry) limbs.push_back((uint32_t)carry);
+    }
+    return limbs;
+}
+
+uint64_t gcd64(uint64_t a, uint64_t b) {
+    while (b) {
+        const uint64_t t = a % b;
+        a = b;
+        b = t;
+    }
+    return a;
+}
+
+// Jobs with the same P form a group sharing K' = P#/L (L = lcm of their d)
+// when every L/d fits 32 bits; otherwise jobs group by their exact K.
+// Groups go longest first onto the least-loaded lane; the result is in that
+// (launch) order.
+std::vector<GroupPlan> plan_groups(const std::vector<const HostJob *> &hj, int lanes) {
+    std::map<uint32_t, std::vector<int>> by_p;
+    for (int i = 0; i < (int)hj.size(); i++) by_p[hj[i]->job.p].push_back(i);
+    std::vector<GroupPlan> out;
+    for (auto &kv : by_p) {
+        uint64_t L = 1;
+        bool ok = kv.second.size() > 1;
+        for (int i : kv.second) {
+            const uint64_t d = hj[i]->job.d;
+            const uint64_t g = gcd64(L, d);
+            if (L / g > (~0ull >> 1) / d) {
+                ok = false;
+                break;
+            }
+            L = L / g * d;
+        }
+        for (int i : kv.second) ok = ok && L / hj[i]->job.d <= 0xFFFFFFFFull;
+        if (ok) {
+            GroupPlan gp;
+            gp.jobs = kv.second;
+            gp.klimbs = primorial_quotient(kv.first, L);
+            for (int i : kv.second) gp.kmul.push_back((uint32_t)(L / hj[i]->job.d));
+            out.push_back(std::move(gp));
+            continue;
+        }
+        std::map<uint32_t, GroupPlan> by_d;  // same K
+        for (int i : kv.second) {
+            GroupPlan &gp = by_d[hj[i]->job.d];
+            gp.jobs.push_back(i);
+            gp.kmul.push_back(1);
+            gp.klimbs = hj[i]->klimbs;
+        }
+        for (auto &dg : by_d) out.push_back(std::move(dg.second));
+    }
+    for (GroupPlan &gp : out)
+        for (int i : gp.jobs) gp.cost += job_cost(*hj[i]);
+    std::sort(out.begin(), out.end(), [](const GroupPlan &a, const GroupPlan &b) { return a.cost > b.cost; });
+    std::vector<uint64_t> load(lanes, 0);
+    for (GroupPlan &gp : out) {
+        gp.lane = (int)(std::min_element(load.begin(), load.end()) - load.begin());
+        load[gp.lane] += gp.cost;
+    }
+    return out;
+}
+
+// Device copies of the groups' K' limbs, packed; offsets per group.
+cudaError_t upload_group_limbs(const std::vector<GroupPlan> &groups, DevBuf &buf,
+                               std::vector<size_t> &offset, cudaStream_t s) {
+    std::vector<uint32_t> all;
+    offset.clear();
+    for (const GroupPlan &gp : groups) {
+        offset.push_back(all.size());
+        all.insert(all.end(), gp.klimbs.begin(), gp.klimbs.end());
+    }
+    return upload(buf, all, s);
+}
+
+}  // namespace
+
 struct pgs_batch {
     pgs_ctx *ctx = nullptr;
     std::vector<pgs_prepared *> jobs;
     std::vector<int> lane_of;
+    std::vector<GroupPlan> groups;         // in launch order
+    std::vector<size_t> group_urange;      // offset (words) of each group's hull ranges
+    std::vector<size_t> group_limbs;       // offset of each group's K' limbs
+    DevBuf urange, glimbs;
     int nlanes = 1;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
@@ -323,8 +514,12 @@ int launch_batch(pgs_ctx *ctx, pgs_batch *b) {
     Lane *l0 = ctx->lanes[0];
     CK(cudaEventRecord(b->fork, l0->stream));
     for (int l = 1; l < b->nlanes; l++) CK(cudaStreamWaitEvent(ctx->lanes[l]->stream, b->fork, 0));
-    for (size_t j = 0; j < b->jobs.size(); j++) {
-        int rc = run_table_job(ctx, b->jobs[j], ctx->lanes[b->lane_of[j]]);
+    for (size_t g = 0; g < b->groups.size(); g++) {
+        const GroupPlan &gp = b->groups[g];
+        std::vector<pgs_prepared *> jobs;
+        for (int j : gp.jobs) jobs.push_back(b->jobs[j]);
+        int rc = run_group(ctx, jobs, ctx->lanes[gp.lane], b->urange.as<unsigned long long>() + b->group_urange[g],
+                           b->glimbs.as<uint32_t>() + b->group_limbs[g], (int)gp.klimbs.size(), gp.kmul);
         if (rc) return rc;
     }
     for (int l = 1; l < b->nlanes; l++) {
@@ -350,16 +545,16 @@ int pgs_batch_prepare(pgs_ctx *ctx, const pgs_job *jobs, int n, int lanes, pgs_b
     std::lock_guard<std::mutex> g(ctx->mu);
     CK(cudaSetDevice(ctx->device));
     *out = nullptr;
+    std::vector<HostJob> hj;
+    int rc = derive_all(jobs, n, hj, true, ctx->err);
+    if (rc) return rc;
     // cover every job: large primes up to the largest limit, small up to the largest S1
     uint64_t limit = 3, small = kSmallMin;
-    for (int i = 0; i < n; i++) {
-        HostJob h;
-        int rc = derive(jobs[i], h, ctx->err, false);
-        if (rc) return rc;
+    for (const HostJob &h : hj) {
         limit = std::max(limit, h.prime_limit);
         small = std::max(small, std::min<uint64_t>(h.s1, h.prime_limit));
     }
-    int rc = table_extend(ctx, limit, small, ctx->stream);
+    rc = table_extend(ctx, limit, small, ctx->stream);
     if (rc) return rc;
     const int L = std::max(1, std::min(lanes, n));
     rc = ensure_lanes(ctx, L);
@@ -367,34 +562,45 @@ int pgs_batch_prepare(pgs_ctx *ctx, const pgs_job *jobs, int n, int lanes, pgs_b
     auto *b = new pgs_batch();
     b->ctx = ctx;
     b->nlanes = L;
-    std::vector<uint64_t> cost;
+    std::vector<const HostJob *> hp;
+    for (const HostJob &h : hj) hp.push_back(&h);
+    b->groups = plan_groups(hp, L);
+    const int G = (int)b->groups.size();
+    b->lane_of.assign(n, 0);
+    for (int g = 0; g < G; g++)
+        for (int j : b->groups[g].jobs) b->lane_of[j] = b->groups[g].lane;
+    b->glimbs.pool = &ctx->dpool;
+    cudaError_t le = upload_group_limbs(b->groups, b->glimbs, b->group_limbs, ctx->stream);
+    if (le != cudaSuccess) {
+        pgs_batch_free(b);
+        return fail(ctx, le, "batch group limbs");
+    }
     for (int i = 0; i < n; i++) {
         pgs_prepared *pr = nullptr;
-        rc = prepare_table_job(ctx, jobs[i], ctx->lanes[i % L]->stream, &pr);
+        rc = prepare_table_job(ctx, jobs[i], ctx->stream, &pr, &hj[i]);
         if (rc) {
             pgs_batch_free(b);
             return rc;
         }
         b->jobs.push_back(pr);
-        cost.push_back(job_cost(pr->hj));
     }
-    // longest job first onto the least-loaded lane
-    std::vector<int> order(n);
-    for (int i = 0; i < n; i++) order[i] = i;
-    std::sort(order.begin(), order.end(), [&](int a, int c) { return cost[a] > cost[c]; });
-    std::vector<uint64_t> load(L, 0);
-    b->lane_of.assign(n, 0);
-    for (int i : order) {
-        int best = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        load[best] += cost[i];
-        b->lane_of[i] = best;
+    size_t words = 0;
+    for (int g = 0; g < G; g++) {
+        b->group_urange.push_back(words);
+        words += 2 * ctx->table->windows.size();
+    }
+    b->urange.pool = &ctx->dpool;
+    cudaError_t ue = b->urange.ensure(std::max<size_t>(words, 2) * 8);
+    if (ue != cudaSuccess) {
+        pgs_batch_free(b);
+        return fail(ctx, ue, "batch ranges");
     }
     CK(cudaEventCreate(&b->t0));
     CK(cudaEventCreate(&b->t1));
     CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     b->joins.assign(L, nullptr);
     for (int l = 1; l < L; l++) CK(cudaEventCreateWithFlags(&b->joins[l], cudaEventDisableTiming));
-    for (int l = 0; l < L; l++) CK(cudaStreamSynchronize(ctx->lanes[l]->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
     *out = b;
     return PGS_OK;
 }
@@ -454,17 +660,97 @@ void pgs_batch_free(pgs_batch *b) {
     for (auto e : b->joins)
         if (e) cudaEventDestroy(e);
     for (auto *pr : b->jobs) delete pr;
+    b->urange.release();
+    b->glimbs.release();
     delete b;
 }
 
+// One pass, pipelined: host work (job tables) is done up front on several
+// threads, each group's uploads go on the context stream and its kernels on
+// its lane as soon as they are enqueued, and results are copied back group by
+// group as each finishes, while the other lanes still compute.
 int pgs_method2_batch(pgs_ctx *ctx, const pgs_job *jobs, int n, pgs_result *outs) {
-    if (!outs) return PGS_EINVAL;
-    pgs_batch *b = nullptr;
-    int rc = pgs_batch_prepare(ctx, jobs, n, 8, &b);
+    if (!ctx || !jobs || n <= 0 || !outs) return PGS_EINVAL;
+    for (int i = 0; i < n; i++) memset(&outs[i], 0, sizeof(pgs_result));
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    std::vector<HostJob> hj;
+    int rc = derive_all(jobs, n, hj, true, ctx->err);
     if (rc) return rc;
-    rc = pgs_batch_run(ctx, b, 0, nullptr);
-    for (int i = 0; rc == PGS_OK && i < n; i++) rc = pgs_batch_fetch(ctx, b, i, &outs[i]);
-    pgs_batch_free(b);
+    uint64_t limit = 3, small = kSmallMin;
+    for (const HostJob &h : hj) {
+        limit = std::max(limit, h.prime_limit);
+        small = std::max(small, std::min<uint64_t>(h.s1, h.prime_limit));
+    }
+    rc = table_extend(ctx, limit, small, ctx->stream);
+    if (rc) return rc;
+    const int L = std::max(1, std::min(8, n));
+    rc = ensure_lanes(ctx, L);
+    if (rc) return rc;
+    std::vector<const HostJob *> hp;
+    for (const HostJob &h : hj) hp.push_back(&h);
+    const std::vector<GroupPlan> groups = plan_groups(hp, L);
+    const int G = (int)groups.size();
+    const size_t nwin = ctx->table->windows.size();
+    DevBuf urange, glimbs;
+    urange.pool = glimbs.pool = &ctx->dpool;
+    std::vector<size_t> limb_off;
+    std::vector<pgs_prepared *> prs(n, nullptr);
+    std::vector<cudaEvent_t> up_done(G, nullptr), done(G, nullptr);
+    cudaStream_t up = ctx->stream;
+    auto cleanup = [&] {
+        for (Lane *l : ctx->lanes) cudaStreamSynchronize(l->stream);
+        cudaStreamSynchronize(up);
+        for (auto *pr : prs) delete pr;
+        for (auto e : up_done)
+            if (e) cudaEventDestroy(e);
+        for (auto e : done)
+            if (e) cudaEventDestroy(e);
+        urange.release();
+        glimbs.release();
+    };
+    cudaError_t e = urange.ensure(std::max<size_t>(2 * nwin * G, 2) * 8);
+    if (e == cudaSuccess) e = upload_group_limbs(groups, glimbs, limb_off, up);
+    for (int k = 0; k < G && e == cudaSuccess; k++) {
+        e = cudaEventCreateWithFlags(&up_done[k], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        cleanup();
+        return fail(ctx, e, "batch setup");
+    }
+    for (int grp = 0; grp < G && rc == PGS_OK; grp++) {
+        const GroupPlan &gp = groups[grp];
+        Lane *lane = ctx->lanes[gp.lane];
+        std::vector<pgs_prepared *> members;
+        for (int j : gp.jobs) {
+            rc = prepare_table_job(ctx, jobs[j], up, &prs[j], &hj[j]);
+            if (rc) break;
+            members.push_back(prs[j]);
+        }
+        if (rc) break;
+        if ((e = cudaEventRecord(up_done[grp], up)) || (e = cudaStreamWaitEvent(lane->stream, up_done[grp], 0))) {
+            rc = fail(ctx, e, "batch upload order");
+            break;
+        }
+        rc = run_group(ctx, members, lane, urange.as<unsigned long long>() + 2 * nwin * grp,
+                       glimbs.as<uint32_t>() + limb_off[grp], (int)gp.klimbs.size(), gp.kmul);
+        if (rc == PGS_OK && (e = cudaEventRecord(done[grp], lane->stream))) rc = fail(ctx, e, "batch event");
+    }
+    // results, group by group in launch order, on the upload stream
+    for (int grp = 0; grp < G && rc == PGS_OK; grp++) {
+        if ((e = cudaStreamWaitEvent(up, done[grp], 0))) {
+            rc = fail(ctx, e, "batch fetch order");
+            break;
+        }
+        for (int j : groups[grp].jobs) {
+            rc = fetch_job(ctx, prs[j], up, &outs[j]);
+            if (rc) break;
+        }
+    }
+    if (rc != PGS_OK)
+        for (int i = 0; i < n; i++) pgs_result_free(&outs[i]);
+    cleanup();
     return rc;
 }
 

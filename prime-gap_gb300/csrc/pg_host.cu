@@ -247,6 +247,7 @@ pg::JobDev job_dev(pgs_prepared *pr) {
     j.col_of_x = pr->col_of_x.as<int32_t>();
     j.comp = pr->comp.as<uint32_t>();
     j.walk = h.walk;
+    j.kmul = 1;
     return j;
 }
 

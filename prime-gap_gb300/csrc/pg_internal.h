@@ -54,14 +54,14 @@ cudaError_t set_pair(unsigned long long *d_out, uint64_t a, uint64_t b, cudaStre
 // ---- K mod p (pg_kmod.cu) ---------------------------------------------------
 
 // For primes base + off[i], i in [d_range[0], d_range[1]) (device values,
-// at most max_count of them): with walk == nullptr write
-// r[i] = K mod p; otherwise write the parity-reduced walk step (r or r/2) and
-// its start residue t0[i] (see WalkParams).  Primes below 2^32 use 32-bit
-// words, others 64-bit (wide).  K limbs on the device.
+// at most max_count of them), at index i - d_range[0]: with walk == nullptr,
+// a = K mod p and, when d_b is given, b = R^2 mod p (R = 2^32 or 2^64); with
+// a walk, a = the walk step and b = its start residue (all words of the
+// primes' width).  Primes below 2^32 use 32-bit words, others 64-bit
+// (wide).  K limbs on the device.
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
                         const unsigned long long *d_range, uint64_t max_count,
-                        const WalkParams *walk, void *d_r, void *d_t0, bool wide,
-                        cudaStream_t stream);
+                        const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream);
 
 // K mod q for an explicit list of 32-bit primes (d-primes, tests).
 cudaError_t kmod_list32(const uint32_t *d_klimbs, int nlimbs, const uint32_t *d_q, uint32_t n,
@@ -82,6 +82,7 @@ struct JobDev {
     const int32_t *col_of_x;   // 2*SL+1 entries, -1 if not a live offset
     uint32_t *comp;            // rows * pitch words
     WalkParams walk;           // parity-reduced large-prime walk
+    uint32_t kmul;             // K = K' * kmul when the walk starts from K' mod p (else 1)
 };
 
 struct HeavyPrime;
@@ -96,10 +97,15 @@ uint32_t heavy_capacity();
 constexpr size_t kHeavyPrimeBytes = 40;
 
 // d_mmask: valid-m bitmask (minc bits); d_xmask: live-offset bitmask (2SL+1 bits).
+// d_a/d_b as written by kmod_window over the index range d_rrange, which
+// contains d_range: with start_in_kernel, K mod p and 2^64 mod p (jobs that
+// share K share them; each starts its walk here), else the job's walk step
+// and start residue.
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
-                         const unsigned long long *d_range, uint64_t max_count, const void *d_r,
-                         const void *d_t0, bool wide, const uint32_t *d_mmask,
-                         const uint32_t *d_xmask, LargeScratch scratch, cudaStream_t stream);
+                         const unsigned long long *d_range, uint64_t max_count, const void *d_a,
+                         const void *d_b, const unsigned long long *d_rrange, bool wide,
+                         bool start_in_kernel, const uint32_t *d_mmask, const uint32_t *d_xmask,
+                         LargeScratch scratch, cudaStream_t stream);
 
 // ---- rows: small primes, merge, extract, format (pg_rows.cu) -----------------
 

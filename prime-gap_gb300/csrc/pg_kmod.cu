@@ -2,13 +2,16 @@
 // K = P#/d against 32-bit and 64-bit primes by Montgomery multiplication.
 //
 // Replaces mpz_fdiv_ui(K, prime) at combined_sieve.cpp:1497 and 1856 (and the
-// mpz_mod_ui of 1674).  One thread per prime walks the limbs of K from the
-// most significant end: u <- REDC(u * R^2 + limb), so after the last limb
-// u = K * R^-1 and REDC(u * R^2) = K mod p.  K's limbs sit in shared memory
-// and are read as warp-wide broadcasts.
+// mpz_mod_ui of 1674).  One thread per prime (four interleaved chains per
+// thread for 32-bit primes) reduces K's limbs, least significant first for
+// long K (W <- REDC(W + limb), then one multiply by R^(n+1) mod p) and most
+// significant first for short K (u <- REDC(u * R^2 + limb)).  K's limbs sit in
+// shared memory and are read as warp-wide broadcasts.
 //
-// Each prime also gets t0 = (r * mstart + SL) mod p, the starting residue of
-// the large-prime walk ((base_r * M + SL) % prime, modulo_search.cpp:345).
+// Output, per prime: either r = K mod p and r2 = R^2 mod p (R = 2^32 or 2^64
+// by the primes' width), from which a kernel can start any job's walk over
+// this K without a division; or, for one job, its walk step and start residue directly
+// ((base_r * M + SL) % prime, modulo_search.cpp:345; see WalkParams).
 #include "pg_arith.cuh"
 #include "pg_internal.h"
 
@@ -19,12 +22,14 @@ namespace {
 constexpr int kKmodThreads = 256;
 constexpr int kMaxSharedLimbs = 12288;  // 48 KiB
 constexpr int kPrimesPerThread = 4;     // 32-bit primes
+constexpr int kLsbMinLimbs = 32;        // 32-bit primes: LSB chain from 32 limbs
+constexpr int kLsbMinLimbsWide = 24;    // 64-bit primes: from 12 words
 
-template <bool kWide>
+template <bool kWide, bool kLsb>
 __global__ void __launch_bounds__(kKmodThreads)
     kmod_kernel(const uint32_t *__restrict__ klimbs, int nlimbs, uint64_t base,
                 const uint32_t *__restrict__ off, const unsigned long long *range,
-                uint64_t max_count, WalkParams walk, int with_walk, void *r_out, void *t0_out) {
+                uint64_t max_count, WalkParams walk, int with_walk, void *a_out, void *b_out) {
     extern __shared__ uint32_t s_limbs[];
     const bool in_shared = nlimbs <= kMaxSharedLimbs;
     if (in_shared)
@@ -44,34 +49,28 @@ __global__ void __launch_bounds__(kKmodThreads)
 #pragma unroll
         for (int k = 0; k < kPrimesPerThread; k++)
             p[k] = idx0 + k < n ? (uint32_t)(base + off[idx0 + k]) : 3u;  // pad with a prime
-        kmod32_multi<kPrimesPerThread>(limbs, nlimbs, p, r, pinv, r2);
+        if (kLsb)
+            kmod32_lsb_multi<kPrimesPerThread>(limbs, nlimbs, p, r, pinv, r2);
+        else
+            kmod32_multi<kPrimesPerThread>(limbs, nlimbs, p, r, pinv, r2);
 #pragma unroll
         for (int k = 0; k < kPrimesPerThread; k++) {
             if (idx0 + k >= n) break;
-            if (!with_walk) {
-                ((uint32_t *)r_out)[idx0 + k] = r[k];
-                continue;
-            }
-            const uint32_t rh = half_mod(r[k], p[k]);
-            const uint32_t c = walk.c_add + (walk.odd_d ? (p[k] >> 1) + 1 : 0u);
-            ((uint32_t *)r_out)[idx0 + k] = walk.odd_d ? rh : r[k];
-            ((uint32_t *)t0_out)[idx0 + k] = start32(rh, walk.m0, c, p[k], pinv[k], r2[k]);
+            uint32_t a = r[k], b = r2[k];
+            if (with_walk) walk_start(walk, p[k], r[k], r2[k], a, b);
+            ((uint32_t *)a_out)[idx0 + k] = a;
+            if (b_out) ((uint32_t *)b_out)[idx0 + k] = b;
         }
     } else {
         const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
         if (idx >= n) return;
         const uint64_t p = base + off[idx];
-        const uint64_t r = kmod64(limbs, nlimbs, p);
-        if (!with_walk) {
-            ((uint64_t *)r_out)[idx] = r;
-            return;
-        }
-        const uint64_t rh = half_mod(r, p);
-        const uint64_t c = walk.c_add + (walk.odd_d ? (p >> 1) + 1 : 0ull);
-        uint64_t t = mulmod_u64(rh, walk.m0 % p, p, 1.0 / (double)p) + c;
-        if (t >= p) t -= p;
-        ((uint64_t *)r_out)[idx] = walk.odd_d ? rh : r;
-        ((uint64_t *)t0_out)[idx] = t;
+        uint64_t pinv, r2;
+        const uint64_t r = kLsb ? kmod64_lsb(limbs, nlimbs, p, &pinv, &r2) : kmod64(limbs, nlimbs, p, &pinv, &r2);
+        uint64_t a = r, b = r2;
+        if (with_walk) walk_start(walk, p, r, pinv, r2, a, b);
+        ((uint64_t *)a_out)[idx] = a;
+        if (b_out) ((uint64_t *)b_out)[idx] = b;
     }
 }
 
@@ -88,21 +87,28 @@ __global__ void __launch_bounds__(kKmodThreads)
 
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
                         const unsigned long long *d_range, uint64_t max_count,
-                        const WalkParams *walk, void *d_r, void *d_t0, bool wide,
-                        cudaStream_t stream) {
-    const WalkParams wp = walk ? *walk : WalkParams{};
-    const int with_walk = walk != nullptr;
+                        const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream) {
     if (max_count == 0) return cudaSuccess;
+    const WalkParams wp = walk ? *walk : WalkParams{};
+    const int ww = walk != nullptr;
     const uint64_t per_thread = wide ? 1 : kPrimesPerThread;
     const uint64_t threads = (max_count + per_thread - 1) / per_thread;
-    uint64_t blocks = (threads + kKmodThreads - 1) / kKmodThreads;
-    size_t smem = nlimbs <= kMaxSharedLimbs ? (size_t)nlimbs * sizeof(uint32_t) : 0;
-    if (wide)
-        kmod_kernel<true><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(
-            d_klimbs, nlimbs, base, d_off, d_range, max_count, wp, with_walk, d_r, d_t0);
+    const unsigned blocks = (unsigned)((threads + kKmodThreads - 1) / kKmodThreads);
+    const size_t smem = nlimbs <= kMaxSharedLimbs ? (size_t)nlimbs * sizeof(uint32_t) : 0;
+    // least significant limb first once the chain outweighs the R^(n+1) power
+    const bool lsb = nlimbs >= (wide ? kLsbMinLimbsWide : kLsbMinLimbs);
+    if (wide && lsb)
+        kmod_kernel<true, true><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
+                                                                        d_range, max_count, wp, ww, d_a, d_b);
+    else if (wide)
+        kmod_kernel<true, false><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
+                                                                         d_range, max_count, wp, ww, d_a, d_b);
+    else if (lsb)
+        kmod_kernel<false, true><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
+                                                                         d_range, max_count, wp, ww, d_a, d_b);
     else
-        kmod_kernel<false><<<(unsigned)blocks, kKmodThreads, smem, stream>>>(
-            d_klimbs, nlimbs, base, d_off, d_range, max_count, wp, with_walk, d_r, d_t0);
+        kmod_kernel<false, false><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
+                                                                          d_range, max_count, wp, ww, d_a, d_b);
     return cudaGetLastError();
 }
 

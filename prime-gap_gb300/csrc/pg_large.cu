@@ -72,6 +72,7 @@ struct Slots {
     T kp[kLargeThreads];
     T kn[kLargeThreads];
     uint32_t start[kLargeThreads + 1];
+    uint32_t warp_total[kLargeThreads / 32];
 };
 
 __device__ __forceinline__ void load_masks(const JobDev &job, const uint32_t *g_mmask,
@@ -91,11 +92,12 @@ __device__ __forceinline__ void load_masks(const JobDev &job, const uint32_t *g_
     __syncthreads();
 }
 
-template <typename T>
+template <typename T, bool kStartIn>
 __global__ void __launch_bounds__(kLargeThreads)
     large_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
-                 const unsigned long long *range, uint64_t max_count, const T *__restrict__ r_in,
-                 const T *__restrict__ t0_in, const uint32_t *__restrict__ g_mmask,
+                 const unsigned long long *range, uint64_t max_count, const T *__restrict__ a_in,
+                 const void *__restrict__ b_in, const unsigned long long *rrange,
+                 const uint32_t *__restrict__ g_mmask,
                  const uint32_t *__restrict__ g_xmask, int masks_in_shared,
                  unsigned long long *group_ctr, HeavyPrime *heavy, unsigned long long *heavy_count,
                  uint32_t heavy_cap) {
@@ -107,6 +109,8 @@ __global__ void __launch_bounds__(kLargeThreads)
     const Marker mark{job, mmask, xmask};
     const uint64_t n = min((uint64_t)(range[1] - range[0]), max_count);
     off += range[0];
+    a_in += range[0] - rrange[0];
+    const T *b = (const T *)b_in + (range[0] - rrange[0]);  // R^2 mod p, or the start residue
     const T w = (T)job.walk.w;
     const uint64_t minc = job.walk.jmax;  // the walk runs over j, not mi
 
@@ -119,8 +123,14 @@ __global__ void __launch_bounds__(kLargeThreads)
         uint32_t items = 0;
         if (i < n) {
             const T p = (T)(base + off[i]);
-            const T r = r_in[i];
-            const Entry<T> e = first_entry<T>(p, r, w, t0_in[i]);
+            T step, t0;
+            if constexpr (!kStartIn)
+                step = a_in[i], t0 = b[i];
+            else if constexpr (sizeof(T) == 4)
+                walk_start(job.walk, p, a_in[i], b[i], step, t0, job.kmul);
+            else
+                walk_start(job.walk, p, a_in[i], neg_inv64(p), b[i], step, t0, job.kmul);
+            const Entry<T> e = first_entry<T>(p, step, w, t0, minc);
             if (e.t < minc && e.y < w) {
                 const uint64_t bound = rotation_steps_bound<T>(e.t, minc, e.g, p);
                 bool local = true;
@@ -149,17 +159,28 @@ __global__ void __launch_bounds__(kLargeThreads)
                 }
             }
         }
-        // exclusive scan of item counts
-        sl.start[threadIdx.x + 1] = items;
+        // exclusive scan of item counts (skipped when the group has none):
+        // shuffle scan within each warp, then the warps' totals
+        if (!__syncthreads_or(items != 0)) continue;
+        const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+        uint32_t incl = items;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
+        }
+        if (lane == 31) sl.warp_total[warp] = incl;
+        __syncthreads();
+        uint32_t before = 0, total = 0;
+#pragma unroll
+        for (int k = 0; k < kLargeThreads / 32; k++) {
+            const uint32_t t = sl.warp_total[k];
+            before += k < (int)warp ? t : 0u;
+            total += t;
+        }
+        sl.start[threadIdx.x + 1] = before + incl;
         if (threadIdx.x == 0) sl.start[0] = 0;
         __syncthreads();
-        for (int o = 1; o < kLargeThreads; o <<= 1) {
-            uint32_t v = threadIdx.x >= (uint32_t)o ? sl.start[threadIdx.x + 1 - o] : 0;
-            __syncthreads();
-            sl.start[threadIdx.x + 1] += v;
-            __syncthreads();
-        }
-        const uint32_t total = sl.start[kLargeThreads];
         for (uint32_t it = threadIdx.x; it < total; it += kLargeThreads) {
             uint32_t lo = 0, hi = kLargeThreads;
             while (hi - lo > 1) {
@@ -209,9 +230,10 @@ __global__ void __launch_bounds__(kLargeThreads)
 uint32_t heavy_capacity() { return 1u << 20; }
 
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
-                         const unsigned long long *d_range, uint64_t max_count, const void *d_r,
-                         const void *d_t0, bool wide, const uint32_t *d_mmask,
-                         const uint32_t *d_xmask, LargeScratch scratch, cudaStream_t stream) {
+                         const unsigned long long *d_range, uint64_t max_count, const void *d_a,
+                         const void *d_b, const unsigned long long *d_rrange, bool wide,
+                         bool start_in_kernel, const uint32_t *d_mmask, const uint32_t *d_xmask,
+                         LargeScratch scratch, cudaStream_t stream) {
     if (max_count == 0) return cudaSuccess;
     const size_t mask_bytes = 4ull * ((job.minc + 31) / 32 + (job.two_sl + 1 + 31) / 32);
     const int in_shared = mask_bytes <= 96 * 1024;
@@ -231,19 +253,25 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kLargeThreads, smem);
         return cudaSuccess;
     };
-    if ((e = wide ? prep(large_kernel<uint64_t>) : prep(large_kernel<uint32_t>))) return e;
-    if (per_sm < 1) per_sm = 1;
-    uint64_t groups = (max_count + kLargeThreads - 1) / kLargeThreads;
-    uint64_t blocks = (uint64_t)sms * per_sm;
-    if (blocks > groups) blocks = groups;
+    auto launch = [&](auto kernel, const auto *a) -> cudaError_t {
+        cudaError_t err = prep(kernel);
+        if (err) return err;
+        if (per_sm < 1) per_sm = 1;
+        const uint64_t groups = (max_count + kLargeThreads - 1) / kLargeThreads;
+        uint64_t blocks = (uint64_t)sms * per_sm;
+        if (blocks > groups) blocks = groups;
+        kernel<<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
+            job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_xmask, in_shared,
+            group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
+        return cudaSuccess;
+    };
     if (wide)
-        large_kernel<uint64_t><<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            job, base, d_off, d_range, max_count, (const uint64_t *)d_r, (const uint64_t *)d_t0,
-            d_mmask, d_xmask, in_shared, group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
+        e = start_in_kernel ? launch(large_kernel<uint64_t, true>, (const uint64_t *)d_a)
+                            : launch(large_kernel<uint64_t, false>, (const uint64_t *)d_a);
     else
-        large_kernel<uint32_t><<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            job, base, d_off, d_range, max_count, (const uint32_t *)d_r, (const uint32_t *)d_t0,
-            d_mmask, d_xmask, in_shared, group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
+        e = start_in_kernel ? launch(large_kernel<uint32_t, true>, (const uint32_t *)d_a)
+                            : launch(large_kernel<uint32_t, false>, (const uint32_t *)d_a);
+    if (e) return e;
     if ((e = cudaGetLastError())) return e;
     if ((e = prep(heavy_kernel))) return e;
     if (per_sm < 1) per_sm = 1;

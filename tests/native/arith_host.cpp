@@ -180,6 +180,49 @@ void ah_first_entry(uint64_t p, uint64_t a, uint64_t w, uint64_t y0, uint64_t *o
     }
 }
 
+// first_entry with an early stop at t_lim: out = {t, y, kp, up, kn, dn}
+void ah_first_entry_lim(uint64_t p, uint64_t a, uint64_t w, uint64_t y0, uint64_t t_lim,
+                        uint64_t *out6) {
+    if (p < 0xFFFFFFFFull) {
+        auto e = pg::first_entry<uint32_t>((uint32_t)p, (uint32_t)a, (uint32_t)w, (uint32_t)y0, t_lim);
+        out6[0] = e.t, out6[1] = e.y, out6[2] = e.g.kp, out6[3] = e.g.up, out6[4] = e.g.kn,
+        out6[5] = e.g.dn;
+    } else {
+        auto e = pg::first_entry<uint64_t>(p, a, w, y0, t_lim);
+        out6[0] = e.t, out6[1] = e.y, out6[2] = e.g.kp, out6[3] = e.g.up, out6[4] = e.g.kn,
+        out6[5] = e.g.dn;
+    }
+}
+
+// least-significant-first K mod q: 4 interleaved 32-bit chains, or the 64-bit word chain
+void ah_kmod4_lsb(const uint32_t *limbs, int n, const uint32_t *q4, uint32_t *out4, uint32_t *r2_4) {
+    uint32_t pinv[4];
+    pg::kmod32_lsb_multi<4>(limbs, n, q4, out4, pinv, r2_4);
+}
+
+uint64_t ah_kmod64_lsb(const uint32_t *limbs, int n, uint64_t q) { return pg::kmod64_lsb(limbs, n, q); }
+
+// walk step and start residue from r = K mod p: out = {step, t0}
+void ah_walk_start(uint64_t p, uint64_t r, uint64_t m0, uint32_t c_add, uint32_t odd_d, uint64_t *out2) {
+    pg::WalkParams wk{};
+    wk.m0 = m0;
+    wk.c_add = c_add;
+    wk.odd_d = odd_d;
+    if (p < 0xFFFFFFFFull) {
+        const uint32_t r1 = (uint32_t)((1ull << 32) % p);
+        const uint32_t r2 = (uint32_t)(((uint64_t)r1 * r1) % p);
+        uint32_t step, t0;
+        pg::walk_start(wk, (uint32_t)p, (uint32_t)r, r2, step, t0);
+        out2[0] = step, out2[1] = t0;
+    } else {
+        const uint64_t r1 = (0ull - p) % p;
+        const uint64_t r2 = (uint64_t)(((unsigned __int128)r1 * r1) % p);
+        uint64_t step, t0;
+        pg::walk_start(wk, p, r, pg::neg_inv64(p), r2, step, t0);
+        out2[0] = step, out2[1] = t0;
+    }
+}
+
 uint64_t ah_kmod(const uint32_t *limbs, int n, uint64_t q) {
     if (q < 0x80000000ull) {
         uint32_t pinv, r2;

@@ -38,6 +38,8 @@ def ah(built):
                                   ctypes.POINTER(u64), ctypes.c_size_t]
     lib.ah_first_entry.restype = None
     lib.ah_first_entry.argtypes = [u64, u64, u64, u64, ctypes.POINTER(u64)]
+    lib.ah_first_entry_lim.restype = None
+    lib.ah_first_entry_lim.argtypes = [u64, u64, u64, u64, u64, ctypes.POINTER(u64)]
     lib.ah_kmod.restype = u64
     lib.ah_kmod.argtypes = [ctypes.POINTER(ctypes.c_uint32), ctypes.c_int, u64]
     lib.ah_start32.restype = ctypes.c_uint32
@@ -216,6 +218,33 @@ def test_first_entry_brute(ah):
         assert (kp, up, kn, dn) == (k_up, (k_up * a) % p, k_dn, p - (k_dn * a) % p)
 
 
+def test_first_entry_early_stop(ah):
+    """With t_lim, the search either returns the full answer (first hit below
+    t_lim) or stops with t >= t_lim exactly when the first hit is >= t_lim."""
+    rng = random.Random(19)
+    full = (ctypes.c_uint64 * 6)()
+    lim = (ctypes.c_uint64 * 6)()
+    stopped = 0
+    for _ in range(3000):
+        bits = rng.choice([16, 24, 31, 32, 40, 45])
+        p = _rand_prime(rng, 2 ** (bits - 1), 2 ** bits)
+        w = rng.choice([3, 101, 2001, 20001, 40001])
+        if w >= p // 2:
+            continue
+        a = rng.randrange(1, p)
+        y0 = rng.randrange(0, p)
+        ah.ah_first_entry(p, a, w, y0, full)
+        t_true = full[0]
+        t_lim = rng.choice([0, 1, t_true, t_true + 1, rng.randrange(0, 2 * t_true + 2), 2**64 - 1])
+        ah.ah_first_entry_lim(p, a, w, y0, t_lim, lim)
+        if t_true < t_lim:
+            assert list(lim) == list(full), (p, a, w, y0, t_lim)
+        else:
+            assert lim[0] >= t_lim, (p, a, w, y0, t_lim)
+            stopped += 1
+    assert stopped > 500
+
+
 def test_first_entry_wide(ah):
     """64-bit moduli against the oracle's Euclid search."""
     rng = random.Random(17)
@@ -261,6 +290,35 @@ def test_kmod4_interleaved(ah):
                 assert list(out) == [pgo.k_mod(limbs, q) for q in qs]
 
 
+def test_kmod_lsb_vs_oracle(ah):
+    """Least-significant-limb-first chains (32-bit x4 and 64-bit words)."""
+    u32p = ctypes.POINTER(ctypes.c_uint32)
+    ah.ah_kmod4_lsb.restype = None
+    ah.ah_kmod4_lsb.argtypes = [u32p, ctypes.c_int, u32p, u32p, u32p]
+    ah.ah_kmod64_lsb.restype = ctypes.c_uint64
+    ah.ah_kmod64_lsb.argtypes = [u32p, ctypes.c_int, ctypes.c_uint64]
+    rng = random.Random(23)
+    for P, d in [(503, 210), (1009, 1), (1511, 2190), (3001, 2190), (3001, 30030), (7, 7)]:
+        limbs = pgo.build_k(P, d)
+        arr = (ctypes.c_uint32 * len(limbs))(*limbs)
+        for lo, hi in [(P + 1, 10**5), (2**30, 2**31), (2**31, 2**32 - 5)]:
+            for _ in range(15):
+                qs = [_rand_prime(rng, max(lo, 3), hi) for _ in range(4)]
+                out = (ctypes.c_uint32 * 4)()
+                r2 = (ctypes.c_uint32 * 4)()
+                ah.ah_kmod4_lsb(arr, len(limbs), (ctypes.c_uint32 * 4)(*qs), out, r2)
+                assert list(out) == [pgo.k_mod(limbs, q) for q in qs], (P, d, qs)
+                assert list(r2) == [pow(2, 64, q) for q in qs]
+        for q in [4294967291] + [_rand_prime(rng, 2**32, 2**46) for _ in range(30)]:
+            assert ah.ah_kmod64_lsb(arr, len(limbs), q) == pgo.k_mod(limbs, q), (P, d, q)
+        # odd limb counts and the largest 32-bit prime
+        out = (ctypes.c_uint32 * 4)()
+        r2 = (ctypes.c_uint32 * 4)()
+        qs = [4294967291, 4294967279, 3, 5]
+        ah.ah_kmod4_lsb(arr, len(limbs), (ctypes.c_uint32 * 4)(*qs), out, r2)
+        assert list(out) == [pgo.k_mod(limbs, q) for q in qs]
+
+
 def test_kmod_against_python_bignum(built):
     from sympy import primorial
 
@@ -278,6 +336,24 @@ def test_start32(ah):
         M = rng.randrange(1, 10**10 + 1)
         sl = rng.randrange(0, min(p, 100000))
         assert ah.ah_start32(r, M, sl, p) == (r * M + sl) % p
+
+
+def test_walk_start(ah):
+    """Step and start residue of the parity-reduced walk (32- and 64-bit)."""
+    ah.ah_walk_start.restype = None
+    ah.ah_walk_start.argtypes = [ctypes.c_uint64] * 3 + [ctypes.c_uint32] * 2 + [ctypes.POINTER(ctypes.c_uint64)]
+    rng = random.Random(29)
+    out = (ctypes.c_uint64 * 2)()
+    for _ in range(1500):
+        p = _rand_prime(rng, 3, rng.choice([2**20, 2**32 - 5, 2**46]))
+        r = rng.randrange(0, p)
+        m0 = rng.randrange(1, 10**10 + 1)
+        c_add = rng.randrange(0, min(p // 8 + 1, 50000))
+        odd = rng.randrange(2)
+        ah.ah_walk_start(p, r, m0, c_add, odd, out)
+        rh = r * pow(2, -1, p) % p
+        c = c_add + ((p + 1) // 2 if odd else 0)
+        assert list(out) == [rh if odd else r, (rh * m0 + c) % p], (p, r, m0, c_add, odd)
 
 
 def test_mulmod(ah):
