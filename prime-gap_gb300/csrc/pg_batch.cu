@@ -246,6 +246,14 @@ int prepare_table_job(pgs_ctx *ctx, const pgs_job &job, cudaStream_t s, pgs_prep
     return PGS_OK;
 }
 
+// K mod p already resident for every prime of some table windows (the
+// request server's cache), indexed by table window: K mod p, R^2 mod p and the
+// device range {0, count} of the whole window.
+struct ResidueSource {
+    std::vector<const void *> a, b;
+    std::vector<const unsigned long long *> full;
+};
+
 // A group of jobs with the same P: their K = P#/d are all multiples of
 // K' = P#/L, L = lcm of their d, so one K' mod p pass per prime window serves
 // every job, each scaling it by L/d (two Montgomery products) as its walk
@@ -265,7 +273,7 @@ struct GroupPlan {
 // window of the hull; d_klimbs: K' on the device (both unused for one job).
 int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
               unsigned long long *d_urange, const uint32_t *d_klimbs = nullptr, int nl_shared = 0,
-              const std::vector<uint32_t> &kmul = {}) {
+              const std::vector<uint32_t> &kmul = {}, const ResidueSource *src = nullptr) {
     const cudaStream_t s = lane->stream;
     PrimeTable &t = *ctx->table;
     const pg::LargeScratch scratch{lane->ctr.as<unsigned long long>(), lane->heavy.as<pg::HeavyPrime>(),
@@ -314,6 +322,17 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
                     user_kmul.push_back(shared ? kmul[j] : 1u);
                 }
         pgs_prepared *lead = users.front().first;
+        if (src) {  // one job, K mod p resident for the whole window
+            unsigned long long *rng = lead->misc.as<unsigned long long>() + 3 + 2 * users.front().second;
+            CK(pg::find_range(w.off.as<uint32_t>(), w.count, w.lo, lead->hj.s1 + 1, lead->hj.prime_limit,
+                              rng, s));
+            const int k = windows[u];
+            CK(pg::large_window(job_dev(lead), w.lo, w.off.as<uint32_t>(), rng, w.count, src->a[k], src->b[k],
+                                src->full[k], wide, true, lead->mmask.as<uint32_t>(),
+                                lead->xmask.as<uint32_t>(), scratch, s));
+            lead->launches += 3;
+            continue;
+        }
         unsigned long long *rr;
         if (shared) {
             rr = d_urange + 2 * u;
@@ -769,6 +788,28 @@ int pgs_method2_batch(pgs_ctx *ctx, const pgs_job *jobs, int n, pgs_result *outs
 
 namespace {
 
+// Served requests with the same (P, d) share K mod p: computed once per
+// table window (for all its primes) on first use and kept, least recently
+// used first out, within a byte budget.  R^2 mod p depends on p alone and is
+// kept once per window.
+struct KEntry {
+    DevBuf limbs;
+    int nl = 0;
+    std::vector<DevBuf> r;          // per table window
+    std::vector<cudaEvent_t> ready; // per table window, recorded after the fill
+    size_t bytes = 0;
+    uint64_t last = 0;
+    int refs = 0;
+};
+struct WinShared {
+    DevBuf r2, full;
+    cudaEvent_t ready = nullptr;
+};
+
+}  // namespace
+
+namespace {
+
 struct Request {
     uint64_t ticket = 0;
     pgs_job job{};
@@ -779,6 +820,7 @@ struct Request {
     uint64_t footprint = 0;
     HostJob *hj = nullptr;  // derived once, at the head of the queue
     int derive_rc = 1;
+    KEntry *kentry = nullptr;  // cache entry in use
     ~Request() { delete hj; }
 };
 
@@ -787,6 +829,10 @@ struct Request {
 struct pgs_server {
     pgs_ctx *ctx = nullptr;
     uint64_t budget = 0;
+    // K mod p cache (dispatcher thread; refs under mu)
+    std::map<std::pair<uint32_t, uint32_t>, KEntry *> kcache;
+    std::vector<WinShared> wins;
+    uint64_t kcache_bytes = 0, kcache_budget = 0, kclock = 0, kfills = 0, khits = 0;
     int nlanes = 1;
     std::mutex mu;
     std::condition_variable cv_done;
@@ -807,6 +853,100 @@ struct pgs_server {
 
 namespace {
 
+// The (P, d) entry of the K mod p cache, created on first use.
+KEntry *kcache_get(pgs_server *srv, const HostJob &h, cudaStream_t s, cudaError_t &e) {
+    const auto key = std::make_pair(h.job.p, h.job.d);
+    auto it = srv->kcache.find(key);
+    if (it != srv->kcache.end()) return it->second;
+    auto *ke = new KEntry();
+    ke->limbs.pool = &srv->ctx->dpool;
+    ke->nl = (int)h.klimbs.size();
+    e = upload(ke->limbs, h.klimbs, s);
+    if (e != cudaSuccess) {
+        ke->limbs.release();
+        delete ke;
+        return nullptr;
+    }
+    srv->kcache[key] = ke;
+    return ke;
+}
+
+void kentry_free(KEntry *ke) {
+    for (auto &b : ke->r) b.release();
+    for (auto ev : ke->ready)
+        if (ev) cudaEventDestroy(ev);
+    ke->limbs.release();
+    delete ke;
+}
+
+// Make K mod p of every window the job uses resident (filling missing
+// windows on stream s) and order s after the fills; fills src.
+int kcache_prepare(pgs_server *srv, KEntry *ke, const pgs_prepared *pr, cudaStream_t s, ResidueSource &src) {
+    pgs_ctx *ctx = srv->ctx;
+    PrimeTable &t = *ctx->table;
+    const size_t nw = t.windows.size();
+    if (srv->wins.size() < nw) srv->wins.resize(nw);
+    if (ke->r.size() < nw) {
+        ke->r.resize(nw);
+        ke->ready.resize(nw, nullptr);
+    }
+    src.a.assign(nw, nullptr);
+    src.b.assign(nw, nullptr);
+    src.full.assign(nw, nullptr);
+    for (int k : pr->tbl_windows) {
+        const TableWindow &w = *t.windows[k];
+        const bool wide = w.lo >= (1ull << 32);
+        const size_t width = wide ? 8 : 4;
+        WinShared &ws = srv->wins[k];
+        bool fill_r2 = false;
+        if (!ws.full.p) {
+            const std::vector<unsigned long long> full{0ull, (unsigned long long)w.count};
+            CK(upload(ws.full, full, s));
+            CK(ws.r2.ensure(w.count * width + 8));
+            CK(cudaEventCreateWithFlags(&ws.ready, cudaEventDisableTiming));
+            fill_r2 = true;
+        }
+        if (!ke->r[k].p) {
+            ke->r[k].pool = &ctx->dpool;
+            CK(ke->r[k].ensure(w.count * width + 8));
+            CK(pg::kmod_window(ke->limbs.as<uint32_t>(), ke->nl, w.lo, w.off.as<uint32_t>(),
+                               ws.full.as<unsigned long long>(), w.count, nullptr, ke->r[k].p,
+                               fill_r2 ? ws.r2.p : nullptr, wide, s));
+            CK(cudaEventCreateWithFlags(&ke->ready[k], cudaEventDisableTiming));
+            CK(cudaEventRecord(ke->ready[k], s));
+            if (fill_r2) CK(cudaEventRecord(ws.ready, s));
+            ke->bytes += ke->r[k].n;
+            srv->kcache_bytes += ke->r[k].n;
+            srv->kfills++;
+        } else {
+            CK(cudaStreamWaitEvent(s, ke->ready[k], 0));
+            srv->khits++;
+        }
+        CK(cudaStreamWaitEvent(s, ws.ready, 0));
+        src.a[k] = ke->r[k].p;
+        src.b[k] = ws.r2.p;
+        src.full[k] = ws.full.as<unsigned long long>();
+    }
+    return PGS_OK;
+}
+
+// Drop least recently used entries no running job holds while over budget.
+void kcache_trim(pgs_server *srv) {
+    while (srv->kcache_bytes > srv->kcache_budget) {
+        auto victim = srv->kcache.end();
+        {
+            std::lock_guard<std::mutex> g(srv->mu);
+            for (auto it = srv->kcache.begin(); it != srv->kcache.end(); ++it)
+                if (it->second->refs == 0 && (victim == srv->kcache.end() || it->second->last < victim->second->last))
+                    victim = it;
+        }
+        if (victim == srv->kcache.end()) return;
+        srv->kcache_bytes -= victim->second->bytes;
+        kentry_free(victim->second);
+        srv->kcache.erase(victim);
+    }
+}
+
 void complete(pgs_server *srv, Request *r, int status) {
     const double t0 = now_s();
     if (status == PGS_OK) status = fetch_job(srv->ctx, r->pr, srv->fetch_stream, &r->res);
@@ -819,6 +959,8 @@ void complete(pgs_server *srv, Request *r, int status) {
     r->status = status;
     srv->in_use -= r->footprint;
     srv->fetching--;
+    if (r->kentry) r->kentry->refs--;
+    r->kentry = nullptr;
     srv->t_last = t;
     if (status == PGS_OK) {
         srv->completed++;
@@ -916,13 +1058,32 @@ void dispatch_loop(pgs_server *srv) {
             rc = table_extend(ctx, h.prime_limit, std::min<uint64_t>(h.s1, h.prime_limit), L->stream);
             if (rc == PGS_OK) rc = lane_buffers(ctx, L);
             if (rc == PGS_OK) rc = prepare_table_job(ctx, r->job, L->stream, &r->pr, r->hj);
-            if (rc == PGS_OK) rc = run_table_job(ctx, r->pr, L);
+            KEntry *ke = nullptr;
+            ResidueSource src;
+            if (rc == PGS_OK) {
+                cudaError_t ce = cudaSuccess;
+                ke = kcache_get(srv, r->pr->hj, L->stream, ce);
+                if (!ke) rc = fail(ctx, ce, "K mod p cache");
+            }
+            if (rc == PGS_OK) {
+                {
+                    std::lock_guard<std::mutex> g(srv->mu);
+                    ke->refs++;
+                    ke->last = ++srv->kclock;
+                    r->kentry = ke;
+                }
+                rc = kcache_prepare(srv, ke, r->pr, L->stream, src);
+            }
+            if (rc == PGS_OK) rc = run_group(ctx, {r->pr}, L, nullptr, nullptr, 0, {}, &src);
             if (rc == PGS_OK && cudaEventRecord(srv->lane_done[lane], L->stream) != cudaSuccess)
                 rc = PGS_ECUDA;
         }
+        kcache_trim(srv);
         std::lock_guard<std::mutex> g(srv->mu);
         srv->prep_s += now_s() - t0;
         if (rc != PGS_OK) {
+            if (r->kentry) r->kentry->refs--;
+            r->kentry = nullptr;
             delete r->pr;
             r->pr = nullptr;
             if (r->derive_rc == PGS_OK) srv->in_use -= r->footprint;
@@ -956,6 +1117,7 @@ int pgs_server_start(pgs_ctx *ctx, uint64_t hbm_budget, int lanes, pgs_server **
     auto *srv = new pgs_server();
     srv->ctx = ctx;
     srv->budget = hbm_budget;
+    srv->kcache_budget = hbm_budget / 4;
     srv->nlanes = lanes;
     srv->lane_req.assign(lanes, nullptr);
     srv->lane_done.assign(lanes, nullptr);
@@ -1025,6 +1187,8 @@ int pgs_server_stats_get(pgs_server *srv, pgs_server_stats *out) {
     out->max_inflight = srv->max_inflight;
     out->host_prep_s = srv->prep_s;
     out->host_fetch_s = srv->fetch_s;
+    out->kmod_fills = srv->kfills;
+    out->kmod_hits = srv->khits;
     if (!srv->latencies.empty()) {
         std::vector<double> v = srv->latencies;
         std::sort(v.begin(), v.end());
@@ -1056,6 +1220,12 @@ int pgs_server_stop(pgs_server *srv) {
     for (auto e : srv->lane_done)
         if (e) cudaEventDestroy(e);
     if (srv->fetch_stream) cudaStreamDestroy(srv->fetch_stream);
+    for (auto &kv : srv->kcache) kentry_free(kv.second);
+    for (auto &ws : srv->wins) {
+        ws.r2.release();
+        ws.full.release();
+        if (ws.ready) cudaEventDestroy(ws.ready);
+    }
     delete srv;
     return PGS_OK;
 }

@@ -87,6 +87,8 @@ class ServerStats(ctypes.Structure):
         ("max_inflight", ctypes.c_uint64),
         ("host_prep_s", ctypes.c_double),
         ("host_fetch_s", ctypes.c_double),
+        ("kmod_fills", ctypes.c_uint64),
+        ("kmod_hits", ctypes.c_uint64),
     ]
 
 

@@ -132,6 +132,32 @@ def test_server_concurrent_submitters(sieve):
     assert got == want
 
 
+def test_server_kmod_cache_reuse(sieve):
+    """Requests with the same (P, d) reuse K mod p; results stay identical,
+    also when the cache budget forces evictions."""
+    rng = random.Random(17)
+    base = workloads.mixed_job(rng)
+    jobs = []
+    for k in range(6):
+        j = workloads.mixed_job(rng, compression=k % 3)
+        j.p, j.d = base.p, base.d
+        j.sieve_length = base.sieve_length
+        j.max_prime = min(j.max_prime, 600_000_000)
+        j.minc = min(j.minc, 4000)
+        jobs.append(j)
+    want = [sieve.method2(j) for j in jobs]
+    for budget in (64 << 30, 1):
+        with sieve.server(hbm_budget=budget, lanes=3) as srv:
+            outs = []
+            for j in jobs:  # one at a time: each later request finds the entry
+                outs.append(srv.wait(srv.submit(j), timeout_ms=120_000)[0])
+            st = srv.stats()
+        assert outs == want
+        assert st["kmod_fills"] >= 1
+        if budget > 1:
+            assert st["kmod_hits"] >= len(jobs) - 1
+
+
 def test_server_rejects_bad_job_without_stalling(sieve):
     good = _small_mix(2, 16)
     bad = pgsieve.JobSpec(503, 210, 1, 100, 100, 10_000_000)  # SL < 6P
