@@ -68,12 +68,11 @@ PG_HD uint64_t neg_inv64(uint64_t p) {
 }
 
 // Montgomery reduction, R = 2^32: t * 2^-32 mod p (result < 2p) for t < p*2^32.
+// For p < 2^31 and t < 2p^2 + 2^32 the sum t + m*p stays below 2^64, so it
+// is one multiply-add whose high word is the result.
 PG_HD uint32_t redc32_lazy(uint64_t t, uint32_t p, uint32_t pinv) {
-    uint32_t m = (uint32_t)t * pinv;
-    uint64_t s = (uint64_t)m * p;
-    // (t + s) is divisible by 2^32; add the high halves and the carry of the low ones.
-    uint64_t hi = (t >> 32) + (s >> 32) + ((uint32_t)t != 0u);
-    return (uint32_t)hi;
+    const uint32_t m = (uint32_t)t * pinv;
+    return (uint32_t)((t + (uint64_t)m * p) >> 32);
 }
 
 PG_HD uint32_t redc32(uint64_t t, uint32_t p, uint32_t pinv) {
@@ -179,16 +178,11 @@ PG_HD uint32_t start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p, uint32_t
 // costs ~log2(n) Montgomery squarings per prime, shared work for long K.
 
 // (W + l) * 2^-32 mod p, result <= p + 1, for W <= p + 1, p < 2^32 - 4.
+// x + m*p <= (p + 2^32) + (2^32 - 1)p = 2^32 (p + 1) < 2^64: one multiply-add.
 PG_HD uint32_t redc32_add(uint32_t W, uint32_t l, uint32_t p, uint32_t pinv) {
     const uint64_t x = (uint64_t)W + l;  // < 2^33
-    const uint32_t xl = (uint32_t)x;
-    const uint32_t m = xl * pinv;
-#if defined(__CUDA_ARCH__)
-    const uint32_t h = __umulhi(m, p);
-#else
-    const uint32_t h = (uint32_t)(((uint64_t)m * p) >> 32);
-#endif
-    return (uint32_t)(x >> 32) + h + (xl != 0u);
+    const uint32_t m = (uint32_t)x * pinv;
+    return (uint32_t)((x + (uint64_t)m * p) >> 32);
 }
 
 // R^(e+1) mod p (R = 2^32): Montgomery power of R (whose Montgomery form is
@@ -641,22 +635,20 @@ PG_HD void rotation_at(uint64_t mi0, uint32_t y0, const ThreeGap<T> &g, uint64_t
     mi = mi0 + (n0 - W) * (uint64_t)g.kp + W * (uint64_t)g.kn;
 }
 
-// Up to `steps` rotation steps from (mi, y), calling emit on the hits, while
-// mi < mi_hi.  up, dn < w < 2^31 so residues fit 32 bits.
+// Up to `steps` rotation steps from (mi, y) while mi < mi_hi, calling
+// emit(mi, y, y < w) at every step (the emitter acts on hits; calling it
+// unconditionally keeps the warp's lanes on one path).  A step wraps when
+// y + up >= C, i.e. y >= dn.  up, dn < w < 2^31 so residues fit 32 bits.
 template <typename T, typename Emit>
 PG_HD void rotation_walk(uint64_t mi, uint32_t y, const ThreeGap<T> &g, uint32_t w, uint64_t mi_hi,
                          uint64_t steps, Emit &emit) {
-    const uint32_t up = (uint32_t)g.up, C = (uint32_t)(g.up + g.dn);
+    const uint32_t up = (uint32_t)g.up, dn = (uint32_t)g.dn;
     const uint64_t kp = g.kp, kn = g.kn;
     for (uint64_t k = 0; k < steps && mi < mi_hi; k++) {
-        if (y < w) emit(mi, y);
-        y += up;
-        if (y >= C) {
-            y -= C;
-            mi += kn;
-        } else {
-            mi += kp;
-        }
+        emit(mi, y, y < w);
+        const bool wrap = y >= dn;
+        y = wrap ? y - dn : y + up;
+        mi += wrap ? kn : kp;
     }
 }
 

@@ -292,7 +292,7 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
         pr->launches++;
         if (pr->sp_bound) {
             CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, 0, t.small.as<uint32_t>(), misc + 1,
-                               pr->sp_bound, nullptr, pr->sr.p, nullptr, false, s));
+                               pr->sp_bound, t.small_limit, nullptr, pr->sr.p, nullptr, false, s));
             pr->launches++;
         }
         if (!h.dq.empty()) {
@@ -344,12 +344,12 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
         }
         // one job: its walk step and start; a group: K' mod p, each job starts its own walk
         if (shared)
-            CK(pg::kmod_window(d_klimbs, nl_shared, w.lo, w.off.as<uint32_t>(), rr, w.count, nullptr,
+            CK(pg::kmod_window(d_klimbs, nl_shared, w.lo, w.off.as<uint32_t>(), rr, w.count, w.hi, nullptr,
                                lane->r.p, lane->t0.p, wide, s));
         else
             CK(pg::kmod_window(lead->klimbs.as<uint32_t>(), (int)lead->hj.klimbs.size(), w.lo,
-                               w.off.as<uint32_t>(), rr, w.count, &lead->hj.walk, lane->r.p, lane->t0.p,
-                               wide, s));
+                               w.off.as<uint32_t>(), rr, w.count, w.hi, &lead->hj.walk, lane->r.p,
+                               lane->t0.p, wide, s));
         lead->launches += 2;
         for (size_t k = 0; k < users.size(); k++) {
             const auto &ui = users[k];
@@ -910,7 +910,7 @@ int kcache_prepare(pgs_server *srv, KEntry *ke, const pgs_prepared *pr, cudaStre
             ke->r[k].pool = &ctx->dpool;
             CK(ke->r[k].ensure(w.count * width + 8));
             CK(pg::kmod_window(ke->limbs.as<uint32_t>(), ke->nl, w.lo, w.off.as<uint32_t>(),
-                               ws.full.as<unsigned long long>(), w.count, nullptr, ke->r[k].p,
+                               ws.full.as<unsigned long long>(), w.count, w.hi, nullptr, ke->r[k].p,
                                fill_r2 ? ws.r2.p : nullptr, wide, s));
             CK(cudaEventCreateWithFlags(&ke->ready[k], cudaEventDisableTiming));
             CK(cudaEventRecord(ke->ready[k], s));

@@ -59,8 +59,9 @@ cudaError_t set_pair(unsigned long long *d_out, uint64_t a, uint64_t b, cudaStre
 // a walk, a = the walk step and b = its start residue (all words of the
 // primes' width).  Primes below 2^32 use 32-bit words, others 64-bit
 // (wide).  K limbs on the device.
+// pmax: no prime of the call exceeds it.
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
-                        const unsigned long long *d_range, uint64_t max_count,
+                        const unsigned long long *d_range, uint64_t max_count, uint64_t pmax,
                         const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream);
 
 // K mod q for an explicit list of 32-bit primes (d-primes, tests).

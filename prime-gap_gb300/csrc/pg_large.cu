@@ -42,14 +42,19 @@ struct Marker {
     const JobDev &job;
     const uint32_t *mmask;  // valid m bits (shared or global)
     const uint32_t *xmask;  // live offset bits (shared or global)
-    __device__ __forceinline__ void operator()(uint64_t j, uint32_t y) const {
-        const uint32_t x = job.walk.xc - 2 * y;
-        if (!((xmask[x >> 5] >> (x & 31)) & 1u)) return;
+    // Called at every walk step (hit or not) with j < jmax, so mi < minc; the
+    // mask words are read unconditionally (x = 0 stands in off a hit) and only
+    // a surviving hit branches to the table reads and the atomic.
+    __device__ __forceinline__ void operator()(uint64_t j, uint32_t y, bool hit) const {
+        const uint32_t x = hit ? job.walk.xc - 2 * y : 0u;
         const uint64_t mi = job.walk.mi_base + job.walk.stride * j;
-        if (!((mmask[mi >> 5] >> (mi & 31)) & 1u)) return;
-        const int32_t row = __ldg(&job.row_of_mi[mi]);
-        const int32_t col = __ldg(&job.col_of_x[x]);
-        atomicOr(&job.comp[(uint64_t)row * job.pitch + ((uint32_t)col >> 5)], 1u << (col & 31));
+        const uint32_t xb = (xmask[x >> 5] >> (x & 31)) & 1u;
+        const uint32_t mb = (mmask[mi >> 5] >> (mi & 31)) & 1u;
+        if (hit & (xb & mb)) {
+            const int32_t row = __ldg(&job.row_of_mi[mi]);
+            const int32_t col = __ldg(&job.col_of_x[x]);
+            atomicOr(&job.comp[(uint64_t)row * job.pitch + ((uint32_t)col >> 5)], 1u << (col & 31));
+        }
     }
 };
 

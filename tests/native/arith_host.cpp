@@ -31,6 +31,9 @@ struct Collect {
         if (n < cap) mi_out[n] = (uint32_t)mi, mod_out[n] = y;
         n++;
     }
+    void operator()(uint64_t mi, uint64_t y, bool hit) {
+        if (hit) (*this)(mi, y);
+    }
 };
 
 // Hits of one prime over [0, max_mi), split into chunks of chunk_len values of
@@ -153,6 +156,9 @@ size_t ah_hits_parity(uint64_t M, uint32_t minc, uint32_t SL, uint64_t p, uint64
         void operator()(uint64_t j, uint64_t y) {
             if (n < cap) mi_out[n] = (uint32_t)(w.mi_base + w.stride * j), x_out[n] = w.xc - 2 * y;
             n++;
+        }
+        void operator()(uint64_t j, uint64_t y, bool hit) {
+            if (hit) (*this)(j, y);
         }
     } c{w, mi_out, x_out, cap, 0};
     unsigned __int128 rh = pg::half_mod(r, p);
