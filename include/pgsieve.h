@@ -164,8 +164,10 @@ int pgs_method2_batch(pgs_ctx *ctx, const pgs_job *jobs, int n, pgs_result *outs
  * text and tables) fits under hbm_budget bytes; admitted jobs run
  * concurrently and their results are copied back as each one finishes (a
  * lane takes its next job as soon as its kernels are done; the copy-back
- * runs on a separate thread and stream).  K mod p is cached per (P, d) and
- * prime window, within a quarter of hbm_budget, for requests that follow.
+ * runs on two separate threads and streams; the next request is derived and
+ * its tables uploaded while every lane is still busy).  K mod p is cached per
+ * (P, d) and prime window, within a quarter of hbm_budget, for requests that
+ * follow.
  * While a server runs it owns the context: make no other calls on it.
  */
 typedef struct pgs_server pgs_server;
@@ -179,6 +181,11 @@ typedef struct {
     double host_fetch_s; /* host time copying results back */
     uint64_t kmod_fills; /* (P, d, prime window) K mod p passes computed */
     uint64_t kmod_hits;  /* ... and reused from the cache */
+    double host_derive_s, host_upload_s, host_launch_s; /* parts of host_prep_s */
+    double pinned_alloc_s; /* part of host_fetch_s spent allocating pinned memory */
+    uint64_t pinned_allocs;
+    double device_alloc_s; /* host time in cudaMalloc (device buffer pool misses) */
+    uint64_t device_allocs;
 } pgs_server_stats;
 int pgs_server_start(pgs_ctx *ctx, uint64_t hbm_budget, int lanes, pgs_server **out);
 int pgs_server_submit(pgs_server *srv, const pgs_job *job, uint64_t *ticket);

@@ -145,14 +145,7 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     pr->events.push_back(e1);
     CK(cudaEventRecord(e0, s));
     // tables
-    CK(upload(pr->klimbs, h.klimbs, s));
-    CK(upload(pr->row_of_mi, h.row_of_mi, s));
-    CK(upload(pr->col_of_x, h.col_of_x, s));
-    CK(upload(pr->valid_mi, h.valid_mi, s));
-    CK(upload(pr->dist, h.dist, s));
-    CK(upload(pr->dq, h.dq, s));
-    CK(upload(pr->mmask, h.mmask, s));
-    CK(upload(pr->xmask, h.xmask, s));
+    CK(upload_tables(pr, s));
     CK(pr->dr.ensure(std::max<size_t>(1, h.dq.size()) * 4));
     CK(cudaEventRecord(e1, s));
     // work buffers

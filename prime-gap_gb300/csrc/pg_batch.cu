@@ -206,17 +206,7 @@ int prepare_table_job(pgs_ctx *ctx, const pgs_job &job, cudaStream_t s, pgs_prep
             pr->tbl_windows.push_back((int)k);
 
     cudaError_t e = cudaSuccess;
-    auto up = [&](DevBuf &b, auto &v) {
-        if (e == cudaSuccess) e = upload(b, v, s);
-    };
-    up(pr->klimbs, h.klimbs);
-    up(pr->row_of_mi, h.row_of_mi);
-    up(pr->col_of_x, h.col_of_x);
-    up(pr->valid_mi, h.valid_mi);
-    up(pr->dist, h.dist);
-    up(pr->dq, h.dq);
-    up(pr->mmask, h.mmask);
-    up(pr->xmask, h.xmask);
+    e = upload_tables(pr, s);
     auto need = [&](DevBuf &b, size_t n) {
         if (e == cudaSuccess) e = b.ensure(n);
     };
@@ -840,7 +830,13 @@ struct pgs_server {
     std::map<uint64_t, Request *> reqs;
     std::vector<Request *> lane_req;   // job whose kernels run on the lane
     std::vector<cudaEvent_t> lane_done;
-    cudaStream_t fetch_stream = nullptr;
+    cudaStream_t fetch_stream = nullptr, fetch_stream2 = nullptr;  // one per copy-back thread
+    std::deque<std::pair<Request *, int>> fetch_queue;                // finished, not yet copied
+    std::condition_variable cv_fetch;
+    bool poll_done = false;
+    std::thread fetcher, fetcher2;
+    cudaStream_t up_stream = nullptr;    // table uploads of the staged request
+    cudaEvent_t staged_ready = nullptr;  // recorded after them
     uint64_t next_ticket = 1, in_use = 0, running = 0, fetching = 0;
     bool stopping = false, dispatcher_done = false;
     std::thread dispatcher, completer;
@@ -849,6 +845,8 @@ struct pgs_server {
     std::vector<double> latencies;
     uint64_t submitted = 0, completed = 0, failed = 0, peak_bytes = 0, max_inflight = 0;
     double t_first = -1, t_last = 0, prep_s = 0, fetch_s = 0;
+    double derive_s = 0, upload_s = 0, launch_s = 0, pinned_s0 = 0, dev_s0 = 0;
+    uint64_t pinned_n0 = 0, dev_n0 = 0;
 };
 
 namespace {
@@ -947,9 +945,9 @@ void kcache_trim(pgs_server *srv) {
     }
 }
 
-void complete(pgs_server *srv, Request *r, int status) {
+void complete(pgs_server *srv, Request *r, int status, cudaStream_t fs) {
     const double t0 = now_s();
-    if (status == PGS_OK) status = fetch_job(srv->ctx, r->pr, srv->fetch_stream, &r->res);
+    if (status == PGS_OK) status = fetch_job(srv->ctx, r->pr, fs, &r->res);
     delete r->pr;
     r->pr = nullptr;
     const double t = now_s();
@@ -989,113 +987,180 @@ void complete_loop(pgs_server *srv) {
                 srv->lane_req[l] = nullptr;  // the lane takes new work now
                 srv->running--;
                 srv->fetching++;
+                srv->fetch_queue.push_back({r, q == cudaSuccess ? PGS_OK : PGS_ECUDA});
             }
-            complete(srv, r, q == cudaSuccess ? PGS_OK : PGS_ECUDA);
+            srv->cv_fetch.notify_one();
             idle = false;
         }
         {
             std::lock_guard<std::mutex> g(srv->mu);
-            if (srv->dispatcher_done && srv->running == 0) return;
+            if (srv->dispatcher_done && srv->running == 0) {
+                srv->poll_done = true;
+                srv->cv_fetch.notify_all();
+                return;
+            }
         }
         if (idle) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
+// Copy-back threads: finished jobs' texts to the host, each on its own
+// stream, so a slow copy (or a pinned allocation) never holds up the lane
+// polling above.
+void fetch_loop(pgs_server *srv, cudaStream_t fs) {
+    cudaSetDevice(srv->ctx->device);
+    for (;;) {
+        std::pair<Request *, int> job;
+        {
+            std::unique_lock<std::mutex> lk(srv->mu);
+            srv->cv_fetch.wait(lk, [&] { return !srv->fetch_queue.empty() || srv->poll_done; });
+            if (srv->fetch_queue.empty()) return;
+            job = srv->fetch_queue.front();
+            srv->fetch_queue.pop_front();
+        }
+        complete(srv, job.first, job.second, fs);
+    }
+}
+
+// A request that failed before or at launch leaves with its status.
+void reject(pgs_server *srv, Request *r, int rc) {
+    std::lock_guard<std::mutex> g(srv->mu);
+    if (r->kentry) r->kentry->refs--;
+    r->kentry = nullptr;
+    delete r->pr;
+    r->pr = nullptr;
+    r->status = rc;
+    srv->failed++;
+    srv->cv_done.notify_all();
+}
+
+// Launch a staged request (tables uploaded on the upload stream) on a free lane.
+int launch_staged(pgs_server *srv, Request *r, int lane) {
+    pgs_ctx *ctx = srv->ctx;
+    Lane *L = ctx->lanes[lane];
+    int rc = lane_buffers(ctx, L);
+    if (rc) return rc;
+    cudaError_t ce = cudaSuccess;
+    KEntry *ke = kcache_get(srv, r->pr->hj, L->stream, ce);
+    if (!ke) return fail(ctx, ce, "K mod p cache");
+    {
+        std::lock_guard<std::mutex> g(srv->mu);
+        ke->refs++;
+        ke->last = ++srv->kclock;
+        r->kentry = ke;
+    }
+    ResidueSource src;
+    rc = kcache_prepare(srv, ke, r->pr, L->stream, src);
+    if (rc) return rc;
+    CK(cudaStreamWaitEvent(L->stream, srv->staged_ready, 0));
+    rc = run_group(ctx, {r->pr}, L, nullptr, nullptr, 0, {}, &src);
+    if (rc) return rc;
+    CK(cudaEventRecord(srv->lane_done[lane], L->stream));
+    return PGS_OK;
+}
+
+// Arrival order.  The head request is staged -- derived, admitted against
+// the budget, its tables uploaded on the upload stream -- while the lanes are
+// busy, and launched on the first lane that frees up.
 void dispatch_loop(pgs_server *srv) {
     pgs_ctx *ctx = srv->ctx;
     cudaSetDevice(ctx->device);
+    Request *staged = nullptr;
     for (;;) {
-        Request *r = nullptr;
-        int lane = -1;
-        {
-            std::lock_guard<std::mutex> g(srv->mu);
-            if (srv->pending.empty()) {
-                if (srv->stopping) {
+        bool progress = false;
+        if (staged) {
+            int lane = -1;
+            {
+                std::lock_guard<std::mutex> g(srv->mu);
+                for (int l = 0; l < srv->nlanes && lane < 0; l++)
+                    if (!srv->lane_req[l]) lane = l;
+            }
+            if (lane >= 0) {
+                const double t0 = now_s();
+                Request *r = staged;
+                staged = nullptr;
+                const int rc = launch_staged(srv, r, lane);
+                kcache_trim(srv);
+                if (rc != PGS_OK) {
+                    {
+                        std::lock_guard<std::mutex> g(srv->mu);
+                        srv->in_use -= r->footprint;
+                    }
+                    reject(srv, r, rc);
+                } else {
+                    std::lock_guard<std::mutex> g(srv->mu);
+                    srv->prep_s += now_s() - t0;
+                    srv->launch_s += now_s() - t0;
+                    srv->lane_req[lane] = r;
+                    srv->running++;
+                    srv->max_inflight = std::max(srv->max_inflight, srv->running + srv->fetching);
+                    if (srv->t_first < 0) srv->t_first = now_s();
+                }
+                progress = true;
+            }
+        }
+        if (!staged) {
+            Request *r = nullptr;
+            {
+                std::lock_guard<std::mutex> g(srv->mu);
+                if (!srv->pending.empty()) {
+                    r = srv->pending.front();
+                } else if (srv->stopping) {
                     srv->dispatcher_done = true;
                     return;
                 }
-            } else {
-                r = srv->pending.front();
-                for (int l = 0; l < srv->nlanes; l++)
-                    if (!srv->lane_req[l]) {
-                        lane = l;
-                        break;
-                    }
             }
-        }
-        if (!r) {
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
-            continue;
-        }
-        const double t0 = now_s();
-        if (r->derive_rc == 1) {  // derive the head while lanes are busy
-            r->hj = new HostJob();
-            r->derive_rc = derive(r->job, *r->hj, srv->err, true);
-            r->footprint = r->derive_rc == PGS_OK ? job_footprint(*r->hj) : 0;
-        }
-        int rc = r->derive_rc;
-        bool admit = rc != PGS_OK;  // failures leave the queue at once
-        if (rc == PGS_OK && lane >= 0) {
-            std::lock_guard<std::mutex> g(srv->mu);
-            // the head waits while it does not fit (unless nothing holds memory)
-            admit = srv->in_use == 0 || srv->in_use + r->footprint <= srv->budget;
-        }
-        if (!admit) {
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
-            continue;
-        }
-        {
-            std::lock_guard<std::mutex> g(srv->mu);
-            srv->pending.pop_front();
-            if (rc == PGS_OK) {
-                srv->in_use += r->footprint;
-                srv->peak_bytes = std::max(srv->peak_bytes, srv->in_use);
-            }
-        }
-        if (rc == PGS_OK) {
-            HostJob &h = *r->hj;
-            Lane *L = ctx->lanes[lane];
-            rc = table_extend(ctx, h.prime_limit, std::min<uint64_t>(h.s1, h.prime_limit), L->stream);
-            if (rc == PGS_OK) rc = lane_buffers(ctx, L);
-            if (rc == PGS_OK) rc = prepare_table_job(ctx, r->job, L->stream, &r->pr, r->hj);
-            KEntry *ke = nullptr;
-            ResidueSource src;
-            if (rc == PGS_OK) {
-                cudaError_t ce = cudaSuccess;
-                ke = kcache_get(srv, r->pr->hj, L->stream, ce);
-                if (!ke) rc = fail(ctx, ce, "K mod p cache");
-            }
-            if (rc == PGS_OK) {
-                {
+            if (r) {
+                const double t0 = now_s();
+                if (r->derive_rc == 1) {
+                    r->hj = new HostJob();
+                    r->derive_rc = derive(r->job, *r->hj, srv->err, true);
+                    r->footprint = r->derive_rc == PGS_OK ? job_footprint(*r->hj) : 0;
                     std::lock_guard<std::mutex> g(srv->mu);
-                    ke->refs++;
-                    ke->last = ++srv->kclock;
-                    r->kentry = ke;
+                    srv->derive_s += now_s() - t0;
                 }
-                rc = kcache_prepare(srv, ke, r->pr, L->stream, src);
+                const double t1 = now_s();
+                int rc = r->derive_rc;
+                bool admit = true;
+                if (rc == PGS_OK) {
+                    std::lock_guard<std::mutex> g(srv->mu);
+                    // the head waits while it does not fit (unless nothing holds memory)
+                    admit = srv->in_use == 0 || srv->in_use + r->footprint <= srv->budget;
+                    if (admit) {
+                        srv->in_use += r->footprint;
+                        srv->peak_bytes = std::max(srv->peak_bytes, srv->in_use);
+                    }
+                }
+                if (admit) {
+                    {
+                        std::lock_guard<std::mutex> g(srv->mu);
+                        srv->pending.pop_front();
+                    }
+                    if (rc == PGS_OK) {
+                        HostJob &h = *r->hj;
+                        rc = table_extend(ctx, h.prime_limit, std::min<uint64_t>(h.s1, h.prime_limit),
+                                          srv->up_stream);
+                        if (rc == PGS_OK) rc = prepare_table_job(ctx, r->job, srv->up_stream, &r->pr, r->hj);
+                        if (rc == PGS_OK && cudaEventRecord(srv->staged_ready, srv->up_stream) != cudaSuccess)
+                            rc = PGS_ECUDA;
+                    }
+                    if (rc == PGS_OK) {
+                        staged = r;
+                        std::lock_guard<std::mutex> g(srv->mu);
+                        srv->prep_s += now_s() - t0;
+                        srv->upload_s += now_s() - t1;
+                    } else {
+                        if (r->derive_rc == PGS_OK) {
+                            std::lock_guard<std::mutex> g(srv->mu);
+                            srv->in_use -= r->footprint;
+                        }
+                        reject(srv, r, rc);
+                    }
+                    progress = true;
+                }
             }
-            if (rc == PGS_OK) rc = run_group(ctx, {r->pr}, L, nullptr, nullptr, 0, {}, &src);
-            if (rc == PGS_OK && cudaEventRecord(srv->lane_done[lane], L->stream) != cudaSuccess)
-                rc = PGS_ECUDA;
         }
-        kcache_trim(srv);
-        std::lock_guard<std::mutex> g(srv->mu);
-        srv->prep_s += now_s() - t0;
-        if (rc != PGS_OK) {
-            if (r->kentry) r->kentry->refs--;
-            r->kentry = nullptr;
-            delete r->pr;
-            r->pr = nullptr;
-            if (r->derive_rc == PGS_OK) srv->in_use -= r->footprint;
-            r->status = rc;
-            srv->failed++;
-            srv->cv_done.notify_all();
-            continue;
-        }
-        srv->lane_req[lane] = r;
-        srv->running++;
-        srv->max_inflight = std::max(srv->max_inflight, srv->running + srv->fetching);
-        if (srv->t_first < 0) srv->t_first = now_s();
+        if (!progress) std::this_thread::sleep_for(std::chrono::microseconds(20));
     }
 }
 
@@ -1118,21 +1183,41 @@ int pgs_server_start(pgs_ctx *ctx, uint64_t hbm_budget, int lanes, pgs_server **
     srv->ctx = ctx;
     srv->budget = hbm_budget;
     srv->kcache_budget = hbm_budget / 4;
+    {
+        PinnedPool &pp = pinned_pool();
+        std::lock_guard<std::mutex> pg(pp.mu);
+        srv->pinned_s0 = pp.alloc_s;
+        srv->pinned_n0 = pp.allocs;
+    }
+    {
+        DevicePool &dp = ctx->dpool;
+        std::lock_guard<std::mutex> dg(dp.mu);
+        srv->dev_s0 = dp.alloc_s;
+        srv->dev_n0 = dp.allocs;
+    }
     srv->nlanes = lanes;
     srv->lane_req.assign(lanes, nullptr);
     srv->lane_done.assign(lanes, nullptr);
     cudaError_t e = cudaStreamCreateWithFlags(&srv->fetch_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&srv->fetch_stream2, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&srv->up_stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&srv->staged_ready, cudaEventDisableTiming);
     for (int l = 0; l < lanes && e == cudaSuccess; l++)
         e = cudaEventCreateWithFlags(&srv->lane_done[l], cudaEventDisableTiming);
     if (e != cudaSuccess) {
         for (auto ev : srv->lane_done)
             if (ev) cudaEventDestroy(ev);
         if (srv->fetch_stream) cudaStreamDestroy(srv->fetch_stream);
+        if (srv->fetch_stream2) cudaStreamDestroy(srv->fetch_stream2);
+        if (srv->up_stream) cudaStreamDestroy(srv->up_stream);
+        if (srv->staged_ready) cudaEventDestroy(srv->staged_ready);
         delete srv;
         return fail(ctx, e, "server start");
     }
     srv->dispatcher = std::thread(dispatch_loop, srv);
     srv->completer = std::thread(complete_loop, srv);
+    srv->fetcher = std::thread(fetch_loop, srv, srv->fetch_stream);
+    srv->fetcher2 = std::thread(fetch_loop, srv, srv->fetch_stream2);
     *out = srv;
     return PGS_OK;
 }
@@ -1189,6 +1274,21 @@ int pgs_server_stats_get(pgs_server *srv, pgs_server_stats *out) {
     out->host_fetch_s = srv->fetch_s;
     out->kmod_fills = srv->kfills;
     out->kmod_hits = srv->khits;
+    out->host_derive_s = srv->derive_s;
+    out->host_upload_s = srv->upload_s;
+    out->host_launch_s = srv->launch_s;
+    {
+        PinnedPool &pp = pinned_pool();
+        std::lock_guard<std::mutex> pg(pp.mu);
+        out->pinned_alloc_s = pp.alloc_s - srv->pinned_s0;
+        out->pinned_allocs = pp.allocs - srv->pinned_n0;
+    }
+    {
+        DevicePool &dp = srv->ctx->dpool;
+        std::lock_guard<std::mutex> dg(dp.mu);
+        out->device_alloc_s = dp.alloc_s - srv->dev_s0;
+        out->device_allocs = dp.allocs - srv->dev_n0;
+    }
     if (!srv->latencies.empty()) {
         std::vector<double> v = srv->latencies;
         std::sort(v.begin(), v.end());
@@ -1212,6 +1312,8 @@ int pgs_server_stop(pgs_server *srv) {
     }
     if (srv->dispatcher.joinable()) srv->dispatcher.join();
     if (srv->completer.joinable()) srv->completer.join();
+    if (srv->fetcher.joinable()) srv->fetcher.join();
+    if (srv->fetcher2.joinable()) srv->fetcher2.join();
     for (auto &kv : srv->reqs) {
         pgs_result_free(&kv.second->res);
         delete kv.second->pr;
@@ -1220,6 +1322,9 @@ int pgs_server_stop(pgs_server *srv) {
     for (auto e : srv->lane_done)
         if (e) cudaEventDestroy(e);
     if (srv->fetch_stream) cudaStreamDestroy(srv->fetch_stream);
+    if (srv->fetch_stream2) cudaStreamDestroy(srv->fetch_stream2);
+    if (srv->up_stream) cudaStreamDestroy(srv->up_stream);
+    if (srv->staged_ready) cudaEventDestroy(srv->staged_ready);
     for (auto &kv : srv->kcache) kentry_free(kv.second);
     for (auto &ws : srv->wins) {
         ws.r2.release();

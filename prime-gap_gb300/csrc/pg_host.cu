@@ -283,6 +283,41 @@ uint32_t rows_per_block(uint32_t nb, int compression) {
     return r;
 }
 
+cudaError_t upload_tables(pgs_prepared *pr, cudaStream_t s) {
+    const HostJob &h = pr->hj;
+    struct Item {
+        DevBuf *b;
+        const void *src;
+        size_t n;
+    } items[] = {{&pr->klimbs, h.klimbs.data(), h.klimbs.size() * 4},
+                 {&pr->row_of_mi, h.row_of_mi.data(), h.row_of_mi.size() * 4},
+                 {&pr->col_of_x, h.col_of_x.data(), h.col_of_x.size() * 4},
+                 {&pr->valid_mi, h.valid_mi.data(), h.valid_mi.size() * 4},
+                 {&pr->dist, h.dist.data(), h.dist.size() * 4},
+                 {&pr->dq, h.dq.data(), h.dq.size() * 4},
+                 {&pr->mmask, h.mmask.data(), h.mmask.size() * 4},
+                 {&pr->xmask, h.xmask.data(), h.xmask.size() * 4}};
+    size_t total = 0;
+    for (const Item &it : items) total += (it.n + 255) / 256 * 256;
+    if (!pr->stage || pr->stage_cap < total) {
+        if (pr->stage) pinned_pool().put(pr->stage, pr->stage_cap);
+        pr->stage = pinned_pool().get(total + 256, &pr->stage_cap);
+        if (!pr->stage) return cudaErrorMemoryAllocation;
+    }
+    size_t off = 0;
+    for (const Item &it : items) {
+        cudaError_t e = it.b->ensure(it.n);
+        if (e) return e;
+        if (it.n) {
+            memcpy(pr->stage + off, it.src, it.n);
+            e = cudaMemcpyAsync(it.b->p, pr->stage + off, it.n, cudaMemcpyHostToDevice, s);
+            if (e) return e;
+        }
+        off += (it.n + 255) / 256 * 256;
+    }
+    return cudaSuccess;
+}
+
 size_t job_ranges(const pgs_prepared *pr) {
     return 1 + (pr->table_mode ? pr->tbl_windows.size() : pr->windows.size());
 }

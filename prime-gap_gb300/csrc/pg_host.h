@@ -4,6 +4,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <chrono>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -46,10 +47,23 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables);
 // Device allocations recycled across jobs on one context: a job's buffers
 // (several GB for the larger configs) are returned here instead of freed, so
 // repeated jobs pay no cudaMalloc/cudaFree.
+// Allocation size classes: n rounded up to one of 8 steps per power of two
+// (at most 12.5 % over), so buffers freed by one job fit the next job's
+// slightly different sizes and pools stop growing after a few jobs.
+inline size_t size_class(size_t n) {
+    if (n <= 4096) return 4096;
+    const int b = 63 - __builtin_clzll((unsigned long long)(n - 1));  // n - 1 < 2^(b+1)
+    const size_t step = (size_t)1 << (b - 2 > 12 ? b - 2 : 12);
+    return (n + step - 1) / step * step;
+}
+
 struct DevicePool {
     std::mutex mu;
     std::vector<std::pair<void *, size_t>> free_list;
+    double alloc_s = 0;  // time spent in cudaMalloc
+    uint64_t allocs = 0;
     cudaError_t get(size_t n, void **p, size_t *cap) {
+        n = size_class(n);
         {
             std::lock_guard<std::mutex> g(mu);
             size_t best = (size_t)-1;
@@ -65,12 +79,18 @@ struct DevicePool {
                 return cudaSuccess;
             }
         }
+        const auto t0 = std::chrono::steady_clock::now();
         cudaError_t e = cudaMalloc(p, n);
         if (e == cudaErrorMemoryAllocation) {
             trim();  // give cached blocks back and retry once
             e = cudaMalloc(p, n);
         }
-        if (e == cudaSuccess) *cap = n;
+        if (e == cudaSuccess) {
+            *cap = n;
+            std::lock_guard<std::mutex> g(mu);
+            alloc_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+            allocs++;
+        }
         return e;
     }
     void put(void *p, size_t cap) {
@@ -114,21 +134,30 @@ struct DevBuf {
 struct PinnedPool {
     std::mutex mu;
     std::vector<std::pair<char *, size_t>> free_list;
+    double alloc_s = 0;  // time spent in cudaMallocHost
+    uint64_t allocs = 0;
     char *get(size_t n, size_t *cap) {
-        std::lock_guard<std::mutex> g(mu);
-        size_t best = (size_t)-1;
-        for (size_t i = 0; i < free_list.size(); i++)
-            if (free_list[i].second >= n && (best == (size_t)-1 || free_list[i].second < free_list[best].second))
-                best = i;
-        if (best != (size_t)-1) {
-            auto e = free_list[best];
-            free_list.erase(free_list.begin() + best);
-            *cap = e.second;
-            return e.first;
+        {
+            std::lock_guard<std::mutex> g(mu);
+            size_t best = (size_t)-1;
+            for (size_t i = 0; i < free_list.size(); i++)
+                if (free_list[i].second >= n &&
+                    (best == (size_t)-1 || free_list[i].second < free_list[best].second))
+                    best = i;
+            if (best != (size_t)-1) {
+                auto e = free_list[best];
+                free_list.erase(free_list.begin() + best);
+                *cap = e.second;
+                return e.first;
+            }
         }
         char *p = nullptr;
-        size_t want = n < 4096 ? 4096 : n;
+        const size_t want = size_class(n);
+        const auto t0 = std::chrono::steady_clock::now();
         if (cudaMallocHost(&p, want) != cudaSuccess) return nullptr;
+        std::lock_guard<std::mutex> g(mu);
+        alloc_s += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        allocs++;
         *cap = want;
         return p;
     }
@@ -193,9 +222,12 @@ struct pgs_prepared {
                 &comp,   &sp,        &sr,       &sp_t0,    &lists,  &counts, &row_bytes,
                 &offsets, &scan_tmp, &misc,     &text,     &mmask,  &xmask};
     }
+    char *stage = nullptr;  // pinned staging block of the table uploads
+    size_t stage_cap = 0;
     ~pgs_prepared() {
         for (auto e : events) cudaEventDestroy(e);
         for (pgh::DevBuf *b : all()) b->release();
+        if (stage) pgh::pinned_pool().put(stage, stage_cap);
     }
 };
 
@@ -219,6 +251,11 @@ cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t s) {
 pg::JobDev job_dev(pgs_prepared *pr);
 pg::RowsDev rows_dev(pgs_prepared *pr);
 uint32_t rows_per_block(uint32_t nb, int compression);
+
+// The job's host tables (K limbs, row/column maps, valid m, distances, primes
+// of d, masks) to their device buffers, through one pinned staging block:
+// a copy from pageable memory is staged by the driver and waits for it.
+cudaError_t upload_tables(pgs_prepared *pr, cudaStream_t s);
 
 // Copy a finished job's text to pinned host memory (no context lock).
 int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out);

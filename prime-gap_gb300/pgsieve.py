@@ -89,6 +89,13 @@ class ServerStats(ctypes.Structure):
         ("host_fetch_s", ctypes.c_double),
         ("kmod_fills", ctypes.c_uint64),
         ("kmod_hits", ctypes.c_uint64),
+        ("host_derive_s", ctypes.c_double),
+        ("host_upload_s", ctypes.c_double),
+        ("host_launch_s", ctypes.c_double),
+        ("pinned_alloc_s", ctypes.c_double),
+        ("pinned_allocs", ctypes.c_uint64),
+        ("device_alloc_s", ctypes.c_double),
+        ("device_allocs", ctypes.c_uint64),
     ]
 
 
