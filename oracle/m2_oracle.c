@@ -963,6 +963,278 @@ int pgo_trial_division(const pgo_job *job, const uint64_t *m, const int64_t *x, 
 }
 
 /* ------------------------------------------------------------------------ */
+/* unknowns as binary lists                                                   */
+
+void pgo_lists_free(pgo_lists *l) {
+    if (!l) return;
+    free(l->m);
+    free(l->n_prev);
+    free(l->n_next);
+    free(l->start);
+    free(l->dist);
+    memset(l, 0, sizeof(*l));
+}
+
+static int lists_alloc(pgo_lists *l, uint64_t rows, uint64_t cap) {
+    memset(l, 0, sizeof(*l));
+    l->rows = rows;
+    l->m = malloc((rows + 1) * sizeof(uint64_t));
+    l->n_prev = malloc((rows + 1) * sizeof(uint32_t));
+    l->n_next = malloc((rows + 1) * sizeof(uint32_t));
+    l->start = malloc((rows + 1) * sizeof(uint64_t));
+    l->dist = malloc((cap + 1) * sizeof(uint32_t));
+    if (!l->m || !l->n_prev || !l->n_next || !l->start || !l->dist) {
+        pgo_lists_free(l);
+        return PGO_ENOMEM;
+    }
+    return PGO_OK;
+}
+
+/* straight from the composite bits: a side's unknowns are the coprime
+ * offsets heading outward from SL that are not marked (save_unknowns_method2,
+ * combined_sieve.cpp:1387-1431, without the text) */
+int pgo_method2_lists(const pgo_job *job, pgo_lists *out) {
+    m2_state s;
+    int rc = state_init(&s, job);
+    if (rc) {
+        state_free(&s);
+        return rc;
+    }
+    if (s.job.threads < 1) s.job.threads = 1;
+    phase_small(&s);
+    for_primes(&s, s.small_threshold + 1, s.medium_threshold, medium_prime);
+    for_primes(&s, s.medium_threshold + 1, s.last_prime, large_prime);
+    const uint32_t SL = s.sl;
+    uint32_t *dists = malloc((s.coprime_count / 2 + 1) * sizeof(uint32_t));
+    size_t nside = 0;
+    for (uint64_t xi = 0; xi < s.coprime_count; xi++)
+        if (s.coprime_x[xi] > SL) dists[nside++] = s.coprime_x[xi] - SL;
+    rc = lists_alloc(out, s.valid_ms, s.valid_ms * 2 * (uint64_t)nside);
+    if (rc == PGO_OK) {
+        uint64_t pos = 0;
+        for (uint64_t mii = 0; mii < s.valid_ms; mii++) {
+            out->m[mii] = s.job.mstart + s.valid_mi[mii];
+            out->start[mii] = pos;
+            for (int side = 0; side <= 1; side++) {
+                uint32_t n = 0;
+                for (size_t i = 0; i < nside; i++) {
+                    const uint32_t x = side ? SL + dists[i] : SL - dists[i];
+                    if (!is_marked(&s, mii, s.x_reindex[x])) {
+                        out->dist[pos++] = dists[i];
+                        n++;
+                    }
+                }
+                if (side) out->n_next[mii] = n;
+                else out->n_prev[mii] = n;
+            }
+        }
+        out->total = pos;
+    }
+    free(dists);
+    state_free(&s);
+    return rc;
+}
+
+/* a cursor over one line */
+typedef struct {
+    const char *p, *end;
+} cursor;
+
+static void skip_ws(cursor *c) {
+    while (c->p < c->end && (*c->p == ' ' || *c->p == '\t')) c->p++;
+}
+/* istream >> int64 */
+static int read_i64(cursor *c, int64_t *v) {
+    skip_ws(c);
+    int neg = 0;
+    if (c->p < c->end && (*c->p == '-' || *c->p == '+')) neg = *c->p++ == '-';
+    if (c->p >= c->end || *c->p < '0' || *c->p > '9') return 0;
+    int64_t x = 0;
+    while (c->p < c->end && *c->p >= '0' && *c->p <= '9') x = x * 10 + (*c->p++ - '0');
+    *v = neg ? -x : x;
+    return 1;
+}
+/* istream >> std::string, compared with `tok` */
+static int read_token(cursor *c, const char *tok) {
+    skip_ws(c);
+    const size_t n = strlen(tok);
+    if ((size_t)(c->end - c->p) < n || memcmp(c->p, tok, n)) return 0;
+    c->p += n;
+    return c->p == c->end || *c->p == ' ' || *c->p == '\n';
+}
+
+/* parse_unknown_line (gap_common.cpp:1186-1360) for every line; the
+ * BitArrayHelper tables (gap_common.cpp:1114-1180) come from the job */
+int pgo_parse_unknowns(const pgo_job *job, const char *text, size_t len, pgo_lists *out) {
+    m2_state s;
+    int rc = state_init(&s, job);
+    if (rc) {
+        state_free(&s);
+        return rc;
+    }
+    const uint32_t SL = s.sl, interval = s.interval;
+    const int d_even = job->d % 2 == 0;
+    /* coprime_X or coprime_X_even, and their flags */
+    uint32_t *cx = malloc((s.coprime_count + 1) * sizeof(uint32_t));
+    uint8_t *base_flags = calloc(interval, 1);
+    size_t ncx = 0;
+    for (uint64_t xi = 0; xi < s.coprime_count; xi++) {
+        const uint32_t x = s.coprime_x[xi];
+        if (d_even && ((x + SL) & 1)) continue; /* X = x - SL must be even */
+        cx[ncx++] = x;
+        base_flags[x] = 1;
+    }
+    uint32_t d_primes[16];
+    int nd = 0;
+    for (uint32_t q = 3; q <= job->p && nd < 16; q++)
+        if (is_prime_small(q) && job->d % q == 0) d_primes[nd++] = q;
+    const uint64_t neg_k_mod_d = (job->d - pgo_k_mod(s.K, s.K_n, job->d)) % job->d; /* mpz_cdiv_ui */
+    uint8_t *flags = malloc(interval);
+    /* a line has at most one unknown per listed offset */
+    rc = lists_alloc(out, s.valid_ms, s.valid_ms * (uint64_t)(ncx + 1));
+    const char *p = text, *end = text + len;
+    uint64_t pos = 0;
+    for (uint64_t mii = 0; rc == PGO_OK && mii < s.valid_ms; mii++) {
+        const char *nl = memchr(p, '\n', (size_t)(end - p));
+        if (!nl) {
+            rc = PGO_EINVAL;
+            break;
+        }
+        cursor c = {p, nl};
+        p = nl + 1;
+        int64_t m_test = -1;
+        if (!read_i64(&c, &m_test) || m_test < 0 || !read_token(&c, ":")) {
+            rc = PGO_EINVAL;
+            break;
+        }
+        out->m[mii] = (uint64_t)m_test;
+        out->start[mii] = pos;
+        if (job->compression == 2) {
+            memcpy(flags, base_flags, interval);
+            const int center_odd = d_even && ((uint64_t)m_test & 1);
+            const int low_is_even = center_odd == (int)(SL & 1);
+            int64_t num = (int64_t)ncx;
+            for (int t = 0; t < nd; t++) {
+                const uint64_t q = d_primes[t];
+                uint64_t first = ((uint64_t)m_test * neg_k_mod_d + SL) % q;
+                const int even_from_low = (first & 1) == 0;
+                if (low_is_even == even_from_low) first += q;
+                for (uint64_t mult = first; mult < interval; mult += 2 * q)
+                    if (flags[mult]) flags[mult] = 0, num--;
+            }
+            int64_t total = -1, bytes_check = -1;
+            if (!read_i64(&c, &total) || total <= 0 || !read_i64(&c, &bytes_check) ||
+                bytes_check != (num + 6) / 7 || !read_token(&c, "||") || c.p >= c.end || *c.p != ' ') {
+                rc = PGO_EINVAL;
+                break;
+            }
+            c.p++;
+            if (c.end - c.p != bytes_check) {
+                rc = PGO_EINVAL;
+                break;
+            }
+            /* the low side comes farthest first in increasing x: collect, reverse */
+            uint32_t np = 0, nn = 0;
+            int bits = 0;
+            size_t index = 0;
+            unsigned char b = (unsigned char)c.p[0];
+            for (size_t i = 0; i < ncx; i++) {
+                const uint32_t x = cx[i];
+                if (!flags[x]) continue;
+                if (bits == 7) {
+                    b = (unsigned char)c.p[++index];
+                    bits = 0;
+                }
+                if ((b & 1) == 0) {
+                    if (x <= SL) out->dist[pos + np++] = SL - x;
+                    else nn++;
+                }
+                b >>= 1;
+                bits++;
+            }
+            for (uint32_t i = 0; i < np / 2; i++) {
+                uint32_t t = out->dist[pos + i];
+                out->dist[pos + i] = out->dist[pos + np - 1 - i];
+                out->dist[pos + np - 1 - i] = t;
+            }
+            bits = 0;
+            index = 0;
+            b = (unsigned char)c.p[0];
+            uint32_t k = 0;
+            for (size_t i = 0; i < ncx; i++) {
+                const uint32_t x = cx[i];
+                if (!flags[x]) continue;
+                if (bits == 7) {
+                    b = (unsigned char)c.p[++index];
+                    bits = 0;
+                }
+                if ((b & 1) == 0 && x > SL) out->dist[pos + np + k++] = x - SL;
+                b >>= 1;
+                bits++;
+            }
+            if ((int64_t)(np + nn) != total) {
+                rc = PGO_EINVAL;
+                break;
+            }
+            out->n_prev[mii] = np;
+            out->n_next[mii] = nn;
+            pos += np + nn;
+            continue;
+        }
+        int64_t ul = -1, uu = -1;
+        if (!read_i64(&c, &ul) || !read_i64(&c, &uu) || !read_token(&c, "|") || c.p >= c.end ||
+            *c.p != ' ') {
+            rc = PGO_EINVAL;
+            break;
+        }
+        ul = -ul;
+        c.p++;
+        if (ul < 0 || uu < 0) {
+            rc = PGO_EINVAL;
+            break;
+        }
+        for (int side = 0; side <= 1 && rc == PGO_OK; side++) {
+            const int64_t n = side ? uu : ul;
+            int64_t acc = 0;
+            for (int64_t k = 0; k < n; k++) {
+                if (job->compression == 1) {
+                    if (c.end - c.p < 2) {
+                        rc = PGO_EINVAL;
+                        break;
+                    }
+                    const unsigned char a = (unsigned char)c.p[0], bb = (unsigned char)c.p[1];
+                    c.p += 2;
+                    acc += (int64_t)(a - 48) * 128 + (bb - 48);
+                } else {
+                    if (!read_i64(&c, &acc)) {
+                        rc = PGO_EINVAL;
+                        break;
+                    }
+                    if (side == 0) acc = -acc;
+                }
+                out->dist[pos++] = (uint32_t)acc;
+            }
+            if (rc == PGO_OK && side == 0) {
+                if (!read_token(&c, "|") || c.p >= c.end || *c.p != ' ') {
+                    rc = PGO_EINVAL;
+                    break;
+                }
+                c.p++;
+            }
+        }
+        out->n_prev[mii] = (uint32_t)ul;
+        out->n_next[mii] = (uint32_t)uu;
+    }
+    if (rc == PGO_OK) out->total = pos;
+    else pgo_lists_free(out);
+    free(cx);
+    free(base_flags);
+    free(flags);
+    state_free(&s);
+    return rc;
+}
+
+/* ------------------------------------------------------------------------ */
 #ifdef PGO_MAIN
 /* m2_oracle -p P -d D --mstart M --minc N --sieve-length SL --max-prime MP(millions)
  *           [-t T] [--rle|--bitcompressed] -o OUT */

@@ -98,6 +98,27 @@ int pgo_plan_job(const pgo_job *job, pgo_plan *plan);
 int pgo_trial_division(const pgo_job *job, const uint64_t *m, const int64_t *x, size_t n,
                        uint64_t *smallest_factor);
 
+/*
+ * The unknowns of every valid m as binary lists: row i (file order) has m[i],
+ * n_prev[i] distances of -X unknowns then n_next[i] of +X unknowns, each side
+ * nearest first, at dist[start[i] ...].  Free with pgo_lists_free.
+ */
+typedef struct {
+    uint64_t rows;
+    uint64_t *m;
+    uint32_t *n_prev, *n_next;
+    uint64_t *start;
+    uint32_t *dist;
+    uint64_t total;
+} pgo_lists;
+
+/* parse_unknown_line (gap_common.cpp:1186-1360) over a whole unknowns file of
+ * any compression; PGO_EINVAL on any line the reference would assert on. */
+int pgo_parse_unknowns(const pgo_job *job, const char *text, size_t len, pgo_lists *out);
+/* The same lists straight from the sieve, without text. */
+int pgo_method2_lists(const pgo_job *job, pgo_lists *out);
+void pgo_lists_free(pgo_lists *l);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,6 +38,18 @@ class OPlan(ctypes.Structure):
     ]
 
 
+class OLists(ctypes.Structure):
+    _fields_ = [
+        ("rows", ctypes.c_uint64),
+        ("m", ctypes.POINTER(ctypes.c_uint64)),
+        ("n_prev", ctypes.POINTER(ctypes.c_uint32)),
+        ("n_next", ctypes.POINTER(ctypes.c_uint32)),
+        ("start", ctypes.POINTER(ctypes.c_uint64)),
+        ("dist", ctypes.POINTER(ctypes.c_uint32)),
+        ("total", ctypes.c_uint64),
+    ]
+
+
 _lib = None
 _u64p = ctypes.POINTER(ctypes.c_uint64)
 
@@ -74,6 +86,12 @@ def load() -> ctypes.CDLL:
         lib.pgo_trial_division.restype = ctypes.c_int
         lib.pgo_trial_division.argtypes = [ctypes.POINTER(OJob), _u64p,
                                            ctypes.POINTER(ctypes.c_int64), ctypes.c_size_t, _u64p]
+        lib.pgo_parse_unknowns.restype = ctypes.c_int
+        lib.pgo_parse_unknowns.argtypes = [ctypes.POINTER(OJob), ctypes.c_char_p, ctypes.c_size_t,
+                                           ctypes.POINTER(OLists)]
+        lib.pgo_method2_lists.restype = ctypes.c_int
+        lib.pgo_method2_lists.argtypes = [ctypes.POINTER(OJob), ctypes.POINTER(OLists)]
+        lib.pgo_lists_free.argtypes = [ctypes.POINTER(OLists)]
         _lib = lib
     return _lib
 
@@ -158,3 +176,39 @@ def trial_division(job: dict, ms: list[int], xs: list[int], threads=8) -> list[i
     if rc != 0:
         raise RuntimeError(f"trial division failed {rc}")
     return list(out[:n])
+
+
+def _lists_out(lib, rc, ol: OLists) -> dict:
+    import numpy as np
+
+    if rc != 0:
+        raise RuntimeError(f"oracle lists failed: {rc}")
+    try:
+        rows, total = ol.rows, ol.total
+        return {
+            "m": np.ctypeslib.as_array(ol.m, (max(rows, 1),))[:rows].copy(),
+            "n_prev": np.ctypeslib.as_array(ol.n_prev, (max(rows, 1),))[:rows].copy(),
+            "n_next": np.ctypeslib.as_array(ol.n_next, (max(rows, 1),))[:rows].copy(),
+            "start": np.ctypeslib.as_array(ol.start, (max(rows, 1),))[:rows].copy(),
+            "dist": np.ctypeslib.as_array(ol.dist, (max(total, 1),))[:total].copy(),
+        }
+    finally:
+        lib.pgo_lists_free(ctypes.byref(ol))
+
+
+def method2_lists(p, d, mstart, minc, sieve_length, max_prime, threads=1) -> dict:
+    """Unknowns per valid m as arrays (m, n_prev, n_next, start, dist)."""
+    lib = load()
+    ol = OLists()
+    rc = lib.pgo_method2_lists(ctypes.byref(_job(p, d, mstart, minc, sieve_length, max_prime, 0,
+                                                 threads)), ctypes.byref(ol))
+    return _lists_out(lib, rc, ol)
+
+
+def parse_unknowns(p, d, mstart, minc, sieve_length, max_prime, compression, text: bytes) -> dict:
+    """parse_unknown_line over a whole unknowns file (any compression)."""
+    lib = load()
+    ol = OLists()
+    rc = lib.pgo_parse_unknowns(ctypes.byref(_job(p, d, mstart, minc, sieve_length, max_prime,
+                                                  compression)), text, len(text), ctypes.byref(ol))
+    return _lists_out(lib, rc, ol)
