@@ -197,6 +197,35 @@ int pgs_server_stats_get(pgs_server *srv, pgs_server_stats *out);
 /* Finish every submitted job, stop the loop and free the server. */
 int pgs_server_stop(pgs_server *srv);
 
+/* ---- unknowns as lists: the next consumer, without a text parse -------- */
+
+/*
+ * Per-m unknown lists in file order, as gap_stats builds them with
+ * parse_unknown_line (gap_common.cpp:1186-1360) from run_gap_file
+ * (gap_stats.cpp:1181-1290): row i is m[i] with n_prev[i] distances of the
+ * -X unknowns then n_next[i] of the +X unknowns, each side nearest first, at
+ * dist[start[i] ...].  Library-owned; free with pgs_unknowns_free.
+ */
+typedef struct {
+    uint64_t rows;
+    uint64_t *m;
+    uint64_t *start;
+    uint32_t *n_prev, *n_next;
+    uint32_t *dist;
+    uint64_t total; /* entries of dist */
+    void *internal;
+} pgs_unknowns;
+/* The lists of a job after pgs_run, read off the device (no text is parsed;
+ * for a bitcompressed job its device-resident text is decoded in place). */
+int pgs_fetch_unknowns(pgs_ctx *ctx, pgs_prepared *prep, pgs_unknowns *out);
+/* Parse the bytes of an unknowns file of the job (plain, RLE or
+ * bitcompressed, per job->compression) on the device.  PGS_EINVAL for a
+ * file whose line count or any line does not match the job (where the
+ * reference asserts). */
+int pgs_parse_unknowns(pgs_ctx *ctx, const pgs_job *job, const char *text, uint64_t len,
+                       pgs_unknowns *out);
+void pgs_unknowns_free(pgs_unknowns *u);
+
 /* ---- the reference's number-theory kernels, batched on the device ---- */
 
 /*

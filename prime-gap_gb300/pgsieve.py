@@ -99,6 +99,19 @@ class ServerStats(ctypes.Structure):
     ]
 
 
+class Unknowns(ctypes.Structure):
+    _fields_ = [
+        ("rows", ctypes.c_uint64),
+        ("m", ctypes.POINTER(ctypes.c_uint64)),
+        ("start", ctypes.POINTER(ctypes.c_uint64)),
+        ("n_prev", ctypes.POINTER(ctypes.c_uint32)),
+        ("n_next", ctypes.POINTER(ctypes.c_uint32)),
+        ("dist", ctypes.POINTER(ctypes.c_uint32)),
+        ("total", ctypes.c_uint64),
+        ("internal", ctypes.c_void_p),
+    ]
+
+
 @dataclass
 class JobSpec:
     """Config fields of one method2 job; max_prime is absolute."""
@@ -153,6 +166,10 @@ _SIGNATURES = {
     "pgs_large_hits_static": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint32,
                                              ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64, _u32p,
                                              _u64p, ctypes.c_size_t, ctypes.POINTER(ctypes.c_size_t)]),
+    "pgs_fetch_unknowns": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(Unknowns)]),
+    "pgs_parse_unknowns": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_char_p,
+                                          ctypes.c_uint64, ctypes.POINTER(Unknowns)]),
+    "pgs_unknowns_free": (None, [ctypes.POINTER(Unknowns)]),
     "pgs_table_reserve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "pgs_batch_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_void_p)]),
@@ -313,6 +330,14 @@ class Sieve:
         self._check(self.lib.pgs_server_start(self.h, hbm_budget, lanes, ctypes.byref(h)))
         return Server(self, h)
 
+    def parse_unknowns(self, job: JobSpec, text: bytes) -> dict:
+        """Per-m unknown lists of an unknowns file, parsed on the device
+        (numpy arrays m, start, n_prev, n_next, dist)."""
+        u = Unknowns()
+        self._check(self.lib.pgs_parse_unknowns(self.h, ctypes.byref(job.c()), text, len(text),
+                                                ctypes.byref(u)))
+        return _unknowns_out(self.lib, u)
+
     def int_peak(self) -> float:
         """Measured 32-bit IMAD issue rate (per second)."""
         v = ctypes.c_double()
@@ -402,6 +427,12 @@ class Prepared:
         finally:
             self.sieve.lib.pgs_result_free(ctypes.byref(res))
         return data
+
+    def unknowns(self) -> dict:
+        """Per-m unknown lists of the last run, straight from the device."""
+        u = Unknowns()
+        self.sieve._check(self.sieve.lib.pgs_fetch_unknowns(self.sieve.h, self.h, ctypes.byref(u)))
+        return _unknowns_out(self.sieve.lib, u)
 
     def close(self) -> None:
         if self.h:
@@ -501,3 +532,20 @@ def _result_stats(res: Result) -> dict:
         "ms_stage": {STAGES[i]: res.ms_stage[i] for i in range(8)},
         "launches": res.launches,
     }
+
+
+def _unknowns_out(lib, u: Unknowns) -> dict:
+    import numpy as np
+
+    try:
+        rows, total = u.rows, u.total
+        arr = np.ctypeslib.as_array
+        return {
+            "m": arr(u.m, (max(rows, 1),))[:rows].copy(),
+            "start": arr(u.start, (max(rows, 1),))[:rows].copy(),
+            "n_prev": arr(u.n_prev, (max(rows, 1),))[:rows].copy(),
+            "n_next": arr(u.n_next, (max(rows, 1),))[:rows].copy(),
+            "dist": arr(u.dist, (max(total, 1),))[:total].copy(),
+        }
+    finally:
+        lib.pgs_unknowns_free(ctypes.byref(u))

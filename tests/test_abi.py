@@ -17,7 +17,8 @@ SYMBOLS = [
     "pgs_plan_job", "pgs_stage_ms", "pgs_int_peak", "pgs_primes", "pgs_k_mod_p", "pgs_modulo_search", "pgs_large_hits",
     "pgs_version", "pgs_table_reserve", "pgs_batch_prepare", "pgs_batch_run", "pgs_batch_fetch",
     "pgs_batch_free", "pgs_method2_batch", "pgs_server_start", "pgs_server_submit", "pgs_server_wait",
-    "pgs_server_stats_get", "pgs_server_stop", "pgs_large_hits_static",
+    "pgs_server_stats_get", "pgs_server_stop", "pgs_large_hits_static", "pgs_fetch_unknowns",
+    "pgs_parse_unknowns", "pgs_unknowns_free",
 ]
 
 
