@@ -476,6 +476,88 @@ def run_batch(args, rank, world, local):
     return 0
 
 
+def run_ingest(args, rank, world, local):
+    """The next consumer's ingestion (gap_stats' parse_unknown_line): config 2's
+    unknowns as per-m lists, parsed on the device from each file format (host
+    text in, host lists out) and read straight off the device after a run,
+    beside the oracle's restatement of the parse on the host."""
+    import ctypes
+
+    import torch
+
+    import pgo
+    import pgsieve
+
+    torch.cuda.set_device(local)
+    job = dict(WORKLOADS["config2"])
+    sieve = pgsieve.Sieve(local)
+    lib = sieve.lib
+    out = {}
+    unknowns = 0
+    for comp, name in ((0, "plain"), (1, "rle"), (2, "bitcompressed")):
+        spec = pgsieve.JobSpec(**job, compression=comp)
+        text = sieve.method2(spec)
+        u = pgsieve.Unknowns()
+
+        def parse():
+            rc = lib.pgs_parse_unknowns(sieve.h, ctypes.byref(spec.c()), text, len(text), ctypes.byref(u))
+            if rc != 0:
+                raise pgsieve.PgsError(rc, lib.pgs_last_error(sieve.h).decode())
+            n = u.total
+            lib.pgs_unknowns_free(ctypes.byref(u))
+            return n
+
+        for _ in range(args.warmup):
+            unknowns = parse()
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            parse()
+        dt = (time.perf_counter() - t) / args.steps
+        out[name] = {"ms": dt * 1e3, "text_bytes": len(text), "text_gb_per_s": len(text) / dt / 1e9,
+                     "unknowns_per_s": unknowns / dt}
+    # straight off the device after a run (no text)
+    spec0 = pgsieve.JobSpec(**job)
+    with sieve.prepare(spec0) as prep:
+        prep.run(False)
+        u = pgsieve.Unknowns()
+        for _ in range(args.warmup):
+            lib.pgs_fetch_unknowns(sieve.h, prep.h, ctypes.byref(u))
+            lib.pgs_unknowns_free(ctypes.byref(u))
+        t = time.perf_counter()
+        for _ in range(args.steps):
+            lib.pgs_fetch_unknowns(sieve.h, prep.h, ctypes.byref(u))
+            lib.pgs_unknowns_free(ctypes.byref(u))
+        dt = (time.perf_counter() - t) / args.steps
+        out["device_lists"] = {"ms": dt * 1e3, "unknowns_per_s": unknowns / dt}
+    # host parse of the same bytes by the oracle (single thread), on the
+    # bitcompressed file of the first 10% of m
+    cpu = None
+    if not args.no_cpu:
+        small = dict(job, minc=job["minc"] // 10)
+        stext = sieve.method2(pgsieve.JobSpec(**small, compression=2))
+        t = time.perf_counter()
+        lists = pgo.parse_unknowns(small["p"], small["d"], small["mstart"], small["minc"],
+                                   small["sieve_length"], small["max_prime"], 2, stext)
+        dt = time.perf_counter() - t
+        cpu = {"value": len(lists["dist"]) / dt, "unit": "unknowns/s", "cores": 1, "kind": "port",
+               "sample": f"bitcompressed file of {small} ({len(stext)} bytes)", "seconds": round(dt, 3)}
+    sieve.close()
+    value = out["bitcompressed"]["unknowns_per_s"]
+    line = {
+        "metric": "unknowns ingested/s (parse_unknown_line replacement)", "value": value,
+        "unit": "unknowns/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": out["bitcompressed"]["ms"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u8/u32 integer", "data": "synthetic",
+        "config": {"workload": "ingest", **job, "unknowns": unknowns,
+                   "value_is": "bitcompressed text on the host to lists on the host"},
+        "formats": out, "cpu_baseline": cpu,
+        "e2e": {"value": value, "unit": "unknowns/s", "h2d_bytes_per_step": out["bitcompressed"]["text_bytes"],
+                "d2h_bytes_per_step": 26301 * 24 + 4 * unknowns},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_served(args, rank, world, local):
     """1000 mixed requests, Poisson arrivals at 80% of the batched job rate,
     admitted against a 150 GB device budget; p50/p99 latency."""
@@ -580,7 +662,7 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS) + ["batch64", "served"])
+    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS) + ["batch64", "served", "ingest"])
     ap.add_argument("--lanes", type=int, default=8, help="streams of the batched/served paths")
     ap.add_argument("--requests", type=int, default=1000, help="served requests")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -588,6 +670,8 @@ def main() -> int:
                     help="override the workload's max_prime (small profiling runs)")
     args = ap.parse_args()
     rank, world, local = _dist()
+    if args.workload == "ingest" and args.impl == "gb300":
+        return run_ingest(args, rank, world, local)
     if args.workload in ("batch64", "served") and args.impl == "gb300":
         return (run_batch if args.workload == "batch64" else run_served)(args, rank, world, local)
     if args.max_prime:
