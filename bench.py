@@ -147,6 +147,35 @@ def run_reference(args, rank, world):
     if rank != 0:
         return 0
     threads = os.cpu_count() or 1
+    if args.workload == "ingest":
+        # the oracle's parse_unknown_line over the first 10% of config 2's m,
+        # bitcompressed file written by the oracle itself
+        import pgo
+
+        j = dict(WORKLOADS["config2"])
+        j["minc"] //= 10
+        text = pgo.method2(j["p"], j["d"], j["mstart"], j["minc"], j["sieve_length"], j["max_prime"], 2,
+                           threads=threads)
+        secs, n = 0.0, 0
+        for _ in range(max(1, args.steps)):
+            t = time.perf_counter()
+            lists = pgo.parse_unknowns(j["p"], j["d"], j["mstart"], j["minc"], j["sieve_length"],
+                                       j["max_prime"], 2, text)
+            secs += time.perf_counter() - t
+            n += len(lists["dist"])
+        value = n / secs
+        line = {
+            "impl": "reference", "metric": "unknowns ingested/s (parse_unknown_line replacement)",
+            "value": value, "unit": "unknowns/s", "n_gpus": world, "steps": args.steps, "warmup": 0,
+            "ms_per_step": secs / max(1, args.steps) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u8/u32 integer", "data": "synthetic",
+            "config": {"workload": "ingest", **j},
+            "cpu_baseline": {"value": value, "unit": "unknowns/s", "cores": 1, "kind": "port",
+                             "sample": f"bitcompressed file of {j}"},
+            "e2e": {"value": value, "unit": "unknowns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return 0
     if args.workload in ("batch64", "served"):
         import workloads
 
