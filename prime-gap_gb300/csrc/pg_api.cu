@@ -221,7 +221,7 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
         CK(mark(b));
         span(PGS_STAGE_PRIMES, a, b);
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), pr->sp_lo,
-                           pr->sp.as<uint32_t>(), misc + 1, pr->sp_bound, pr->sp_hi, nullptr, pr->sr.p,
+                           pr->sp.as<uint32_t>(), misc + 1, pr->sp_bound, nullptr, pr->sr.p,
                            nullptr, false, s));
         CK(mark(a));
         span(PGS_STAGE_KMOD, b, a);
@@ -241,12 +241,12 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
         CK(pg::sieve_window(ctx->base, win.lo, win.hi, ctx->win_off.as<uint32_t>(), win.bound, cnt, s));
         CK(mark(e_b));
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
-                           ctx->win_off.as<uint32_t>(), rng, win.bound, win.hi, &h.walk, ctx->win_r.p,
+                           ctx->win_off.as<uint32_t>(), rng, win.bound, &h.walk, ctx->win_r.p,
                            ctx->win_t0.p, win.wide, s));
         CK(mark(e_c));
         CK(pg::large_window(job, win.lo, ctx->win_off.as<uint32_t>(), rng, win.bound, ctx->win_r.p,
-                            ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint32_t>(),
-                            pr->xmask.as<uint32_t>(),
+                            ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint2>(),
+                            pr->ymask.as<uint2>(),
                             pg::LargeScratch{ctx->large_ctr.as<unsigned long long>(),
                                              ctx->heavy.as<pg::HeavyPrime>(), pg::heavy_capacity()},
                             s));

@@ -164,7 +164,7 @@ uint64_t job_footprint(const HostJob &h) {
     uint64_t b = rows * (per_row + 2ull * h.H * per_entry);     // text
     b += rows * h.pitch * 4ull + rows * 2ull * std::max<uint32_t>(h.H, 1) * 4;  // bitset, lists
     b += rows * (8 + 8 + 8 + 4);                                // counts, bytes, offsets, valid_mi
-    b += h.job.minc * 4 + (2ull * h.job.sieve_length + 1) * 4;  // row_of_mi, col_of_x
+    b += (h.mmask.size() + h.ymask.size()) * 4ull;              // masks, rank counts
     return b;
 }
 
@@ -282,7 +282,7 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
         pr->launches++;
         if (pr->sp_bound) {
             CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, 0, t.small.as<uint32_t>(), misc + 1,
-                               pr->sp_bound, t.small_limit, nullptr, pr->sr.p, nullptr, false, s));
+                               pr->sp_bound, nullptr, pr->sr.p, nullptr, false, s));
             pr->launches++;
         }
         if (!h.dq.empty()) {
@@ -318,8 +318,8 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
                               rng, s));
             const int k = windows[u];
             CK(pg::large_window(job_dev(lead), w.lo, w.off.as<uint32_t>(), rng, w.count, src->a[k], src->b[k],
-                                src->full[k], wide, true, lead->mmask.as<uint32_t>(),
-                                lead->xmask.as<uint32_t>(), scratch, s));
+                                src->full[k], wide, true, lead->mmask.as<uint2>(),
+                                lead->ymask.as<uint2>(), scratch, s));
             lead->launches += 3;
             continue;
         }
@@ -334,11 +334,11 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
         }
         // one job: its walk step and start; a group: K' mod p, each job starts its own walk
         if (shared)
-            CK(pg::kmod_window(d_klimbs, nl_shared, w.lo, w.off.as<uint32_t>(), rr, w.count, w.hi, nullptr,
+            CK(pg::kmod_window(d_klimbs, nl_shared, w.lo, w.off.as<uint32_t>(), rr, w.count, nullptr,
                                lane->r.p, lane->t0.p, wide, s));
         else
             CK(pg::kmod_window(lead->klimbs.as<uint32_t>(), (int)lead->hj.klimbs.size(), w.lo,
-                               w.off.as<uint32_t>(), rr, w.count, w.hi, &lead->hj.walk, lane->r.p,
+                               w.off.as<uint32_t>(), rr, w.count, &lead->hj.walk, lane->r.p,
                                lane->t0.p, wide, s));
         lead->launches += 2;
         for (size_t k = 0; k < users.size(); k++) {
@@ -353,8 +353,8 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
                 pr->launches++;
             }
             CK(pg::large_window(jd, w.lo, w.off.as<uint32_t>(), rng, w.count, lane->r.p,
-                                lane->t0.p, rr, wide, shared, pr->mmask.as<uint32_t>(),
-                                pr->xmask.as<uint32_t>(), scratch, s));
+                                lane->t0.p, rr, wide, shared, pr->mmask.as<uint2>(),
+                                pr->ymask.as<uint2>(), scratch, s));
             pr->launches += 2;
         }
     }
@@ -908,7 +908,7 @@ int kcache_prepare(pgs_server *srv, KEntry *ke, const pgs_prepared *pr, cudaStre
             ke->r[k].pool = &ctx->dpool;
             CK(ke->r[k].ensure(w.count * width + 8));
             CK(pg::kmod_window(ke->limbs.as<uint32_t>(), ke->nl, w.lo, w.off.as<uint32_t>(),
-                               ws.full.as<unsigned long long>(), w.count, w.hi, nullptr, ke->r[k].p,
+                               ws.full.as<unsigned long long>(), w.count, nullptr, ke->r[k].p,
                                fill_r2 ? ws.r2.p : nullptr, wide, s));
             CK(cudaEventCreateWithFlags(&ke->ready[k], cudaEventDisableTiming));
             CK(cudaEventRecord(ke->ready[k], s));

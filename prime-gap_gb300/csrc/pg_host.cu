@@ -46,6 +46,20 @@ uint32_t ndigits(uint64_t v) {
     return n;
 }
 
+// A bitmask as {bits, rank} pairs: word w of the mask followed by the number
+// of set bits in words [0, w), so that the rank of any bit is one pair read
+// and a popcount.
+static std::vector<uint32_t> with_ranks(const std::vector<uint32_t> &mask) {
+    std::vector<uint32_t> out(2 * mask.size());
+    uint32_t run = 0;
+    for (size_t w = 0; w < mask.size(); w++) {
+        out[2 * w] = mask[w];
+        out[2 * w + 1] = run;
+        run += (uint32_t)__builtin_popcount(mask[w]);
+    }
+    return out;
+}
+
 int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     h.job = j;
     // Args::argparse validation (gap_common.cpp:1007-1094)
@@ -167,13 +181,8 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     if (!tables) return PGS_OK;
 
     h.valid_mi.reserve(valid);
-    h.row_of_mi.assign(minc, -1);
-    for (uint64_t mi = 0; mi < minc; mi++) {
-        if (m_ok[mi]) {
-            h.row_of_mi[mi] = (int32_t)h.valid_mi.size();
-            h.valid_mi.push_back((uint32_t)mi);
-        }
-    }
+    for (uint64_t mi = 0; mi < minc; mi++)
+        if (m_ok[mi]) h.valid_mi.push_back((uint32_t)mi);
     // live offsets: coprime to K and of the parity that makes m*K + X odd
     for (uint32_t dd = 1; dd <= SL; dd++) {
         uint32_t x = SL + dd;
@@ -183,18 +192,6 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     h.Hp = (h.H + 31) / 32 * 32;
     h.pitch = (2 * h.Hp / 32 + 3) / 4 * 4;
     if (h.pitch == 0) h.pitch = 4;
-    h.col_of_x.assign(interval, -1);
-    h.xmask.assign((interval + 31) / 32, 0);
-    for (uint32_t i = 0; i < h.H; i++) {
-        uint32_t lo = SL - h.dist[i], hi = SL + h.dist[i];
-        h.col_of_x[lo] = (int32_t)i;
-        h.col_of_x[hi] = (int32_t)(h.Hp + i);
-        h.xmask[lo >> 5] |= 1u << (lo & 31);
-        h.xmask[hi >> 5] |= 1u << (hi & 31);
-    }
-    h.mmask.assign((minc + 31) / 32, 0);
-    for (uint64_t mi = 0; mi < minc; mi++)
-        if (m_ok[mi]) h.mmask[mi >> 5] |= 1u << (mi & 31);
     // parity-reduced large-prime walk (pg::WalkParams)
     pg::WalkParams &w = h.walk;
     if (d_even) {
@@ -216,6 +213,27 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
         w.odd_d = 1;
     }
     w.m0 = ms + w.mi_base;
+    // Bitmasks over the walk's own coordinates: valid m over walk indices j
+    // (mi = mi_base + stride*j; with d even every valid m is odd, on that
+    // lattice) and live offsets over walk residues y (x = X + SL = xc - 2y,
+    // the walk's parity of x).  A hit's bitset row is the rank of j among the
+    // valid m; its column, with ry = live y below y (live x above x), is
+    // ry - H for x < SL (the low side runs in distance order) and Hp+H-1-ry
+    // above SL.
+    h.mmask.assign((w.jmax + 31) / 32, 0);
+    uint64_t on_lattice = 0;
+    for (uint64_t j = 0; j < w.jmax; j++)
+        if (m_ok[w.mi_base + w.stride * j]) h.mmask[j >> 5] |= 1u << (j & 31), on_lattice++;
+    if (on_lattice != valid) return err = "valid m off the walk lattice", PGS_EABORT;
+    h.ymask.assign((w.w + 31) / 32, 0);
+    for (uint32_t dd : h.dist)
+        for (uint32_t x : {SL - dd, SL + dd}) {
+            const uint32_t y = (w.xc - x) / 2;
+            h.ymask[y >> 5] |= 1u << (y & 31);
+        }
+    h.y_lo = (w.xc - SL) / 2 + 1;  // x < SL exactly for y >= y_lo
+    h.mmask = with_ranks(h.mmask);
+    h.ymask = with_ranks(h.ymask);
     return PGS_OK;
 }
 
@@ -243,9 +261,8 @@ pg::JobDev job_dev(pgs_prepared *pr) {
     j.half_cols = h.H;
     j.side_pad = h.Hp;
     j.pitch = h.pitch;
-    j.row_of_mi = pr->row_of_mi.as<int32_t>();
-    j.col_of_x = pr->col_of_x.as<int32_t>();
     j.comp = pr->comp.as<uint32_t>();
+    j.y_lo = h.y_lo;
     j.walk = h.walk;
     j.kmul = 1;
     return j;
@@ -290,13 +307,11 @@ cudaError_t upload_tables(pgs_prepared *pr, cudaStream_t s) {
         const void *src;
         size_t n;
     } items[] = {{&pr->klimbs, h.klimbs.data(), h.klimbs.size() * 4},
-                 {&pr->row_of_mi, h.row_of_mi.data(), h.row_of_mi.size() * 4},
-                 {&pr->col_of_x, h.col_of_x.data(), h.col_of_x.size() * 4},
                  {&pr->valid_mi, h.valid_mi.data(), h.valid_mi.size() * 4},
                  {&pr->dist, h.dist.data(), h.dist.size() * 4},
                  {&pr->dq, h.dq.data(), h.dq.size() * 4},
                  {&pr->mmask, h.mmask.data(), h.mmask.size() * 4},
-                 {&pr->xmask, h.xmask.data(), h.xmask.size() * 4}};
+                 {&pr->ymask, h.ymask.data(), h.ymask.size() * 4}};
     size_t total = 0;
     for (const Item &it : items) total += (it.n + 255) / 256 * 256;
     if (!pr->stage || pr->stage_cap < total) {

@@ -26,12 +26,13 @@ struct HostJob {
     std::vector<uint32_t> klimbs;
     uint32_t kbits = 0;
     std::vector<uint32_t> valid_mi;
-    std::vector<int32_t> row_of_mi;
-    std::vector<int32_t> col_of_x;
     std::vector<uint32_t> dist;
     std::vector<uint32_t> dq;  // odd primes dividing d
-    std::vector<uint32_t> mmask, xmask;  // valid-m and live-offset bitmasks
+    // valid-m bitmask over walk indices j and live-offset bitmask over walk
+    // residues y (pg_host.cu), as {bits, set bits before the word} pairs
+    std::vector<uint32_t> mmask, ymask;
     uint32_t x_par = 0, nb = 0, H = 0, Hp = 0, pitch = 0;
+    uint32_t y_lo = 0;  // walk residues y >= y_lo are offsets below SL
     uint64_t coprime_x = 0;
     uint64_t small_threshold = 0, medium_threshold = 0, prime_limit = 0;
     uint64_t s1 = 0;
@@ -210,7 +211,7 @@ struct pgs_prepared {
     std::vector<int> tbl_windows;
     size_t footprint = 0;  // device bytes held by this job
     uint64_t win_bound = 0;
-    pgh::DevBuf klimbs, row_of_mi, col_of_x, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0, mmask, xmask;
+    pgh::DevBuf klimbs, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0, mmask, ymask;
     pgh::DevBuf lists, counts, row_bytes, offsets, scan_tmp, misc, text;
     std::vector<cudaEvent_t> events;
     std::vector<std::pair<int, std::pair<int, int>>> spans;  // stage, (ev a, ev b)
@@ -218,9 +219,9 @@ struct pgs_prepared {
     uint64_t launches = 0;
     bool ran = false;
     std::vector<pgh::DevBuf *> all() {
-        return {&klimbs, &row_of_mi, &col_of_x, &valid_mi, &dist,   &dq,     &dr,
-                &comp,   &sp,        &sr,       &sp_t0,    &lists,  &counts, &row_bytes,
-                &offsets, &scan_tmp, &misc,     &text,     &mmask,  &xmask};
+        return {&klimbs, &valid_mi, &dist,  &dq,       &dr,      &comp,     &sp,
+                &sr,     &sp_t0,    &lists, &counts,   &row_bytes, &offsets, &scan_tmp,
+                &misc,   &text,     &mmask, &ymask};
     }
     char *stage = nullptr;  // pinned staging block of the table uploads
     size_t stage_cap = 0;

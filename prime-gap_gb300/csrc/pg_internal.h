@@ -59,9 +59,8 @@ cudaError_t set_pair(unsigned long long *d_out, uint64_t a, uint64_t b, cudaStre
 // a walk, a = the walk step and b = its start residue (all words of the
 // primes' width).  Primes below 2^32 use 32-bit words, others 64-bit
 // (wide).  K limbs on the device.
-// pmax: no prime of the call exceeds it.
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
-                        const unsigned long long *d_range, uint64_t max_count, uint64_t pmax,
+                        const unsigned long long *d_range, uint64_t max_count,
                         const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream);
 
 // K mod q for an explicit list of 32-bit primes (d-primes, tests).
@@ -79,9 +78,8 @@ struct JobDev {
     uint32_t half_cols; // H: live columns per side
     uint32_t side_pad;  // Hp: H rounded up to 32, start of the high side
     uint32_t pitch;     // 32-bit words per composite row
-    const int32_t *row_of_mi;  // minc entries, -1 if gcd(m, d) > 1
-    const int32_t *col_of_x;   // 2*SL+1 entries, -1 if not a live offset
     uint32_t *comp;            // rows * pitch words
+    uint32_t y_lo;             // walk residues y >= y_lo are offsets X < 0
     WalkParams walk;           // parity-reduced large-prime walk
     uint32_t kmul;             // K = K' * kmul when the walk starts from K' mod p (else 1)
 };
@@ -97,7 +95,9 @@ struct LargeScratch {
 uint32_t heavy_capacity();
 constexpr size_t kHeavyPrimeBytes = 40;
 
-// d_mmask: valid-m bitmask (minc bits); d_xmask: live-offset bitmask (2SL+1 bits).
+// d_mmask: valid-m bitmask over walk indices j (walk.jmax bits), d_ymask:
+// live-offset bitmask over walk residues y (walk.w bits), each as {bits, set
+// bits before the word} pairs (uint2 per word).
 // d_a/d_b as written by kmod_window over the index range d_rrange, which
 // contains d_range: with start_in_kernel, K mod p and 2^64 mod p (jobs that
 // share K share them; each starts its walk here), else the job's walk step
@@ -105,7 +105,7 @@ constexpr size_t kHeavyPrimeBytes = 40;
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_range, uint64_t max_count, const void *d_a,
                          const void *d_b, const unsigned long long *d_rrange, bool wide,
-                         bool start_in_kernel, const uint32_t *d_mmask, const uint32_t *d_xmask,
+                         bool start_in_kernel, const uint2 *d_mmask, const uint2 *d_ymask,
                          LargeScratch scratch, cudaStream_t stream);
 
 // ---- rows: small primes, merge, extract, format (pg_rows.cu) -----------------

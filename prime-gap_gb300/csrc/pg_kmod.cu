@@ -4,17 +4,15 @@
 // Replaces mpz_fdiv_ui(K, prime) at combined_sieve.cpp:1497 and 1856 (and the
 // mpz_mod_ui of 1674).  One thread per prime (four interleaved chains per
 // thread for 32-bit primes) reduces K's limbs: most significant first,
-// u <- REDC(u * R^2 + limb) with lazy reduction, for primes below 2^31;
-// least significant first, W <- REDC(W + limb) and one multiply by
-// R^(n+1) mod p at the end, for larger primes and long K.  K's limbs sit in
-// shared memory and are read as warp-wide broadcasts.
+// u <- REDC(u * R^2 + limb), for short K; least significant first,
+// W <- REDC(W + limb) and one multiply by R^(n+1) mod p at the end, for long
+// K, where the cheaper step outweighs the power.  K's limbs sit in shared
+// memory and are read as warp-wide broadcasts.
 //
 // Output, per prime: either r = K mod p and r2 = R^2 mod p (R = 2^32 or 2^64
 // by the primes' width), from which a kernel can start any job's walk over
 // this K without a division; or, for one job, its walk step and start residue directly
 // ((base_r * M + SL) % prime, modulo_search.cpp:345; see WalkParams).
-#include <algorithm>
-
 #include "pg_arith.cuh"
 #include "pg_internal.h"
 
@@ -25,7 +23,7 @@ namespace {
 constexpr int kKmodThreads = 256;
 constexpr int kMaxSharedLimbs = 12288;  // 48 KiB
 constexpr int kPrimesPerThread = 4;     // 32-bit primes
-constexpr int kLsbMinLimbs = 20;        // 32-bit primes >= 2^31: LSB chain from 20 limbs
+constexpr int kLsbMinLimbs = 32;        // 32-bit primes: LSB chain from 32 limbs
 constexpr int kLsbMinLimbsWide = 24;    // 64-bit primes: from 12 words
 
 template <bool kWide, bool kLsb>
@@ -43,7 +41,7 @@ __global__ void __launch_bounds__(kKmodThreads)
     const uint64_t begin = range[0];
     const uint64_t n = min((uint64_t)(range[1] - begin), max_count);
     off += begin;
-    // grid-stride: each block loads K's limbs once
+    // the grid covers max_count primes: one pass of the loop per thread
     const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
     if (!kWide) {
         // kPrimesPerThread consecutive primes per thread, interleaved chains
@@ -93,26 +91,19 @@ __global__ void __launch_bounds__(kKmodThreads)
 }  // namespace
 
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
-                        const unsigned long long *d_range, uint64_t max_count, uint64_t pmax,
+                        const unsigned long long *d_range, uint64_t max_count,
                         const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream) {
     if (max_count == 0) return cudaSuccess;
     const WalkParams wp = walk ? *walk : WalkParams{};
     const int ww = walk != nullptr;
     const uint64_t per_thread = wide ? 1 : kPrimesPerThread;
     const uint64_t threads = (max_count + per_thread - 1) / per_thread;
-    int dev = 0, sms = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    // a few waves of resident blocks; each block strides over the rest
-    const uint64_t cap = (uint64_t)std::max(sms, 1) * 32;
-    const unsigned blocks = (unsigned)std::min<uint64_t>((threads + kKmodThreads - 1) / kKmodThreads, cap);
+    const unsigned blocks = (unsigned)((threads + kKmodThreads - 1) / kKmodThreads);
     const size_t smem = nlimbs <= kMaxSharedLimbs ? (size_t)nlimbs * sizeof(uint32_t) : 0;
-    // Primes below 2^31 take the most-significant-first chain with lazy
-    // reduction (a multiply-add, a multiply and a multiply-add per limb);
-    // larger ones the least-significant-first chain (an add, a multiply and a
-    // multiply-add) once it outweighs the R^(n+1) power.
-    const bool lsb =
-        wide ? nlimbs >= kLsbMinLimbsWide : (pmax >= 0x80000000ull && nlimbs >= kLsbMinLimbs);
+    // least significant limb first once the cheaper step (an add, a multiply
+    // and a multiply-add, against a multiply-add, a multiply and a
+    // multiply-add) outweighs the R^(n+1) power
+    const bool lsb = nlimbs >= (wide ? kLsbMinLimbsWide : kLsbMinLimbs);
     if (wide && lsb)
         kmod_kernel<true, true><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
                                                                         d_range, max_count, wp, ww, d_a, d_b);

@@ -23,7 +23,8 @@
 // prime, and the rest publish their rotation in shared memory for phase 2,
 // which spreads their steps over the CTA in items of kItemSteps.  Hits go
 // through a valid-m bitmask and a live-offset bitmask held in shared memory;
-// only the survivors (a few percent) read the row/column tables and set one
+// only the survivors (a few percent) take their bitset row and column as
+// ranks in those masks (rank counts beside them, no table reads) and set one
 // bit of the L2-resident composite bitset with a global atomicOr.
 #include "pg_arith.cuh"
 #include "pg_internal.h"
@@ -38,22 +39,27 @@ constexpr uint32_t kItemSteps = 64;
 constexpr uint64_t kHeavySteps = 16384;
 
 // A walk hit (j, Y) is m = mstart + mi_base + stride*j, x = X + SL = xc - 2Y.
+// The masks are indexed by j and Y and stored as {bits, set bits before the
+// word} pairs, so one 64-bit read per mask gives both a hit's filter bits and,
+// for a survivor, its bitset row (rank of j among the valid m) and column
+// (from ry, the live Y below Y: ry - H for X < 0, Hp + H - 1 - ry above).
 struct Marker {
     const JobDev &job;
-    const uint32_t *mmask;  // valid m bits (shared or global)
-    const uint32_t *xmask;  // live offset bits (shared or global)
-    // Called at every walk step (hit or not) with j < jmax, so mi < minc; the
-    // mask words are read unconditionally (x = 0 stands in off a hit) and only
-    // a surviving hit branches to the table reads and the atomic.
-    __device__ __forceinline__ void operator()(uint64_t j, uint32_t y, bool hit) const {
-        const uint32_t x = hit ? job.walk.xc - 2 * y : 0u;
-        const uint64_t mi = job.walk.mi_base + job.walk.stride * j;
-        const uint32_t xb = (xmask[x >> 5] >> (x & 31)) & 1u;
-        const uint32_t mb = (mmask[mi >> 5] >> (mi & 31)) & 1u;
-        if (hit & (xb & mb)) {
-            const int32_t row = __ldg(&job.row_of_mi[mi]);
-            const int32_t col = __ldg(&job.col_of_x[x]);
-            atomicOr(&job.comp[(uint64_t)row * job.pitch + ((uint32_t)col >> 5)], 1u << (col & 31));
+    const uint2 *mmask;  // valid m over j (shared or global)
+    const uint2 *ymask;  // live offsets over Y
+    // Called at every walk step (hit or not) with j < jmax; the mask pairs
+    // are read unconditionally (Y = 0 stands in off a hit) and only a
+    // surviving hit branches to the atomic.
+    __device__ __forceinline__ void operator()(uint64_t j64, uint32_t y, bool hit) const {
+        const uint32_t j = (uint32_t)j64, yi = hit ? y : 0u;
+        const uint2 yv = ymask[yi >> 5], mv = mmask[j >> 5];
+        const uint32_t yb = (yv.x >> (yi & 31)) & 1u;
+        const uint32_t mb = (mv.x >> (j & 31)) & 1u;
+        if (hit & (yb & mb)) {
+            const uint32_t row = mv.y + __popc(mv.x & ((1u << (j & 31)) - 1u));
+            const uint32_t ry = yv.y + __popc(yv.x & ((1u << (yi & 31)) - 1u));
+            const uint32_t col = yi >= job.y_lo ? ry - job.half_cols : job.side_pad + job.half_cols - 1 - ry;
+            atomicOr(&job.comp[(uint64_t)row * job.pitch + (col >> 5)], 1u << (col & 31));
         }
     }
 };
@@ -80,19 +86,24 @@ struct Slots {
     uint32_t warp_total[kLargeThreads / 32];
 };
 
-__device__ __forceinline__ void load_masks(const JobDev &job, const uint32_t *g_mmask,
-                                           const uint32_t *g_xmask, int in_shared,
-                                           uint32_t *s_masks, const uint32_t *&mmask,
-                                           const uint32_t *&xmask) {
-    const uint32_t mwords = (job.minc + 31) / 32;
-    const uint32_t xwords = (job.two_sl + 1 + 31) / 32;
+// Words of the two masks: valid m over walk indices, live offsets over
+// walk residues.
+__host__ __device__ inline uint32_t mask_words_m(const JobDev &job) { return (uint32_t)((job.walk.jmax + 31) / 32); }
+__host__ __device__ inline uint32_t mask_words_y(const JobDev &job) { return (job.walk.w + 31) / 32; }
+
+// Copies the masks ({bits, rank} pairs) to shared memory when they fit
+// (in_shared); returns where the kernel reads them.
+__device__ __forceinline__ void load_masks(const JobDev &job, const uint2 *g_mmask, const uint2 *g_ymask,
+                                           int in_shared, uint2 *s_masks, const uint2 *&mmask,
+                                           const uint2 *&ymask) {
+    const uint32_t mwords = mask_words_m(job), ywords = mask_words_y(job);
     mmask = g_mmask;
-    xmask = g_xmask;
+    ymask = g_ymask;
     if (in_shared) {
         for (uint32_t i = threadIdx.x; i < mwords; i += blockDim.x) s_masks[i] = g_mmask[i];
-        for (uint32_t i = threadIdx.x; i < xwords; i += blockDim.x) s_masks[mwords + i] = g_xmask[i];
+        for (uint32_t i = threadIdx.x; i < ywords; i += blockDim.x) s_masks[mwords + i] = g_ymask[i];
         mmask = s_masks;
-        xmask = s_masks + mwords;
+        ymask = s_masks + mwords;
     }
     __syncthreads();
 }
@@ -102,16 +113,16 @@ __global__ void __launch_bounds__(kLargeThreads)
     large_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
                  const unsigned long long *range, uint64_t max_count, const T *__restrict__ a_in,
                  const void *__restrict__ b_in, const unsigned long long *rrange,
-                 const uint32_t *__restrict__ g_mmask,
-                 const uint32_t *__restrict__ g_xmask, int masks_in_shared,
+                 const uint2 *__restrict__ g_mmask,
+                 const uint2 *__restrict__ g_ymask, int masks_in_shared,
                  unsigned long long *group_ctr, HeavyPrime *heavy, unsigned long long *heavy_count,
                  uint32_t heavy_cap) {
-    extern __shared__ uint32_t s_masks[];
+    extern __shared__ uint2 s_masks[];
     __shared__ Slots<T> sl;
     __shared__ unsigned long long s_group;
-    const uint32_t *mmask, *xmask;
-    load_masks(job, g_mmask, g_xmask, masks_in_shared, s_masks, mmask, xmask);
-    const Marker mark{job, mmask, xmask};
+    const uint2 *mmask, *ymask;
+    load_masks(job, g_mmask, g_ymask, masks_in_shared, s_masks, mmask, ymask);
+    const Marker mark{job, mmask, ymask};
     const uint64_t n = min((uint64_t)(range[1] - range[0]), max_count);
     off += range[0];
     a_in += range[0] - rrange[0];
@@ -209,12 +220,12 @@ __global__ void __launch_bounds__(kLargeThreads)
 __global__ void __launch_bounds__(kLargeThreads)
     heavy_kernel(JobDev job, const HeavyPrime *__restrict__ heavy,
                  const unsigned long long *heavy_count, uint32_t heavy_cap,
-                 const uint32_t *__restrict__ g_mmask, const uint32_t *__restrict__ g_xmask,
+                 const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask,
                  int masks_in_shared) {
-    extern __shared__ uint32_t s_masks[];
-    const uint32_t *mmask, *xmask;
-    load_masks(job, g_mmask, g_xmask, masks_in_shared, s_masks, mmask, xmask);
-    const Marker mark{job, mmask, xmask};
+    extern __shared__ uint2 s_masks[];
+    const uint2 *mmask, *ymask;
+    load_masks(job, g_mmask, g_ymask, masks_in_shared, s_masks, mmask, ymask);
+    const Marker mark{job, mmask, ymask};
     const uint64_t nh = min((uint64_t)*heavy_count, (uint64_t)heavy_cap);
     const uint32_t w = job.walk.w;
     for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
@@ -237,10 +248,10 @@ uint32_t heavy_capacity() { return 1u << 20; }
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_range, uint64_t max_count, const void *d_a,
                          const void *d_b, const unsigned long long *d_rrange, bool wide,
-                         bool start_in_kernel, const uint32_t *d_mmask, const uint32_t *d_xmask,
+                         bool start_in_kernel, const uint2 *d_mmask, const uint2 *d_ymask,
                          LargeScratch scratch, cudaStream_t stream) {
     if (max_count == 0) return cudaSuccess;
-    const size_t mask_bytes = 4ull * ((job.minc + 31) / 32 + (job.two_sl + 1 + 31) / 32);
+    const size_t mask_bytes = 8ull * (mask_words_m(job) + mask_words_y(job));
     const int in_shared = mask_bytes <= 96 * 1024;
     const size_t smem = in_shared ? mask_bytes : 0;
     int dev = 0, sms = 0, per_sm = 0;
@@ -250,11 +261,10 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
     if ((e = cudaMemsetAsync(scratch.counters, 0, 2 * sizeof(unsigned long long), stream))) return e;
     unsigned long long *group_ctr = scratch.counters, *heavy_count = scratch.counters + 1;
     auto prep = [&](auto kernel) -> cudaError_t {
-        if (smem > 48 * 1024) {
-            cudaError_t err =
-                cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-            if (err) return err;
-        }
+        // static + dynamic shared memory above 48 KiB needs the opt-in, and
+        // the kernels' static part is several KiB: always state the size
+        cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err) return err;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kLargeThreads, smem);
         return cudaSuccess;
     };
@@ -266,7 +276,7 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
         uint64_t blocks = (uint64_t)sms * per_sm;
         if (blocks > groups) blocks = groups;
         kernel<<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_xmask, in_shared,
+            job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask, in_shared,
             group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
         return cudaSuccess;
     };
@@ -281,7 +291,7 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
     if ((e = prep(heavy_kernel))) return e;
     if (per_sm < 1) per_sm = 1;
     heavy_kernel<<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(
-        job, scratch.heavy, heavy_count, scratch.heavy_cap, d_mmask, d_xmask, in_shared);
+        job, scratch.heavy, heavy_count, scratch.heavy_cap, d_mmask, d_ymask, in_shared);
     return cudaGetLastError();
 }
 

@@ -80,6 +80,19 @@ def test_method2_random_vs_oracle(sieve, job):
     assert got == want, _first_diff(got, want)
 
 
+@pytest.mark.parametrize("minc", [177_000, 340_000, 400_000])
+def test_method2_masks_near_shared_memory_limits(sieve, minc):
+    """Valid-m and live-offset masks (8 bytes per 32 walk indices or
+    residues; odd d walks every m) whose shared-memory copy, together with the
+    large kernel's static shared memory, crosses the 48 KiB default (177,000
+    m: 44.5 KiB), nears the 96 KiB limit of the shared copy (340,000 m: 83.3
+    KiB) or exceeds it and is read from global memory (400,000 m: 97.9 KiB)."""
+    spec = pgsieve.JobSpec(89, 105, 1000003, minc, 1000, 2_000_000, 1)
+    got = sieve.method2(spec)
+    want = pgo.method2(89, 105, 1000003, minc, 1000, 2_000_000, 1, threads=16)
+    assert got == want, _first_diff(got, want)
+
+
 def test_prepare_run_fetch_repeatable(sieve, goldens):
     g = goldens["fn1"]
     with sieve.prepare(_spec(g)) as prep:
