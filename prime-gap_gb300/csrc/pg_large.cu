@@ -36,7 +36,7 @@ namespace {
 constexpr int kLargeThreads = 256;
 constexpr uint64_t kDirectSteps = 24;
 constexpr uint32_t kItemSteps = 64;
-constexpr uint64_t kHeavySteps = 16384;
+constexpr uint64_t kHeavySteps = 4096;
 
 // A walk hit (j, Y) is m = mstart + mi_base + stride*j, x = X + SL = xc - 2Y.
 // The masks are indexed by j and Y and stored as {bits, set bits before the
