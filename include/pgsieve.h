@@ -226,6 +226,56 @@ int pgs_parse_unknowns(pgs_ctx *ctx, const pgs_job *job, const char *text, uint6
                        pgs_unknowns *out);
 void pgs_unknowns_free(pgs_unknowns *u);
 
+/* ---- probable-prime tests of the unknowns (the step after the sieve) ---- */
+
+/*
+ * Base-2 strong probable-prime test of count numbers, each n_limbs
+ * little-endian 32-bit limbs at limbs[i * n_limbs ...]; out[i] = 1 for a
+ * probable prime.  Replaces test_runner_t::run_test / kernel_miller_rabin
+ * (miller_rabin.h:247-383) with the one base gap_test_gpu uses (ROUNDS = 1,
+ * gap_test_gpu.cu:81); its squaring loop bound is kept (miller_rabin.h:231-243:
+ * up to s squarings for N - 1 = d 2^s).  rounds must be 1.  Numbers up to 4092
+ * bits; even numbers and numbers below 8 are answered on the host.
+ */
+int pgs_prp_test(pgs_ctx *ctx, const uint32_t *limbs, uint32_t n_limbs, size_t count, int rounds,
+                 uint8_t *out);
+
+typedef struct {
+    uint32_t p, d;          /* K = p#/d */
+    uint32_t sieve_length;  /* past it a side searches on without unknowns */
+    float min_merit;        /* gap_test's --min-merit (the reference's default is 18) */
+    int one_side_skip;      /* 1: gap_test_gpu's skip of the next side when the previous
+                               gap's merit is below min_merit/2 - 2 (gap_test_gpu.cu:570-596);
+                               0: both sides always (gap_test_simple) */
+} pgs_gap_params;
+
+typedef struct {
+    int32_t prev_p, next_p;     /* distances from m*K to the nearest probable primes below
+                                   and above; next_p = 0 when the next side was skipped */
+    uint32_t p_tests, n_tests;  /* unknowns tested on each side, the found one included
+                                   (every unknown of a side that ran past the sieve length) */
+    uint32_t flags;             /* 1: prev past the sieve length, 2: next past it,
+                                   4: next side skipped */
+} pgs_gap_result;
+
+typedef struct {
+    uint64_t rounds;     /* device rounds (candidate selection, tests, resolution) */
+    uint64_t prp_tests;  /* probable-prime tests run, speculative ones included */
+    uint32_t limbs;      /* 32-bit limbs per number on the device */
+} pgs_gap_stats;
+
+/*
+ * The prime gap around m*K for every row of lists: each side's unknowns tested
+ * nearest first until a probable prime, then past the sieve length the first
+ * probable prime beyond it (replaces gap_test_gpu's load / GPU / overflow
+ * threads, gap_test_gpu.cu:213-640, and test_interval_cpu with
+ * mpz_prevprime / mpz_nextprime, gap_test_common.cpp:128-181).  out has
+ * lists->rows entries; stats may be NULL.  PGS_EINVAL for p, d or lists that do
+ * not fit (m*K up to 4092 bits).
+ */
+int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *params, const pgs_unknowns *lists,
+                 pgs_gap_result *out, pgs_gap_stats *stats);
+
 /* ---- the reference's number-theory kernels, batched on the device ---- */
 
 /*

@@ -1,11 +1,13 @@
 #!/bin/bash
 # Test infrastructure only: compile the reference combined_sieve from its own
 # sources (read in place, never copied) against the declaration shims in
-# oracle/refshim, into oracle/_ref/.  Two binaries are produced:
+# oracle/refshim, into oracle/_ref/.  Three binaries are produced:
 #   combined_sieve          unmodified sources
 #   combined_sieve_wheelfix same sources with the inverted wheel test in
 #                           combined_sieve.cpp:1134-1140 corrected, so jobs with
 #                           gcd(d,210)=30 and SL > 30583 do not abort
+#   gap_test_simple         unmodified sources (gap_test_simple.cpp,
+#                           gap_test_common.cpp)
 # Never built with -DNDEBUG: the reference has side effects inside assert().
 # Needs the runtime libgmp.so.10 and libsqlite3.so.0; exits 0 with a message
 # when the sources or libraries are absent.
@@ -45,4 +47,8 @@ sed -e 's/if (wheel % 7) {/if (wheel % 7 == 0) {/' \
     "$REF/combined_sieve.cpp" | \
     g++ $CXXFLAGS -o "$OUT/combined_sieve_wheelfix" -x c++ - -x none $SRCS "$GMP" "$SQL"
 
-echo "build_ref: built $OUT/combined_sieve and $OUT/combined_sieve_wheelfix"
+# The reference's CPU gap tester (mpz_probab_prime_p, mpz_prevprime/nextprime):
+# the known answers of the probable-prime gap search.
+g++ $CXXFLAGS -o "$OUT/gap_test_simple" "$REF/gap_test_simple.cpp" "$REF/gap_test_common.cpp" $SRCS "$GMP" "$SQL"
+
+echo "build_ref: built $OUT/combined_sieve, $OUT/combined_sieve_wheelfix and $OUT/gap_test_simple"

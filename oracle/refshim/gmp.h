@@ -35,6 +35,7 @@ unsigned long __gmpz_get_ui(mpz_srcptr);
 double __gmpz_get_d_2exp(long *, mpz_srcptr);
 void __gmpz_add_ui(mpz_ptr, mpz_srcptr, unsigned long);
 void __gmpz_sub_ui(mpz_ptr, mpz_srcptr, unsigned long);
+void __gmpz_sub(mpz_ptr, mpz_srcptr, mpz_srcptr);
 void __gmpz_mul(mpz_ptr, mpz_srcptr, mpz_srcptr);
 void __gmpz_mul_ui(mpz_ptr, mpz_srcptr, unsigned long);
 void __gmpz_mod(mpz_ptr, mpz_srcptr, mpz_srcptr);
@@ -65,6 +66,7 @@ int __gmpz_probab_prime_p(mpz_srcptr, int);
 #define mpz_get_d_2exp __gmpz_get_d_2exp
 #define mpz_add_ui __gmpz_add_ui
 #define mpz_sub_ui __gmpz_sub_ui
+#define mpz_sub __gmpz_sub
 #define mpz_mul __gmpz_mul
 #define mpz_mul_ui __gmpz_mul_ui
 #define mpz_mod __gmpz_mod

@@ -32,7 +32,7 @@ NVCC_FLAGS = ARCH + [
     f"-I{INCLUDE}", f"-I{CSRC}",
 ]
 CU_SOURCES = ["pg_primes.cu", "pg_kmod.cu", "pg_large.cu", "pg_rows.cu", "pg_tools.cu", "pg_host.cu",
-              "pg_api.cu", "pg_batch.cu", "pg_static.cu", "pg_unknowns.cu"]
+              "pg_api.cu", "pg_batch.cu", "pg_static.cu", "pg_unknowns.cu", "pg_prp.cu"]
 
 LIB = BUILD / "libpgsieve.so"
 CLI = BUILD / "combined_sieve"

@@ -112,6 +112,34 @@ class Unknowns(ctypes.Structure):
     ]
 
 
+class GapParams(ctypes.Structure):
+    _fields_ = [
+        ("p", ctypes.c_uint32),
+        ("d", ctypes.c_uint32),
+        ("sieve_length", ctypes.c_uint32),
+        ("min_merit", ctypes.c_float),
+        ("one_side_skip", ctypes.c_int),
+    ]
+
+
+class GapResult(ctypes.Structure):
+    _fields_ = [
+        ("prev_p", ctypes.c_int32),
+        ("next_p", ctypes.c_int32),
+        ("p_tests", ctypes.c_uint32),
+        ("n_tests", ctypes.c_uint32),
+        ("flags", ctypes.c_uint32),
+    ]
+
+
+class GapStats(ctypes.Structure):
+    _fields_ = [
+        ("rounds", ctypes.c_uint64),
+        ("prp_tests", ctypes.c_uint64),
+        ("limbs", ctypes.c_uint32),
+    ]
+
+
 @dataclass
 class JobSpec:
     """Config fields of one method2 job; max_prime is absolute."""
@@ -170,6 +198,10 @@ _SIGNATURES = {
     "pgs_parse_unknowns": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_char_p,
                                           ctypes.c_uint64, ctypes.POINTER(Unknowns)]),
     "pgs_unknowns_free": (None, [ctypes.POINTER(Unknowns)]),
+    "pgs_prp_test": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint32), ctypes.c_uint32,
+                                    ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(ctypes.c_uint8)]),
+    "pgs_prp_gaps": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GapParams), ctypes.POINTER(Unknowns),
+                                    ctypes.POINTER(GapResult), ctypes.POINTER(GapStats)]),
     "pgs_table_reserve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "pgs_batch_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_void_p)]),
@@ -337,6 +369,44 @@ class Sieve:
         self._check(self.lib.pgs_parse_unknowns(self.h, ctypes.byref(job.c()), text, len(text),
                                                 ctypes.byref(u)))
         return _unknowns_out(self.lib, u)
+
+    def prp_test(self, numbers: list[int]) -> list[bool]:
+        """Base-2 strong probable-prime test of each number (pgs_prp_test)."""
+        if not numbers:
+            return []
+        n_limbs = max(1, max((x.bit_length() + 31) // 32 for x in numbers))
+        buf = (ctypes.c_uint32 * (n_limbs * len(numbers)))()
+        for i, x in enumerate(numbers):
+            for j in range(n_limbs):
+                buf[i * n_limbs + j] = (x >> (32 * j)) & 0xFFFFFFFF
+        out = (ctypes.c_uint8 * len(numbers))()
+        self._check(self.lib.pgs_prp_test(self.h, buf, n_limbs, len(numbers), 1, out))
+        return [bool(v) for v in out]
+
+    def prp_gaps(self, p: int, d: int, sieve_length: int, lists: dict, min_merit: float = 18.0,
+                 one_side_skip: bool = False) -> tuple[list[tuple[int, int, int, int, int]], dict]:
+        """The gap around m*K for every row of ``lists`` (numpy arrays m, start,
+        n_prev, n_next, dist as from parse_unknowns / Prepared.unknowns):
+        [(prev_p, next_p, p_tests, n_tests, flags)] and the search stats."""
+        import numpy as np
+
+        rows = len(lists["m"])
+        arrs = {k: np.ascontiguousarray(lists[k], dtype=t) for k, t in
+                (("m", np.uint64), ("start", np.uint64), ("n_prev", np.uint32), ("n_next", np.uint32),
+                 ("dist", np.uint32))}
+        u = Unknowns()
+        u.rows, u.total = rows, len(arrs["dist"])
+        u.m = arrs["m"].ctypes.data_as(_u64p)
+        u.start = arrs["start"].ctypes.data_as(_u64p)
+        u.n_prev = arrs["n_prev"].ctypes.data_as(_u32p)
+        u.n_next = arrs["n_next"].ctypes.data_as(_u32p)
+        u.dist = arrs["dist"].ctypes.data_as(_u32p)
+        prm = GapParams(p, d, sieve_length, min_merit, int(one_side_skip))
+        out = (GapResult * max(1, rows))()
+        st = GapStats()
+        self._check(self.lib.pgs_prp_gaps(self.h, ctypes.byref(prm), ctypes.byref(u), out, ctypes.byref(st)))
+        res = [(r.prev_p, r.next_p, r.p_tests, r.n_tests, r.flags) for r in out[:rows]]
+        return res, {"rounds": st.rounds, "prp_tests": st.prp_tests, "limbs": st.limbs}
 
     def int_peak(self) -> float:
         """Measured 32-bit IMAD issue rate (per second)."""
