@@ -2,7 +2,7 @@
 """Throughput of the GB300 method2 sieve (and of the CPU reference arm).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
-                    [--workload config2|config1|config3]
+                    [--workload config2|config1|config3|batch64|served|ingest|prp]
 
 One step = one whole method2 job (prime sieve, K mod p, large-prime marks,
 small-prime rows, compaction, text) on the default workload: P=1511, d=2190,
@@ -173,6 +173,36 @@ def run_reference(args, rank, world):
             "cpu_baseline": {"value": value, "unit": "unknowns/s", "cores": 1, "kind": "port",
                              "sample": f"bitcompressed file of {j}"},
             "e2e": {"value": value, "unit": "unknowns/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line), flush=True)
+        return 0
+    if args.workload == "prp":
+        # the oracle's gap search over the first 64 m of config 2's unknowns
+        # (lists from the oracle's own sieve), all host cores
+        import pgo
+
+        j = dict(WORKLOADS["config2"], minc=300)
+        text = pgo.method2(j["p"], j["d"], j["mstart"], j["minc"], j["sieve_length"], j["max_prime"], 0,
+                           threads=threads)
+        lists = pgo.parse_unknowns(j["p"], j["d"], j["mstart"], j["minc"], j["sieve_length"], j["max_prime"], 0,
+                                   text)
+        secs, rows = 0.0, 0
+        c = None
+        for _ in range(max(1, args.steps)):
+            c = _prp_cpu_sample(lists, j, threads)
+            secs += c["seconds"]
+            rows += c["rows"]
+        value = rows / secs
+        line = {
+            "impl": "reference", "metric": "prime gaps searched/s (gap_test_gpu replacement)", "value": value,
+            "unit": "m/s", "n_gpus": world, "steps": args.steps, "warmup": 0,
+            "ms_per_step": secs / max(1, args.steps) * 1e3, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "u32 multi-precision", "data": "synthetic",
+            "config": {"workload": "prp", **WORKLOADS["config2"], "min_merit": PRP_MIN_MERIT,
+                       "one_side_skip": True},
+            "cpu_baseline": {"value": value, "unit": "m/s", "cores": threads, "kind": "port",
+                             "sample": c["sample"], "tests_per_s": c["tests_per_s"]},
+            "e2e": {"value": value, "unit": "m/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line), flush=True)
         return 0
@@ -587,6 +617,127 @@ def run_ingest(args, rank, world, local):
     return 0
 
 
+PRP_MIN_MERIT = 18.0  # gap_test's default --min-merit (gap_common.h:49)
+PRP_SAMPLE_ROWS = 64  # rows of the all-core reference arm (16 for the one-core baseline)
+
+
+def _prp_rows_oracle(payload):
+    """One worker of the CPU gap search: the oracle over a chunk of rows."""
+    import prp_oracle as po
+
+    p, d, sl, lists = payload
+    k = po.primorial_k(p, d)
+    res = po.gap_search(k, sl, lists, min_merit=PRP_MIN_MERIT, one_side_skip=True)
+    return len(res), sum(r[2] + r[3] for r in res)
+
+
+def _prp_cpu_sample(lists: dict, job: dict, workers: int, rows: int = PRP_SAMPLE_ROWS) -> dict:
+    """The oracle's gap search (gap_test_gpu semantics) over the first `rows`
+    rows on `workers` processes (spawned)."""
+    import concurrent.futures
+    import multiprocessing
+
+    rows = min(rows, len(lists["m"]))
+    chunks = []
+    for w in range(workers):
+        idx = list(range(w, rows, workers))
+        if idx:
+            chunks.append((job["p"], job["d"], job["sieve_length"],
+                           {"m": [int(lists["m"][i]) for i in idx], "start": [int(lists["start"][i]) for i in idx],
+                            "n_prev": [int(lists["n_prev"][i]) for i in idx],
+                            "n_next": [int(lists["n_next"][i]) for i in idx], "dist": lists["dist"]}))
+    t = time.perf_counter()
+    if workers == 1:
+        done = [_prp_rows_oracle(c) for c in chunks]
+    else:
+        ctx = multiprocessing.get_context("spawn")
+        with concurrent.futures.ProcessPoolExecutor(max_workers=len(chunks), mp_context=ctx) as ex:
+            done = list(ex.map(_prp_rows_oracle, chunks))
+    dt = time.perf_counter() - t
+    n_rows = sum(a for a, _ in done)
+    tests = sum(b for _, b in done)
+    return {"seconds": dt, "rows": n_rows, "tests": tests, "value": n_rows / dt, "tests_per_s": tests / dt,
+            "sample": f"first {n_rows} m of config 2's unknowns, one-side skip, min_merit {PRP_MIN_MERIT}"}
+
+
+def _prp_lists(sieve, job):
+    import pgsieve
+
+    with sieve.prepare(pgsieve.JobSpec(**job)) as prep:
+        prep.run(False)
+        return prep.unknowns()
+
+
+def run_prp(args, rank, world, local):
+    """The prime-gap search after the sieve (gap_test_gpu): config 2's unknown
+    lists (26,301 m) from the host to the device, each side tested nearest
+    first with the base-2 strong probable-prime test until a probable prime,
+    gap_test_gpu's one-side skip at min_merit 18, results back to the host."""
+    import torch
+    import pgsieve
+
+    torch.cuda.set_device(local)
+    job = dict(WORKLOADS["config2"])
+    sieve = pgsieve.Sieve(local)
+    lists = _prp_lists(sieve, job)
+    rows = len(lists["m"])
+
+    def step():
+        return sieve.prp_gaps(job["p"], job["d"], job["sieve_length"], lists, min_merit=PRP_MIN_MERIT,
+                              one_side_skip=True)
+
+    for _ in range(args.warmup):
+        res, st = step()
+    clocks = ClockSampler(local)
+    torch.cuda.synchronize()
+    clocks.start()
+    t = time.perf_counter()
+    launched = counted = rounds = 0
+    for _ in range(args.steps):
+        res, st = step()
+        launched += st["prp_tests"]
+        rounds += st["rounds"]
+        counted += sum(r[2] + r[3] for r in res)
+    torch.cuda.synchronize()
+    dt = (time.perf_counter() - t) / args.steps
+    clock_info = clocks.stop()
+    peak = sieve.int_peak()
+    # roofline: Montgomery products of n limbs, 2n^2 32-bit multiply-adds
+    # (64-bit results: two IMAD issue slots each) per product, one product per
+    # bit of N, over every test launched
+    import prp_oracle as po
+
+    n = st["limbs"]
+    bits = po.primorial_k(job["p"], job["d"]).bit_length() + int(max(lists["m"])).bit_length()
+    ops = launched / args.steps * bits * 2 * n * n * 2
+    cpu = None
+    if not args.no_cpu:
+        c = _prp_cpu_sample(lists, job, 1, rows=16)
+        cpu = {"value": c["value"], "unit": "m/s", "cores": 1, "kind": "port", "sample": c["sample"],
+               "tests_per_s": c["tests_per_s"], "seconds": round(c["seconds"], 2)}
+    sieve.close()
+    value = rows / dt
+    line = {
+        "metric": "prime gaps searched/s (gap_test_gpu replacement)", "value": value, "unit": "m/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": dt * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32 multi-precision",
+        "data": "synthetic",
+        "config": {"workload": "prp", **job, "rows": rows, "unknowns": int(len(lists["dist"])),
+                   "min_merit": PRP_MIN_MERIT, "one_side_skip": True, "bits": bits,
+                   "value_is": "lists on the host to gaps on the host"},
+        "prp_tests_per_s": counted / args.steps / dt, "prp_launched_per_s": launched / args.steps / dt,
+        "rounds_per_step": rounds / args.steps,
+        "roofline": {"kernel": f"prp_kernel<{n // 8}>", "bound": "int", "achieved": ops / dt, "peak": peak,
+                     "unit": "int ops/s", "frac": ops / dt / peak, "traffic": None,
+                     "peak_source": "measured live: IMAD microbenchmark (pgs_int_peak)"},
+        "cpu_baseline": cpu, "clocks": clock_info, "gpu_launches": args.steps * (2 + 3 * rounds // args.steps),
+        "e2e": {"value": value, "unit": "m/s", "h2d_bytes_per_step": rows * 24 + 4 * int(len(lists["dist"])),
+                "d2h_bytes_per_step": rows * 20},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_served(args, rank, world, local):
     """1000 mixed requests, Poisson arrivals at 80% of the batched job rate,
     admitted against a 150 GB device budget; p50/p99 latency."""
@@ -691,7 +842,8 @@ def main() -> int:
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default="config2", choices=sorted(WORKLOADS) + ["batch64", "served", "ingest"])
+    ap.add_argument("--workload", default="config2",
+                    choices=sorted(WORKLOADS) + ["batch64", "served", "ingest", "prp"])
     ap.add_argument("--lanes", type=int, default=8, help="streams of the batched/served paths")
     ap.add_argument("--requests", type=int, default=1000, help="served requests")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
@@ -701,6 +853,8 @@ def main() -> int:
     rank, world, local = _dist()
     if args.workload == "ingest" and args.impl == "gb300":
         return run_ingest(args, rank, world, local)
+    if args.workload == "prp" and args.impl == "gb300":
+        return run_prp(args, rank, world, local)
     if args.workload in ("batch64", "served") and args.impl == "gb300":
         return (run_batch if args.workload == "batch64" else run_served)(args, rank, world, local)
     if args.max_prime:
