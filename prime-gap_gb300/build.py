@@ -105,8 +105,8 @@ def build_reference() -> None:
     ref = Path(os.environ.get("PG_REFERENCE_DIR", "/root/reference"))
     if not (ref / "combined_sieve.cpp").exists():
         return
-    out = ORACLE / "_ref" / "combined_sieve"
-    if out.exists():
+    outs = [ORACLE / "_ref" / name for name in ("combined_sieve", "combined_sieve_wheelfix", "gap_test_simple")]
+    if all(o.exists() for o in outs):
         return
     subprocess.run(["bash", str(script)], check=True, capture_output=True)
 

@@ -11,19 +11,24 @@
 //
 // --method1 produces the same bytes (the reference checks the two methods
 // against each other, misc/tests.sh:62-67) under the .m1.txt name.
-// Not carried over: the d optimizer for d % 4 == 0 and the automatic
-// sieve-length choice of set_defaults (combined_sieve.cpp:160-300).
+// set_defaults (combined_sieve.cpp:160-344) runs as in the reference: the d
+// optimizer for d % 4 == 0 (count_K_d statistics, gap_common.cpp:455-571,
+// then exit 0), the automatic sieve length and the automatic max_prime.
 #include <dlfcn.h>
 #include <getopt.h>
 #include <libgen.h>
 
+#include <cassert>
 #include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <map>
 #include <string>
+#include <tuple>
+#include <vector>
 
 #include "pgsieve.h"
 
@@ -61,6 +66,188 @@ bool is_prime_brute(uint64_t n) {
     for (uint64_t t = 3; t * t <= n; t += 2)
         if (n % t == 0) return false;
     return true;
+}
+
+// ---- set_defaults (combined_sieve.cpp:160-344) and its helpers ----
+
+uint64_t gcd_u64(uint64_t a, uint64_t b) { return b == 0 ? a : gcd_u64(b, a % b); }
+
+std::vector<uint32_t> primes_upto(uint32_t n) {
+    std::vector<uint32_t> out;
+    std::vector<char> comp(n + 1, 0);
+    for (uint32_t i = 2; i <= n; i++) {
+        if (comp[i]) continue;
+        out.push_back(i);
+        for (uint64_t j = (uint64_t)i * i; j <= n; j += i) comp[j] = 1;
+    }
+    return out;
+}
+
+// K = p#/d as 32-bit limbs (init_K, gap_common.cpp:116-121; d divides p#)
+std::vector<uint32_t> build_k(uint32_t p, uint32_t d) {
+    std::vector<uint32_t> k{1};
+    uint32_t rest = d;
+    for (uint32_t q : primes_upto(p)) {
+        if (rest % q == 0) {
+            rest /= q;
+            continue;
+        }
+        uint64_t c = 0;
+        for (auto &l : k) {
+            const uint64_t t = (uint64_t)l * q + c;
+            l = (uint32_t)t;
+            c = t >> 32;
+        }
+        if (c) k.push_back((uint32_t)c);
+    }
+    assert(rest == 1);
+    return k;
+}
+
+uint32_t k_mod(const std::vector<uint32_t> &k, uint32_t d) {
+    uint64_t r = 0;
+    for (size_t i = k.size(); i-- > 0;) r = ((r << 32) | k[i]) % d;
+    return (uint32_t)r;
+}
+
+// _log(K) (gap_common.cpp:100-104): GMP's truncated 53-bit mantissa in
+// [0.5, 1) and its exponent
+double k_log(const std::vector<uint32_t> &k) {
+    const uint32_t b = 32u * (uint32_t)(k.size() - 1) + (32u - (uint32_t)__builtin_clz(k.back()));
+    uint64_t top = 0;
+    for (uint32_t i = 0; i < 53; i++) {
+        const uint32_t bit = b >= i + 1 ? (k[(b - 1 - i) >> 5] >> ((b - 1 - i) & 31)) & 1u : 0u;
+        top = (top << 1) | bit;
+    }
+    return std::log((double)top / 9007199254740992.0) + std::log(2.0) * b;
+}
+
+// prob_prime_coprime (gap_common.cpp:615-625)
+double prob_prime_coprime(const Config &c) {
+    const double N_log = k_log(build_k(c.p, c.d)) + std::log((double)c.mstart);
+    double prob = 1 / N_log - 1 / (N_log * N_log);
+    for (uint32_t q : primes_upto(c.p)) prob /= (1 - 1.0 / q);
+    return prob;
+}
+
+// count_K_d (gap_common.cpp:455-571): average expected gap, coprime
+// offsets per side and the chance a side has no prime within SL, over the
+// first (up to 5000) valid m.
+std::tuple<double, uint32_t, double, double> count_K_d(const Config &c) {
+    const uint64_t d = c.d;
+    const uint64_t K_mod_d = k_mod(build_k(c.p, c.d), c.d);
+    const std::vector<uint32_t> P_primes = primes_upto(c.p);
+    assert(P_primes.back() == c.p);
+    const double prob_prime_adj = prob_prime_coprime(c);
+    std::vector<uint32_t> D_primes;
+    for (uint32_t q : P_primes)
+        if (d % q == 0) D_primes.push_back(q);
+    const size_t sl = c.sieve_length, length = 2 * sl + 1;
+    std::vector<char> compositeK(length, 0), composite(length);
+    for (uint32_t q : P_primes)
+        if (d % q != 0)
+            for (size_t x = sl % q; x < length; x += q) compositeK[x] = 1;
+    double expected_length = 0, remaining_prob = 0;
+    size_t expected_count = 0, m_count = 0;
+    const uint64_t intervals = std::min<uint64_t>(d, 5000);
+    for (uint64_t m = c.mstart; m_count < intervals; m++) {
+        if (m >= c.mstart + c.minc) break;
+        if (d > 1 && gcd_u64(m, d) > 1) continue;
+        m_count++;
+        composite = compositeK;
+        for (uint32_t q : D_primes) {
+            assert(K_mod_d % q != 0);
+            const uint64_t first = (q - (((m % q) * (K_mod_d % q) + q - (sl % q)) % q)) % q;
+            for (size_t x = first; x < length; x += q) composite[x] = 1;
+        }
+        for (int dir = -1; dir <= 1; dir += 2) {
+            double expected = 0, prob = 1.0;
+            for (int x = 0; (size_t)x <= sl; x++) {
+                if (!composite[sl + dir * x]) {
+                    expected += x * prob * prob_prime_adj;
+                    prob *= 1 - prob_prime_adj;
+                    expected_count += 1;
+                }
+            }
+            expected += sl * prob;
+            expected_length += expected;
+            remaining_prob += prob;
+        }
+    }
+    return {expected_length / m_count, (uint32_t)(expected_count / (m_count * 2)),
+            remaining_prob / (m_count * 2), prob_prime_adj};
+}
+
+// The d optimizer (combined_sieve.cpp:166-209): for d = 4 * large_prime (or
+// 4), statistics of d = lp * q# for lp in {1, large prime}; exits 0.
+[[noreturn]] void d_optimizer(Config c) {
+    c.sieve_length = c.p * c.min_merit;
+    c.mstart = 1;
+    c.d /= 4;
+    const std::vector<uint32_t> P_primes = primes_upto(c.p);
+    const uint32_t rand_prime = P_primes[P_primes.size() - 2 - (rand() % 10)];
+    const uint32_t large_p = c.d > 1 ? c.d : rand_prime;
+    assert(is_prime_brute(large_p));
+    printf("d optimizer for P = %d# | large prime=%d | SL=%d (%.1f merit)\n", c.p, large_p, c.sieve_length,
+           c.min_merit);
+    const uint32_t primes[] = {1, 2, 3, 5, 7, 11, 13, 17, 19, 23};
+    for (uint32_t lp : {1u, large_p}) {
+        c.d = lp;
+        for (uint32_t q : primes) {
+            if (q != 1 && c.d % q == 0) continue;
+            if (__builtin_umul_overflow(c.d, q, &c.d)) break;
+            c.minc = std::min(c.d, 20000U);
+            const auto expected = count_K_d(c);
+            printf("Optimizing | d = %5d * %2d# | %d remaining, %5.0f avg gap | SL insufficient %.3f%% of time\n",
+                   lp, q, std::get<1>(expected), std::get<0>(expected), 100 * std::get<2>(expected));
+        }
+    }
+    exit(0);
+}
+
+// The automatic sieve length (combined_sieve.cpp:224-308): the smallest SL
+// at which, for the worst (m*K) mod d of the range, the chance that no
+// coprime offset in (0, SL] is prime falls to 0.8 %.
+uint32_t auto_sieve_length(const Config &c) {
+    const double prob_prime_coprime_P = prob_prime_coprime(c);
+    std::vector<uint32_t> K_primes;
+    for (uint32_t q : primes_upto(c.p))
+        if (c.d % q != 0) K_primes.push_back(q);
+    assert(c.p >= 503);
+    assert(c.d <= 30030);
+    const uint32_t base = k_mod(build_k(c.p, c.d), c.d);
+    std::vector<uint32_t> count_by_mod_d(c.d, 0);
+    for (uint64_t mi = 0; mi < c.minc; mi++) {
+        const uint64_t m = c.mstart + mi;
+        if (gcd_u64(m, c.d) == 1) {
+            const uint32_t center = (uint32_t)(((unsigned __int128)m * base) % c.d);
+            const uint32_t center_down = (c.d - center) % c.d;
+            count_by_mod_d[center] += 1;
+            count_by_mod_d[center_down] += 1;
+        }
+    }
+    std::map<uint32_t, uint32_t> coprime_by_mod_d;
+    for (size_t i = 0; i < c.d; i++)
+        if (count_by_mod_d[i] > 0) coprime_by_mod_d[(uint32_t)i] = 0;
+    for (size_t tSL = 1;; tSL += 1) {
+        bool any_divisible = false;
+        for (uint32_t q : K_primes)
+            if (tSL % q == 0) {
+                any_divisible = true;
+                break;
+            }
+        if (any_divisible) continue;
+        for (auto &cc : coprime_by_mod_d)
+            if (gcd_u64(cc.first + tSL, c.d) == 1) cc.second += 1;
+        uint32_t min_coprime = (uint32_t)tSL;
+        for (auto &cc : coprime_by_mod_d) min_coprime = std::min(min_coprime, cc.second);
+        const double prob_gap_shorter = std::pow(1 - prob_prime_coprime_P, min_coprime);
+        if (prob_gap_shorter <= 0.008) {
+            printf("AUTO SET: sieve length: %ld (coprime: %d, prob_gap longer %.2f%%)\n", (long)tSL, min_coprime,
+                   100 * prob_gap_shorter);
+            return (uint32_t)tSL;
+        }
+    }
 }
 
 void show_usage(const char *name) {
@@ -290,27 +477,22 @@ int main(int argc, char **argv) {
         return 1;
     }
     // set_defaults (combined_sieve.cpp:160-344)
-    if (c.d % 4 == 0) {
-        printf("d optimizer (d %% 4 == 0) is not part of this build\n");
-        return 1;
-    }
+    if (c.d % 4 == 0) d_optimizer(c);
     if (c.sieve_length == 0) {
-        printf("--sieve-length must be given (automatic choice is not part of this build)\n");
-        return 1;
+        c.sieve_length = auto_sieve_length(c);
+        assert(c.sieve_length > 100);
     }
     if (c.max_prime == 0) {
-        pgs_job probe{c.p, c.d, c.mstart, c.minc, c.sieve_length, 10000000000ull, 0, 0};
-        pgs_plan plan;
-        pgs_plan_job(&probe, &plan);
-        double k_log = plan.k_bits * std::log(2.0);
-        c.max_prime = k_log >= 1500 ? 100000000000ull : 10000000000ull;
+        const double K_log = k_log(build_k(c.p, c.d));
+        c.max_prime = K_log >= 1500 ? 100000000000ull : 10000000000ull;
         if (c.method1) {
             printf("Can't use method1 and not set max_prime");
             return 1;
         }
-        if (c.verbose >= 0)
-            printf("AUTO SET: max_prime (log(K) = ~%.0f): %llu\n", k_log,
-                   (unsigned long long)c.max_prime);
+        if (c.verbose >= 0) {
+            printf("AUTO SET: max_prime (log(K) = ~%.0f): %llu\n", K_log, (unsigned long long)c.max_prime);
+            printf("WATCH for 'Estimated 2x faster (CTRL+C to stop sieving)' warning");
+        }
     }
     // main()'s checks (combined_sieve.cpp:86-135)
     if (!c.save_unknowns && !c.testing) {
