@@ -258,8 +258,7 @@ def run_gb300(args, rank, world, local):
 
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
     torch.cuda.set_device(local)
-    job = dict(WORKLOADS[args.workload])
-    job["mstart"] = job["mstart"] + rank * job["minc"]  # each rank its own block of m
+    job = _rank_job(WORKLOADS[args.workload], rank)
     spec = pgsieve.JobSpec(**job)
     sieve = pgsieve.Sieve(local)
     ext = torch.cuda.ExternalStream(sieve.stream)
@@ -297,10 +296,7 @@ def run_gb300(args, rank, world, local):
     barrier()
     clock_info = clocks.stop()
     total_ms = sum(step_ms)
-    if dist:
-        t = torch.tensor([total_ms], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
+    total_ms = _max_over_ranks(torch, dist, local, total_ms)
 
     stats: dict = {}
     data = prep.fetch(stats)
@@ -328,11 +324,7 @@ def run_gb300(args, rank, world, local):
         out_len = len(view)
         view.close()
     barrier()
-    e2e_total = sum(e2e_s)
-    if dist:
-        t = torch.tensor([e2e_total], dtype=torch.float64, device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_total = float(t.item())
+    e2e_total = _max_over_ranks(torch, dist, local, sum(e2e_s))
     plan = pgsieve.plan(spec)
     h2d = (4 * ((plan["k_bits"] + 31) // 32) + 4 * spec.minc + 4 * (2 * spec.sieve_length + 1)
            + 4 * plan["valid_ms"] + 2 * spec.sieve_length)
@@ -341,7 +333,8 @@ def run_gb300(args, rank, world, local):
            "ms_per_step": e2e_total / args.steps * 1e3}
 
     # roofline of the dominant kernel (large-prime marks): integer-pipe bound.
-    # Algorithmic integer ops per launch from the model in the design doc.
+    # Algorithmic integer ops per launch: 8 per continued-fraction level and
+    # 6 per hit (large_kernel_model_ops).
     s1 = 4 * spec.sieve_length + 2
     n_windows = max(1, stats["prime_limit"] // (1 << 30) - (s1 + 1) // (1 << 30) + 1)
     large_ms = stage_sum.get("large", 0.0) / (args.steps * n_windows)
@@ -405,11 +398,20 @@ def _many_setup(args, rank, world, local):
 
 
 def _max_over_ranks(torch, dist, local, v: float) -> float:
+    """The largest v over the ranks (the slowest rank's time)."""
     if not dist:
         return v
-    t = torch.tensor([v], dtype=torch.float64, device=f"cuda:{local}")
+    dev = f"cuda:{local}" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def _rank_job(job: dict, rank: int) -> dict:
+    """Each rank sieves its own block of m, [mstart + rank*minc, mstart +
+    (rank+1)*minc): rows depend on their m alone, so the blocks need no
+    exchange and the ranks' files concatenate to the whole range's file."""
+    return dict(job, mstart=job["mstart"] + rank * job["minc"])
 
 
 def _cpu_sample_jobs(jobs, threads: int, rows_fraction: float = 0.1) -> dict:

@@ -90,7 +90,7 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     // combined_sieve.cpp:97-103
     if ((uint64_t)SL < 6ull * P || (uint64_t)SL > 22ull * P)
         return err = "sieve_length outside [6P, 22P]", PGS_EINVAL;
-    if (2ull * SL + 1 > 4000000ull) return err = "sieve_length too large for this build", PGS_EINVAL;
+    if (2ull * SL + 1 > 4000000ull) return err = "sieve_length too large (2*SL+1 above 4,000,000)", PGS_EINVAL;
 
     // K = P#/d (gap_common.cpp:116-121); d must divide P#
     {
