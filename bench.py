@@ -703,6 +703,14 @@ def run_prp(args, rank, world, local):
     torch.cuda.synchronize()
     dt = (time.perf_counter() - t) / args.steps
     clock_info = clocks.stop()
+    # the same search over a prepared job's lists in place (no host round trip)
+    with sieve.prepare(pgsieve.JobSpec(**job)) as prep:
+        prep.run(False)
+        prep.prp_gaps(min_merit=PRP_MIN_MERIT, one_side_skip=True)
+        t = time.perf_counter()
+        for _ in range(2):
+            prep.prp_gaps(min_merit=PRP_MIN_MERIT, one_side_skip=True)
+        prepared_ms = (time.perf_counter() - t) / 2 * 1e3
     peak = sieve.int_peak()
     # roofline: Montgomery products of n limbs, 2n^2 32-bit multiply-adds
     # (64-bit results: two IMAD issue slots each) per product, one product per
@@ -728,7 +736,7 @@ def run_prp(args, rank, world, local):
                    "min_merit": PRP_MIN_MERIT, "one_side_skip": True, "bits": bits,
                    "value_is": "lists on the host to gaps on the host"},
         "prp_tests_per_s": counted / args.steps / dt, "prp_launched_per_s": launched / args.steps / dt,
-        "rounds_per_step": rounds / args.steps,
+        "rounds_per_step": rounds / args.steps, "from_prepared_job_ms": prepared_ms,
         "roofline": {"kernel": f"prp_kernel<{n // 8}>", "bound": "int", "achieved": ops / dt, "peak": peak,
                      "unit": "int ops/s", "frac": ops / dt / peak, "traffic": None,
                      "peak_source": "measured live: IMAD microbenchmark (pgs_int_peak)"},

@@ -275,6 +275,12 @@ typedef struct {
  */
 int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *params, const pgs_unknowns *lists,
                  pgs_gap_result *out, pgs_gap_stats *stats);
+/* The same search over the lists of a job after pgs_run, in place on the
+ * device (no host copy of the lists): out has one entry per valid m of the
+ * job, in file order.  The job's own p, d and sieve length are used;
+ * params gives min_merit and one_side_skip. */
+int pgs_prp_gaps_prepared(pgs_ctx *ctx, pgs_prepared *prep, const pgs_gap_params *params,
+                          pgs_gap_result *out, pgs_gap_stats *stats);
 
 /* ---- the reference's number-theory kernels, batched on the device ---- */
 

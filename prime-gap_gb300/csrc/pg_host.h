@@ -236,6 +236,20 @@ namespace pgh {
 
 int fail(pgs_ctx *ctx, cudaError_t e, const char *what);
 
+// A job's unknown lists as one packed device block: m (u64), start (u64),
+// n_prev, n_next (u32) per row, then the distances (u32), as pgs_unknowns.
+struct PackedLists {
+    DevBuf block;
+    uint64_t rows = 0, total = 0;
+    uint64_t *m = nullptr, *start = nullptr;
+    uint32_t *n_prev = nullptr, *n_next = nullptr, *dist = nullptr;
+};
+// Carves pk.block (allocated for rows and max_total distances) into its pieces.
+cudaError_t packed_alloc(PackedLists &pk, uint64_t rows, uint64_t max_total);
+// A sieved job's lists on the device (pg_unknowns.cu); the caller releases
+// pk.block after the stream is done with it.
+int job_lists_device(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, PackedLists &pk);
+
 #define CK(x)                                              \
     do {                                                   \
         cudaError_t e_ = (x);                              \

@@ -647,19 +647,15 @@ int pgs_prp_test(pgs_ctx *ctx, const uint32_t *limbs, uint32_t n_limbs, size_t c
     return PGS_OK;
 }
 
-int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *prm, const pgs_unknowns *lists, pgs_gap_result *out,
-                 pgs_gap_stats *stats) {
-    if (!ctx || !prm || !lists || (lists->rows && !out)) return PGS_EINVAL;
-    if (stats) std::memset(stats, 0, sizeof(*stats));
-    std::lock_guard<std::mutex> g(ctx->mu);
-    CK(cudaSetDevice(ctx->device));
-    const uint64_t rows = lists->rows;
-    if (rows == 0) return PGS_OK;
-    if (rows >= (1ull << 31) || !lists->m || !lists->start || !lists->n_prev || !lists->n_next ||
-        (lists->total && !lists->dist)) {
-        ctx->err = "pgs_prp_gaps: bad lists";
-        return PGS_EINVAL;
-    }
+}  // extern "C"
+
+namespace {
+
+// Device lists of rows (d_m .. d_dist, as pgs_unknowns) and the host copy of
+// their m: the gap search.  The caller holds ctx->mu and checked the lists.
+int prp_gaps_core(pgs_ctx *ctx, const pgs_gap_params *prm, uint64_t rows, const uint64_t *h_m,
+                  const uint64_t *d_m, const uint64_t *d_start, const uint32_t *d_np, const uint32_t *d_nn,
+                  const uint32_t *d_dist, pgs_gap_result *out, pgs_gap_stats *stats) {
     if (prm->p < 2 || !is_prime_u64(prm->p) || prm->d == 0 || prm->sieve_length == 0 ||
         prm->sieve_length >= (1u << 30)) {
         ctx->err = "pgs_prp_gaps: bad p, d or sieve_length";
@@ -671,13 +667,7 @@ int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *prm, const pgs_unknowns *li
         return PGS_EINVAL;
     }
     uint64_t max_m = 0;
-    for (uint64_t r = 0; r < rows; r++) {
-        max_m = std::max(max_m, lists->m[r]);
-        if (lists->m[r] == 0 || lists->start[r] + lists->n_prev[r] + lists->n_next[r] > lists->total) {
-            ctx->err = "pgs_prp_gaps: row outside the distance array";
-            return PGS_EINVAL;
-        }
-    }
+    for (uint64_t r = 0; r < rows; r++) max_m = std::max(max_m, h_m[r]);
     const uint32_t bits = bits_of(k) + (64u - (uint32_t)__builtin_clzll(max_m)) + 1u;
     if (bits > 8u * pg::kMaxL * 32u - 4u) {
         ctx->err = "pgs_prp_gaps: m*K above 4092 bits";
@@ -688,13 +678,11 @@ int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *prm, const pgs_unknowns *li
     std::vector<uint32_t> skip(rows, 0u);
     if (prm->one_side_skip) {
         const double klog = k_log(k);
-        for (uint64_t r = 0; r < rows; r++) skip[r] = skip_threshold(klog, lists->m[r], prm->min_merit);
+        for (uint64_t r = 0; r < rows; r++) skip[r] = skip_threshold(klog, h_m[r], prm->min_merit);
     }
     const cudaStream_t s = ctx->stream;
-    DevBuf d_k, d_kp, d_m, d_start, d_np, d_nn, d_dist, d_skip, d_centers, d_state, d_items, d_res, d_out,
-        d_ctr;
-    DevBuf *bufs[] = {&d_k, &d_kp, &d_m, &d_start, &d_np, &d_nn, &d_dist, &d_skip, &d_centers,
-                      &d_state, &d_items, &d_res, &d_out, &d_ctr};
+    DevBuf d_k, d_kp, d_skip, d_centers, d_state, d_items, d_res, d_out, d_ctr;
+    DevBuf *bufs[] = {&d_k, &d_kp, &d_skip, &d_centers, &d_state, &d_items, &d_res, &d_out, &d_ctr};
     for (DevBuf *b : bufs) b->pool = &ctx->dpool;
     auto cleanup = [&] {
         cudaStreamSynchronize(s);
@@ -703,16 +691,6 @@ int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *prm, const pgs_unknowns *li
     const uint64_t max_items = std::max<uint64_t>(rows, kRoundTarget + kMaxSpec);
     cudaError_t e = upload(d_k, k, s);
     if (e == cudaSuccess) e = upload(d_kp, kprimes, s);
-    auto up = [&](DevBuf &b, const void *src, size_t bytes) {
-        cudaError_t err = b.ensure(bytes);
-        if (err == cudaSuccess && bytes) err = cudaMemcpyAsync(b.p, src, bytes, cudaMemcpyHostToDevice, s);
-        return err;
-    };
-    if (e == cudaSuccess) e = up(d_m, lists->m, rows * 8);
-    if (e == cudaSuccess) e = up(d_start, lists->start, rows * 8);
-    if (e == cudaSuccess) e = up(d_np, lists->n_prev, rows * 4);
-    if (e == cudaSuccess) e = up(d_nn, lists->n_next, rows * 4);
-    if (e == cudaSuccess) e = up(d_dist, lists->dist, lists->total * 4);
     if (e == cudaSuccess) e = upload(d_skip, skip, s);
     if (e == cudaSuccess) e = d_centers.ensure(rows * n * 4ull);
     if (e == cudaSuccess) e = d_state.ensure(rows * sizeof(pg::GapRow));
@@ -724,11 +702,10 @@ int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *prm, const pgs_unknowns *li
         cleanup();
         return fail(ctx, e, "pgs_prp_gaps setup");
     }
-    const pg::GapLists ls{d_start.as<uint64_t>(), d_np.as<uint32_t>(), d_nn.as<uint32_t>(),
-                          d_dist.as<uint32_t>()};
+    const pg::GapLists ls{d_start, d_np, d_nn, d_dist};
     unsigned long long *ctr = d_ctr.as<unsigned long long>();  // items, active, errors
     const unsigned rb = (unsigned)((rows + 255) / 256);
-    pg::centers_kernel<<<rb, 256, 0, s>>>(d_k.as<uint32_t>(), (uint32_t)k.size(), d_m.as<uint64_t>(), rows, n,
+    pg::centers_kernel<<<rb, 256, 0, s>>>(d_k.as<uint32_t>(), (uint32_t)k.size(), d_m, rows, n,
                                           d_centers.as<uint32_t>());
     pg::gap_init_kernel<<<rb, 256, 0, s>>>(d_state.as<pg::GapRow>(), rows, ls, d_skip.as<uint32_t>(),
                                            d_centers.as<uint32_t>(), n, prm->sieve_length,
@@ -779,6 +756,73 @@ int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *prm, const pgs_unknowns *li
         stats->limbs = n;
     }
     return PGS_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pgs_prp_gaps(pgs_ctx *ctx, const pgs_gap_params *prm, const pgs_unknowns *lists, pgs_gap_result *out,
+                 pgs_gap_stats *stats) {
+    if (!ctx || !prm || !lists || (lists->rows && !out)) return PGS_EINVAL;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    const uint64_t rows = lists->rows;
+    if (rows == 0) return PGS_OK;
+    if (rows >= (1ull << 31) || !lists->m || !lists->start || !lists->n_prev || !lists->n_next ||
+        (lists->total && !lists->dist)) {
+        ctx->err = "pgs_prp_gaps: bad lists";
+        return PGS_EINVAL;
+    }
+    for (uint64_t r = 0; r < rows; r++)
+        if (lists->m[r] == 0 || lists->start[r] + lists->n_prev[r] + lists->n_next[r] > lists->total) {
+            ctx->err = "pgs_prp_gaps: row outside the distance array";
+            return PGS_EINVAL;
+        }
+    const cudaStream_t s = ctx->stream;
+    PackedLists pk;
+    pk.block.pool = &ctx->dpool;
+    cudaError_t e = packed_alloc(pk, rows, lists->total);
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        return bytes ? cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s) : cudaSuccess;
+    };
+    if (e == cudaSuccess) e = up(pk.m, lists->m, rows * 8);
+    if (e == cudaSuccess) e = up(pk.start, lists->start, rows * 8);
+    if (e == cudaSuccess) e = up(pk.n_prev, lists->n_prev, rows * 4);
+    if (e == cudaSuccess) e = up(pk.n_next, lists->n_next, rows * 4);
+    if (e == cudaSuccess) e = up(pk.dist, lists->dist, lists->total * 4);
+    int rc = e == cudaSuccess ? prp_gaps_core(ctx, prm, rows, lists->m, pk.m, pk.start, pk.n_prev, pk.n_next,
+                                              pk.dist, out, stats)
+                              : fail(ctx, e, "pgs_prp_gaps upload");
+    cudaStreamSynchronize(s);
+    pk.block.release();
+    return rc;
+}
+
+int pgs_prp_gaps_prepared(pgs_ctx *ctx, pgs_prepared *prep, const pgs_gap_params *prm, pgs_gap_result *out,
+                          pgs_gap_stats *stats) {
+    if (!ctx || !prep || !prm || !out || prep->ctx != ctx || !prep->ran) return PGS_EINVAL;
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    std::lock_guard<std::mutex> g(ctx->mu);
+    CK(cudaSetDevice(ctx->device));
+    const HostJob &h = prep->hj;
+    const uint64_t rows = h.valid_mi.size();
+    if (rows == 0) return PGS_OK;
+    std::vector<uint64_t> m(rows);
+    for (uint64_t r = 0; r < rows; r++) m[r] = h.job.mstart + h.valid_mi[r];
+    pgs_gap_params jp = *prm;  // the job's own p, d and sieve length
+    jp.p = h.job.p;
+    jp.d = h.job.d;
+    jp.sieve_length = h.job.sieve_length;
+    const cudaStream_t s = ctx->stream;
+    PackedLists pk;
+    int rc = job_lists_device(ctx, prep, s, pk);
+    if (rc == PGS_OK)
+        rc = prp_gaps_core(ctx, &jp, rows, m.data(), pk.m, pk.start, pk.n_prev, pk.n_next, pk.dist, out, stats);
+    cudaStreamSynchronize(s);
+    pk.block.release();
+    return rc;
 }
 
 }  // extern "C"

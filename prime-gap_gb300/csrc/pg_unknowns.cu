@@ -299,29 +299,9 @@ using namespace pgh;
 
 namespace {
 
-// The packed output block on the device and its pieces.
-struct Packed {
-    DevBuf block;
-    uint64_t rows = 0;
-    uint64_t *m = nullptr, *start = nullptr;
-    uint32_t *n_prev = nullptr, *n_next = nullptr, *dist = nullptr;
-};
-
-cudaError_t packed_alloc(Packed &pk, uint64_t rows, uint64_t max_total) {
-    pk.rows = rows;
-    cudaError_t e = pk.block.ensure(rows * 24 + max_total * 4 + 64);
-    if (e) return e;
-    char *b = pk.block.as<char>();
-    pk.m = (uint64_t *)b;
-    pk.start = (uint64_t *)(b + rows * 8);
-    pk.n_prev = (uint32_t *)(b + rows * 16);
-    pk.n_next = (uint32_t *)(b + rows * 20);
-    pk.dist = (uint32_t *)(b + rows * 24);
-    return cudaSuccess;
-}
 
 // Copy the packed block to library-owned pinned memory and fill *out.
-int packed_fetch(pgs_ctx *ctx, const Packed &pk, uint64_t total, cudaStream_t s, pgs_unknowns *out) {
+int packed_fetch(pgs_ctx *ctx, const PackedLists &pk, uint64_t total, cudaStream_t s, pgs_unknowns *out) {
     const uint64_t rows = pk.rows;
     const size_t bytes = rows * 24 + total * 4;
     size_t cap = 0;
@@ -347,15 +327,16 @@ int packed_fetch(pgs_ctx *ctx, const Packed &pk, uint64_t total, cudaStream_t s,
     return PGS_OK;
 }
 
-// Parse text already on the device (d_text, len bytes) for the derived job h.
-int parse_device_text(pgs_ctx *ctx, const HostJob &h, const char *d_text, uint64_t len, cudaStream_t s,
-                      pgs_unknowns *out) {
+// Parse text already on the device (d_text, len bytes) for the derived job h
+// into the packed block pk (pk.total set).
+int parse_device_text_packed(pgs_ctx *ctx, const HostJob &h, const char *d_text, uint64_t len, cudaStream_t s,
+                             PackedLists &pk) {
     const uint64_t rows = h.valid_mi.size();
     const uint64_t nchunks = (len + pg::kChunk - 1) / pg::kChunk;
     DevBuf counts, offs, tmp, line_end, body, tot, err, misc, dist_tab;
-    Packed pk;
-    DevBuf *bufs[] = {&counts, &offs, &tmp, &line_end, &body, &tot, &err, &misc, &dist_tab, &pk.block};
+    DevBuf *bufs[] = {&counts, &offs, &tmp, &line_end, &body, &tot, &err, &misc, &dist_tab};
     for (DevBuf *b : bufs) b->pool = &ctx->dpool;
+    pk.block.pool = &ctx->dpool;
     auto cleanup = [&] {
         cudaStreamSynchronize(s);
         for (DevBuf *b : bufs) b->release();
@@ -455,12 +436,83 @@ int parse_device_text(pgs_ctx *ctx, const HostJob &h, const char *d_text, uint64
         ctx->err = "malformed unknowns line " + std::to_string(bad - 1);
         return PGS_EINVAL;
     }
-    const int rc = packed_fetch(ctx, pk, total, s, out);
+    pk.total = total;
     cleanup();
+    return PGS_OK;
+}
+
+int parse_device_text(pgs_ctx *ctx, const HostJob &h, const char *d_text, uint64_t len, cudaStream_t s,
+                      pgs_unknowns *out) {
+    PackedLists pk;
+    int rc = parse_device_text_packed(ctx, h, d_text, len, s, pk);
+    if (rc == PGS_OK) rc = packed_fetch(ctx, pk, pk.total, s, out);
+    cudaStreamSynchronize(s);
+    pk.block.release();
     return rc;
 }
 
 }  // namespace
+
+namespace pgh {
+
+cudaError_t packed_alloc(PackedLists &pk, uint64_t rows, uint64_t max_total) {
+    pk.rows = rows;
+    cudaError_t e = pk.block.ensure(rows * 24 + max_total * 4 + 64);
+    if (e) return e;
+    char *b = pk.block.as<char>();
+    pk.m = (uint64_t *)b;
+    pk.start = (uint64_t *)(b + rows * 8);
+    pk.n_prev = (uint32_t *)(b + rows * 16);
+    pk.n_next = (uint32_t *)(b + rows * 20);
+    pk.dist = (uint32_t *)(b + rows * 24);
+    return cudaSuccess;
+}
+
+// A sieved job's lists as a packed device block (no host copy): the device
+// lists of a plain or RLE job gathered in row order, or a bitcompressed job's
+// device text decoded in place.  pk.total = entries of pk.dist.
+int job_lists_device(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, PackedLists &pk) {
+    const HostJob &h = pr->hj;
+    pk.block.pool = &ctx->dpool;
+    if (h.job.compression == 2) {
+        uint64_t len = 0;
+        CK(cudaMemcpyAsync(&len, pr->misc.p, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        return parse_device_text_packed(ctx, h, pr->text.as<char>(), len, s, pk);
+    }
+    const uint64_t rows = h.valid_mi.size();
+    DevBuf tot, tmp, misc;
+    DevBuf *bufs[] = {&tot, &tmp, &misc};
+    for (DevBuf *b : bufs) b->pool = &ctx->dpool;
+    auto cleanup = [&] {
+        cudaStreamSynchronize(s);
+        for (DevBuf *b : bufs) b->release();
+    };
+    cudaError_t e = packed_alloc(pk, rows, rows * 2ull * h.H);
+    if (e == cudaSuccess) e = tot.ensure(rows * 8 + 8);
+    if (e == cudaSuccess) e = tmp.ensure(pg::scan_tmp_words(rows) * 8 + 8);
+    if (e == cudaSuccess) e = misc.ensure(16);
+    uint64_t total = 0;
+    if (e == cudaSuccess && rows) {
+        const uint32_t *counts = pr->counts.as<uint32_t>();
+        pg::totals_kernel<<<pg::grid(rows, 256), 256, 0, s>>>(counts, rows, tot.as<uint64_t>(), pk.n_prev,
+                                                              pk.n_next);
+        pg::m_kernel<<<pg::grid(rows, 256), 256, 0, s>>>(pr->valid_mi.as<uint32_t>(), rows, h.job.mstart, pk.m);
+        e = pg::scan_u64(tot.as<uint64_t>(), pk.start, misc.as<uint64_t>(), rows, tmp.as<uint64_t>(), s);
+        if (e == cudaSuccess)
+            pg::gather_kernel<<<pg::grid(rows * 32, 256), 256, 0, s>>>(pr->lists.as<uint32_t>(), counts, h.H,
+                                                                       rows, pk.start, pk.dist);
+        if (e == cudaSuccess) e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaMemcpyAsync(&total, misc.p, 8, cudaMemcpyDeviceToHost, s);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    }
+    cleanup();
+    if (e != cudaSuccess) return fail(ctx, e, "job lists");
+    pk.total = total;
+    return PGS_OK;
+}
+
+}  // namespace pgh
 
 extern "C" {
 
@@ -496,47 +548,11 @@ int pgs_fetch_unknowns(pgs_ctx *ctx, pgs_prepared *pr, pgs_unknowns *out) {
     std::lock_guard<std::mutex> g(ctx->mu);
     CK(cudaSetDevice(ctx->device));
     const cudaStream_t s = ctx->stream;
-    const HostJob &h = pr->hj;
-    if (h.job.compression == 2) {
-        // the device holds the bitcompressed text: decode it in place
-        uint64_t len = 0;
-        CK(cudaMemcpyAsync(&len, pr->misc.p, 8, cudaMemcpyDeviceToHost, s));
-        CK(cudaStreamSynchronize(s));
-        return parse_device_text(ctx, h, pr->text.as<char>(), len, s, out);
-    }
-    const uint64_t rows = h.valid_mi.size();
-    Packed pk;
-    DevBuf tot, tmp, misc;
-    DevBuf *bufs[] = {&pk.block, &tot, &tmp, &misc};
-    for (DevBuf *b : bufs) b->pool = &ctx->dpool;
-    auto cleanup = [&] {
-        cudaStreamSynchronize(s);
-        for (DevBuf *b : bufs) b->release();
-    };
-    cudaError_t e = packed_alloc(pk, rows, rows * 2ull * h.H);
-    if (e == cudaSuccess) e = tot.ensure(rows * 8 + 8);
-    if (e == cudaSuccess) e = tmp.ensure(pg::scan_tmp_words(rows) * 8 + 8);
-    if (e == cudaSuccess) e = misc.ensure(16);
-    uint64_t total = 0;
-    if (e == cudaSuccess && rows) {
-        const uint32_t *counts = pr->counts.as<uint32_t>();
-        pg::totals_kernel<<<pg::grid(rows, 256), 256, 0, s>>>(counts, rows, tot.as<uint64_t>(), pk.n_prev,
-                                                              pk.n_next);
-        pg::m_kernel<<<pg::grid(rows, 256), 256, 0, s>>>(pr->valid_mi.as<uint32_t>(), rows, h.job.mstart, pk.m);
-        e = pg::scan_u64(tot.as<uint64_t>(), pk.start, misc.as<uint64_t>(), rows, tmp.as<uint64_t>(), s);
-        if (e == cudaSuccess)
-            pg::gather_kernel<<<pg::grid(rows * 32, 256), 256, 0, s>>>(pr->lists.as<uint32_t>(), counts, h.H,
-                                                                       rows, pk.start, pk.dist);
-        if (e == cudaSuccess) e = cudaGetLastError();
-        if (e == cudaSuccess) e = cudaMemcpyAsync(&total, misc.p, 8, cudaMemcpyDeviceToHost, s);
-        if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    }
-    if (e != cudaSuccess) {
-        cleanup();
-        return fail(ctx, e, "fetch unknowns");
-    }
-    const int rc = packed_fetch(ctx, pk, total, s, out);
-    cleanup();
+    PackedLists pk;
+    int rc = job_lists_device(ctx, pr, s, pk);
+    if (rc == PGS_OK) rc = packed_fetch(ctx, pk, pk.total, s, out);
+    cudaStreamSynchronize(s);
+    pk.block.release();
     return rc;
 }
 

@@ -202,6 +202,8 @@ _SIGNATURES = {
                                     ctypes.c_size_t, ctypes.c_int, ctypes.POINTER(ctypes.c_uint8)]),
     "pgs_prp_gaps": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(GapParams), ctypes.POINTER(Unknowns),
                                     ctypes.POINTER(GapResult), ctypes.POINTER(GapStats)]),
+    "pgs_prp_gaps_prepared": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.POINTER(GapParams),
+                                             ctypes.POINTER(GapResult), ctypes.POINTER(GapStats)]),
     "pgs_table_reserve": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint64]),
     "pgs_batch_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_int, ctypes.c_int,
                                          ctypes.POINTER(ctypes.c_void_p)]),
@@ -329,7 +331,7 @@ class Sieve:
     def prepare(self, job: JobSpec) -> "Prepared":
         h = ctypes.c_void_p()
         self._check(self.lib.pgs_prepare(self.h, ctypes.byref(job.c()), ctypes.byref(h)))
-        return Prepared(self, h)
+        return Prepared(self, h, job)
 
     def reserve_table(self, limit: int) -> None:
         """Generate (once) the resident prime table up to ``limit``."""
@@ -475,8 +477,8 @@ class ResultView:
 class Prepared:
     """A job whose tables are resident on the device (pgs_prepare)."""
 
-    def __init__(self, sieve: Sieve, h: ctypes.c_void_p):
-        self.sieve, self.h = sieve, h
+    def __init__(self, sieve: Sieve, h: ctypes.c_void_p, spec: JobSpec | None = None):
+        self.sieve, self.h, self.spec = sieve, h, spec
 
     def run(self, record_stages: bool = True) -> None:
         self.sieve._check(self.sieve.lib.pgs_run(self.sieve.h, self.h, int(record_stages)))
@@ -497,6 +499,19 @@ class Prepared:
         finally:
             self.sieve.lib.pgs_result_free(ctypes.byref(res))
         return data
+
+    def prp_gaps(self, min_merit: float = 18.0, one_side_skip: bool = False):
+        """The gap search over this job's lists in place on the device
+        (pgs_prp_gaps_prepared): [(prev_p, next_p, p_tests, n_tests, flags)]
+        per valid m and the search stats."""
+        n = plan(self.spec)["valid_ms"]
+        out = (GapResult * max(1, n))()
+        st = GapStats()
+        prm = GapParams(0, 0, 0, min_merit, int(one_side_skip))
+        self.sieve._check(self.sieve.lib.pgs_prp_gaps_prepared(self.sieve.h, self.h, ctypes.byref(prm), out,
+                                                                ctypes.byref(st)))
+        return [(r.prev_p, r.next_p, r.p_tests, r.n_tests, r.flags) for r in out[:n]], \
+            {"rounds": st.rounds, "prp_tests": st.prp_tests, "limbs": st.limbs}
 
     def unknowns(self) -> dict:
         """Per-m unknown lists of the last run, straight from the device."""

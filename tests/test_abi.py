@@ -18,7 +18,7 @@ SYMBOLS = [
     "pgs_version", "pgs_table_reserve", "pgs_batch_prepare", "pgs_batch_run", "pgs_batch_fetch",
     "pgs_batch_free", "pgs_method2_batch", "pgs_server_start", "pgs_server_submit", "pgs_server_wait",
     "pgs_server_stats_get", "pgs_server_stop", "pgs_large_hits_static", "pgs_fetch_unknowns",
-    "pgs_parse_unknowns", "pgs_unknowns_free", "pgs_prp_test", "pgs_prp_gaps",
+    "pgs_parse_unknowns", "pgs_unknowns_free", "pgs_prp_test", "pgs_prp_gaps", "pgs_prp_gaps_prepared",
 ]
 
 

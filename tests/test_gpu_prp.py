@@ -87,6 +87,21 @@ def test_prp_gaps_match_reference_gap_test(sieve, name):
     assert stats["prp_tests"] >= g["prp_tests"] and stats["rounds"] > 0
 
 
+@pytest.mark.parametrize("name", sorted(GAPS))
+def test_prp_gaps_on_prepared_job_in_place(sieve, name):
+    """pgs_prp_gaps_prepared: the same gaps from the job's device lists,
+    without the lists leaving the device."""
+    g = GAPS[name]
+    job = pgsieve.JobSpec(g["p"], g["d"], g["mstart"], g["minc"], g["sieve_length"], g["max_prime"],
+                          g["compression"])
+    with sieve.prepare(job) as prep:
+        prep.run(False)
+        res, _ = prep.prp_gaps()
+        m = prep.unknowns()["m"]
+    assert [[int(m[i]), r[0], r[1]] for i, r in enumerate(res)] == g["gaps"]
+    assert sum(r[2] + r[3] for r in res) == g["prp_tests"]
+
+
 def test_prp_gaps_one_side_skip_matches_oracle(sieve):
     g = GAPS["small_bc_d30"]
     lists = _lists(sieve, g)
