@@ -36,6 +36,7 @@ CU_SOURCES = ["pg_primes.cu", "pg_kmod.cu", "pg_large.cu", "pg_rows.cu", "pg_too
 
 LIB = BUILD / "libpgsieve.so"
 CLI = BUILD / "combined_sieve"
+GAP_TEST_CLI = BUILD / "gap_test"
 ORACLE_LIB = ORACLE_BUILD / "libm2oracle.so"
 ORACLE_BIN = ORACLE_BUILD / "m2_oracle"
 ARITH_HOST_LIB = BUILD / "libpgarith_host.so"
@@ -77,10 +78,10 @@ def build_lib(jobs: int = 8, verbose: bool = False) -> Path:
             fut.result()
     if _stale(LIB, objs):
         _run([NVCC, *ARCH, "-shared", "-o", str(LIB), *map(str, objs), "-cudart", "static"])
-    cli_src = HOST / "combined_sieve.cpp"
-    if cli_src.exists() and _stale(CLI, [cli_src, LIB] + hdrs):
-        _run(["g++", "-O2", "-std=c++17", "-Wall", f"-I{INCLUDE}", str(cli_src), "-o", str(CLI),
-              f"-L{BUILD}", "-lpgsieve", "-Wl,-rpath,$ORIGIN", "-ldl"])
+    for src, out in ((HOST / "combined_sieve.cpp", CLI), (HOST / "gap_test.cpp", GAP_TEST_CLI)):
+        if src.exists() and _stale(out, [src, HOST / "cli_common.h", LIB] + hdrs):
+            _run(["g++", "-O2", "-std=c++17", "-Wall", f"-I{INCLUDE}", str(src), "-o", str(out),
+                  f"-L{BUILD}", "-lpgsieve", "-Wl,-rpath,$ORIGIN", "-ldl"])
     return LIB
 
 
