@@ -105,6 +105,16 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(sm)}
 
 
+def _hbm_peak() -> tuple[float, str]:
+    """Measured HBM copy bandwidth (GB/s) of the GB300s, or the
+    fallback figure when the measurement file is absent."""
+    f = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(f.read_text())["hbm_gbs"]), "of measured (MEASURED_PEAKS.json hbm_gbs, copy)"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "of fallback (6.8 TB/s)"
+
+
 def _traffic_per_launch() -> float | None:
     if not PROFILE_TRAFFIC.exists():
         return None
@@ -341,11 +351,21 @@ def run_gb300(args, rank, world, local):
     model_ops = large_kernel_model_ops(spec, stats, plan) / n_windows
     achieved = model_ops / (large_ms * 1e-3) if large_ms else None
     traffic = _traffic_per_launch()
-    roofline = {"kernel": "large_kernel<uint32_t>", "bound": "int", "achieved": achieved,
-                "peak": imad_peak, "unit": "int ops/s",
-                "frac": achieved / imad_peak if achieved else None, "traffic": traffic,
-                "peak_source": "measured live: IMAD microbenchmark (pgs_int_peak)",
-                "avg_launch_ms": large_ms}
+    roofline_int = {"kernel": "large_kernel<uint32_t>", "bound": "int", "achieved": achieved,
+                    "peak": imad_peak, "unit": "int ops/s",
+                    "frac": achieved / imad_peak if achieved else None, "traffic": traffic,
+                    "peak_source": "measured live: IMAD microbenchmark (pgs_int_peak)",
+                    "avg_launch_ms": large_ms}
+    # the same kernel against HBM: its algorithmic bytes are the streamed
+    # inputs, 12 B per prime (offset, walk step, start residue; the bitset of
+    # hits stays in L2), against the measured copy bandwidth
+    hbm_peak, hbm_src = _hbm_peak()
+    alg_bytes = 12.0 * stats["primes"] / n_windows
+    hbm_gbs = alg_bytes / (large_ms * 1e-3) / 1e9 if large_ms else None
+    roofline = {"kernel": "large_kernel<uint32_t>", "bound": "hbm", "achieved": hbm_gbs, "peak": hbm_peak,
+                "unit": "GB/s", "frac": hbm_gbs / hbm_peak if hbm_gbs else None, "traffic": traffic,
+                "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_ms": large_ms, "peak_source": hbm_src,
+                "note": "integer-issue bound, not memory bound: see roofline_int"}
 
     if rank != 0:
         return 0
@@ -363,7 +383,8 @@ def run_gb300(args, rank, world, local):
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}"},
         "primes_per_s": primes_per_s, "bit_exact": bit_exact, "output_md5": md5,
         "stage_ms_per_step": {k: v / args.steps for k, v in stage_sum.items()},
-        "e2e": e2e, "roofline": roofline, "cpu_baseline": cpu, "clocks": clock_info,
+        "e2e": e2e, "roofline": roofline, "roofline_int": roofline_int, "cpu_baseline": cpu,
+        "clocks": clock_info,
         "gpu_launches": int(stats["launches"]) * args.steps,
     }
     print(json.dumps(line), flush=True)
