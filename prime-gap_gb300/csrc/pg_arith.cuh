@@ -55,8 +55,8 @@ PG_HD uint64_t mulmod_u64(uint64_t a, uint64_t b, uint64_t p, double inv_p) {
 
 // -p^{-1} mod 2^32 for odd p (Newton iteration on the 2-adic inverse).
 PG_HD uint32_t neg_inv32(uint32_t p) {
-    uint32_t x = p;  // correct to 3 bits
-    for (int i = 0; i < 4; i++) x *= 2u - p * x;
+    uint32_t x = (3u * p) ^ 2u;  // correct to 5 bits
+    for (int i = 0; i < 3; i++) x *= 2u - p * x;
     return 0u - x;
 }
 
@@ -75,11 +75,22 @@ PG_HD uint32_t redc32_lazy(uint64_t t, uint32_t p, uint32_t pinv) {
     return (uint32_t)((t + (uint64_t)m * p) >> 32);
 }
 
+PG_HD uint32_t umulhi32(uint32_t a, uint32_t b) {
+#if defined(__CUDA_ARCH__)
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
 PG_HD uint32_t redc32(uint64_t t, uint32_t p, uint32_t pinv) {
-    uint64_t m = (uint32_t)((uint32_t)t * pinv);
-    uint64_t s = m * p;
-    uint64_t hi = (t >> 32) + (s >> 32) + ((uint32_t)t != 0u);
-    return (uint32_t)(hi >= p ? hi - p : hi);
+    const uint32_t lo = (uint32_t)t, hi = (uint32_t)(t >> 32);
+    const uint32_t m = lo * pinv;
+    // hi < p and hi(m*p) < p, so the true sum is below 2p < 2^33: at most
+    // one wrap, which shows as s < a
+    const uint32_t a = hi + (lo != 0u);
+    const uint32_t s = a + umulhi32(m, p);
+    return (s < a || s >= p) ? s - p : s;
 }
 
 // R^2 mod p (R = 2^32) from r1 = R mod p without a 64-bit division: x = 2^33
@@ -162,6 +173,13 @@ PG_HD void kmod32_multi(const uint32_t *limbs, int n, const uint32_t *p, uint32_
 // (r * M + sl) mod p with the Montgomery constants of p (M < 3 * 2^32, sl < p).
 PG_HD uint32_t start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p, uint32_t pinv,
                        uint32_t r2) {
+    if ((M >> 32) == 0) {
+        // M * r2 < 2^32 p: REDC(M r2) = M R mod p, and REDC(r M R) = r M mod p
+        const uint32_t mr = redc32(M * r2, p, pinv);
+        const uint32_t rm = redc32((uint64_t)r * mr, p, pinv);
+        const uint64_t t = (uint64_t)rm + sl;
+        return (uint32_t)(t >= p ? t - p : t);
+    }
     uint32_t a = redc32(M, p, pinv);                  // M R^-1
     uint32_t mm = redc32((uint64_t)a * r2, p, pinv);  // M mod p
     uint32_t b = redc32((uint64_t)r * mm, p, pinv);   // r M R^-1
@@ -175,7 +193,8 @@ PG_HD uint32_t start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p, uint32_t
 // W = K * R^-n after n limbs (each step multiplies what came before by R^-1),
 // and REDC(W * R^(n+1)) = K mod p.  A step is one add and one REDC (two
 // multiplies) instead of the most-significant-first step's three; R^(n+1) mod p
-// costs ~log2(n) Montgomery squarings per prime, shared work for long K.
+// costs log2(n) Montgomery squarings and popcount(n) - 1 products per prime,
+// outweighed by the cheaper steps for long K.
 
 // (W + l) * 2^-32 mod p, result <= p + 1, for W <= p + 1, p < 2^32 - 4.
 // x + m*p <= (p + 2^32) + (2^32 - 1)p = 2^32 (p + 1) < 2^64: one multiply-add.
@@ -185,29 +204,16 @@ PG_HD uint32_t redc32_add(uint32_t W, uint32_t l, uint32_t p, uint32_t pinv) {
     return (uint32_t)((x + (uint64_t)m * p) >> 32);
 }
 
-// R^(e+1) mod p (R = 2^32): Montgomery power of R (whose Montgomery form is
-// r2 = R^2 mod p), starting from the Montgomery form of 1 (r1 = R mod p).
-PG_HD uint32_t mont_rpow32(uint32_t e, uint32_t p, uint32_t pinv, uint32_t r1, uint32_t r2) {
-    uint32_t acc = r1, b = r2;
-    while (e) {
-        if (e & 1u) acc = redc32((uint64_t)acc * b, p, pinv);
-        e >>= 1;
-        if (e) b = redc32((uint64_t)b * b, p, pinv);
-    }
-    return acc;
-}
-
-// NP primes (odd, 3 <= p < 2^32 - 4) at once, least significant limb first.
-// Also returns pinv and r2 = 2^64 mod p of each prime.
+// NP primes (odd, 3 <= p < 2^32 - 4) at once, least significant limb first
+// (n >= 1 limbs).  Also returns pinv and r2 = 2^64 mod p of each prime.
 template <int NP>
 PG_HD void kmod32_lsb_multi(const uint32_t *limbs, int n, const uint32_t *p, uint32_t *r,
                             uint32_t *pinv, uint32_t *r2) {
-    uint32_t W[NP], r1[NP];
+    uint32_t W[NP];
 #pragma unroll
     for (int k = 0; k < NP; k++) {
         pinv[k] = neg_inv32(p[k]);
-        r1[k] = (0u - p[k]) % p[k];
-        r2[k] = r2_from_r1(r1[k], p[k], pinv[k]);
+        r2[k] = r2_from_r1((0u - p[k]) % p[k], p[k], pinv[k]);
         W[k] = 0;
     }
     for (int i = 0; i < n; i++) {
@@ -215,11 +221,25 @@ PG_HD void kmod32_lsb_multi(const uint32_t *limbs, int n, const uint32_t *p, uin
 #pragma unroll
         for (int k = 0; k < NP; k++) W[k] = redc32_add(W[k], l, p[k], pinv[k]);
     }
+    // R^(n+1) mod p from r2 = R^2: with x = R^(f+1), a Montgomery square
+    // gives R^(2f+1) and a product with r2 gives R^(f+2); the bits of n
+    // after the leading one double f and add one (f = 1 to f = n)
+    uint32_t X[NP];
 #pragma unroll
-    for (int k = 0; k < NP; k++) {
-        const uint32_t X = mont_rpow32((uint32_t)n, p[k], pinv[k], r1[k], r2[k]);
-        r[k] = redc32((uint64_t)W[k] * X, p[k], pinv[k]);  // W * X < (p + 2) * p < p * 2^32
+    for (int k = 0; k < NP; k++) X[k] = r2[k];
+    int top = 31;
+    while (top > 0 && !(((uint32_t)n >> top) & 1u)) top--;
+    for (int b = top - 1; b >= 0; b--) {
+        const bool one = ((uint32_t)n >> b) & 1u;
+#pragma unroll
+        for (int k = 0; k < NP; k++) {
+            X[k] = redc32((uint64_t)X[k] * X[k], p[k], pinv[k]);
+            if (one) X[k] = redc32((uint64_t)X[k] * r2[k], p[k], pinv[k]);
+        }
     }
+#pragma unroll
+    for (int k = 0; k < NP; k++)
+        r[k] = redc32((uint64_t)W[k] * X[k], p[k], pinv[k]);  // W * X < (p + 2) * p < p * 2^32
 }
 
 // Odd primes 2^31 <= p < 2^46 (and any odd p >= 3 below that): R = 2^64.
@@ -513,9 +533,10 @@ PG_HD uint64_t half_mod(uint64_t r, uint64_t p) { return (r & 1u) ? ((r + p) >> 
 // step' = r/2 and c = c_add (+ (p+1)/2 when d is odd).  r2 = 2^64 mod p
 // (32-bit primes only; it comes with K mod p).
 // kmul != 1: r is K' mod p for K = K' * kmul; K mod p = REDC(REDC(r * kmul) * r2).
+// pinv: -p^-1 mod 2^32 when the caller has it, else 0 (computed here).
 PG_HD void walk_start(const WalkParams &wk, uint32_t p, uint32_t r, uint32_t r2, uint32_t &step,
-                      uint32_t &t0, uint32_t kmul = 1) {
-    const uint32_t pinv = neg_inv32(p);
+                      uint32_t &t0, uint32_t kmul = 1, uint32_t pinv = 0) {
+    if (pinv == 0) pinv = neg_inv32(p);
     if (kmul != 1) r = redc32((uint64_t)redc32((uint64_t)r * kmul, p, pinv) * r2, p, pinv);
     const uint32_t rh = half_mod(r, p);
     const uint32_t c = wk.c_add + (wk.odd_d ? (p >> 1) + 1 : 0u);

@@ -60,7 +60,7 @@ __global__ void __launch_bounds__(kKmodThreads)
             for (int k = 0; k < kPrimesPerThread; k++) {
                 if (idx0 + k >= n) break;
                 uint32_t a = r[k], b = r2[k];
-                if (with_walk) walk_start(walk, p[k], r[k], r2[k], a, b);
+                if (with_walk) walk_start(walk, p[k], r[k], r2[k], a, b, 1, pinv[k]);
                 ((uint32_t *)a_out)[idx0 + k] = a;
                 if (b_out) ((uint32_t *)b_out)[idx0 + k] = b;
             }

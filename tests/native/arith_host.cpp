@@ -252,4 +252,8 @@ uint32_t ah_start32(uint32_t r, uint64_t M, uint32_t sl, uint32_t p) {
 }
 
 uint64_t ah_mulmod(uint64_t a, uint64_t b, uint64_t p) { return pg::mulmod_u64(a, b, p, 1.0 / (double)p); }
+
+// Montgomery reduction (R = 2^32) and -p^-1 mod 2^32 of the K mod p kernel.
+uint32_t ah_redc32(uint64_t t, uint32_t p) { return pg::redc32(t, p, pg::neg_inv32(p)); }
+uint32_t ah_neg_inv32(uint32_t p) { return pg::neg_inv32(p); }
 }

@@ -338,6 +338,25 @@ def test_start32(ah):
         assert ah.ah_start32(r, M, sl, p) == (r * M + sl) % p
 
 
+def test_redc32_and_inverse(ah):
+    """REDC for R = 2^32 over the whole 32-bit prime range, including the
+    largest moduli, where the reduced sum passes 2^32 before its one
+    subtraction, and inputs up to p * 2^32 - 1."""
+    ah.ah_redc32.restype = ctypes.c_uint32
+    ah.ah_redc32.argtypes = [ctypes.c_uint64, ctypes.c_uint32]
+    ah.ah_neg_inv32.restype = ctypes.c_uint32
+    ah.ah_neg_inv32.argtypes = [ctypes.c_uint32]
+    rng = random.Random(41)
+    moduli = [3, 5, 7, 65537, 2**31 - 1, 2**31 + 11, 2**32 - 5, 2**32 - 17]
+    moduli += [rng.randrange(3, 2**32 - 4) | 1 for _ in range(300)]
+    for p in moduli:
+        assert (p * ah.ah_neg_inv32(p)) % 2**32 == 2**32 - 1
+        rinv = pow(2**32, -1, p)
+        tops = [p * 2**32 - 1, p * 2**32 - 2**32, (p - 1) * 2**32 + 1, 0, 1]
+        for t in tops + [rng.randrange(0, p * 2**32) for _ in range(40)]:
+            assert ah.ah_redc32(t, p) == t * rinv % p, (t, p)
+
+
 def test_walk_start(ah):
     """Step and start residue of the parity-reduced walk (32- and 64-bit)."""
     ah.ah_walk_start.restype = None
