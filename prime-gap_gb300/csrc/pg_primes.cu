@@ -23,10 +23,17 @@ namespace {
 
 constexpr int kSieveThreads = 512;
 constexpr uint32_t kSegWords = kSegBits / 32;
-__constant__ uint32_t c_tiny[17] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61};
+constexpr int kTinyCount = 17;
+
+// The odd primes below 64, as compile-time constants (the loops over them
+// are unrolled, so every division by one becomes a multiply and shift).
+__host__ __device__ constexpr uint32_t tiny_q(int t) {
+    constexpr uint32_t q[kTinyCount] = {3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37, 41, 43, 47, 53, 59, 61};
+    return q[t];
+}
 
 // bits at multiples of q inside a 32-bit word (q >= 32 -> bit 0 only)
-__device__ __forceinline__ uint32_t tiny_pattern(uint32_t q) {
+__host__ __device__ constexpr uint32_t tiny_pattern(uint32_t q) {
     uint32_t m = 0;
     for (uint32_t b = 0; b < 32; b += q) m |= 1u << b;
     return m;
@@ -44,41 +51,62 @@ __device__ uint32_t base_bound(const uint32_t *base, uint32_t nbase, uint64_t hi
     return lo;
 }
 
+// Bit index (odd numbers from seg_lo, odd) of the first odd multiple of q at
+// or above max(q^2, seg_lo), for q^2 <= seg_hi: below 2q + 2^18, so 32 bits.
+// With rem = seg_lo mod q and d = (q - rem) mod q, seg_lo + d is the first
+// multiple, odd iff d is even (seg_lo odd); else the next odd one is q on.
+// Segments below 2^32 take a 32-bit remainder.
+__device__ __forceinline__ uint32_t first_index(uint32_t q, uint64_t seg_lo, bool lo32) {
+    const uint64_t sq = (uint64_t)q * q;
+    if (sq >= seg_lo) return (uint32_t)((sq - seg_lo) >> 1);
+    const uint32_t rem = lo32 ? (uint32_t)seg_lo % q : (uint32_t)(seg_lo % q);
+    const uint32_t d = rem == 0 ? 0u : q - rem;
+    return (d & 1u) ? (d + q) >> 1 : d >> 1;
+}
+
 // Marks composites of the segment [seg_lo, seg_hi] (seg_lo odd) in `bits`.
-// Primes themselves stay clear; 1 is marked.
+// Primes themselves stay clear; 1 is marked.  Blocks of kSieveThreads.
 __device__ void sieve_segment(uint32_t *bits, uint64_t seg_lo, uint64_t seg_hi,
                               const uint32_t *base, uint32_t nbase) {
     const uint32_t nbits = (uint32_t)((seg_hi - seg_lo) / 2 + 1);
     __shared__ uint32_t s_nq;
-    __shared__ uint32_t s_j0[17];
     if (threadIdx.x == 0) s_nq = base_bound(base, nbase, seg_hi);
-    if (threadIdx.x < 17) {
-        uint32_t q = c_tiny[threadIdx.x];
-        // index j with seg_lo + 2j == 0 (mod q): j = -seg_lo * (q+1)/2 mod q
-        uint32_t lm = (uint32_t)(seg_lo % q);
-        uint32_t neg = (q - lm) % q;
-        s_j0[threadIdx.x] = (uint32_t)((neg * ((q + 1) / 2)) % q);
-    }
-    __syncthreads();
 
-    // tiny primes: per-word patterns; this also initialises every word
-    for (uint32_t w = threadIdx.x; w < kSegWords; w += blockDim.x) {
+    // tiny primes: per-word patterns; this also initialises every word.
+    // Word w holds indices 32w + b; q divides seg_lo + 2(32w + b) for
+    // b = o (mod q), o = j0 - 32w mod q with j0 = -seg_lo (q+1)/2 mod q.
+    // Each thread's words are kSieveThreads apart, so o drops by a constant.
+    uint32_t o[kTinyCount];
+#pragma unroll
+    for (int t = 0; t < kTinyCount; t++) {
+        const uint32_t q = tiny_q(t);
+        const uint32_t neg = (q - (uint32_t)(seg_lo % q)) % q;
+        const uint32_t j0 = neg * ((q + 1) / 2) % q;
+        o[t] = (j0 + q - (32u * threadIdx.x) % q) % q;
+    }
+    constexpr uint32_t wstep = 32u * kSieveThreads;
+    for (uint32_t w = threadIdx.x; w < kSegWords; w += kSieveThreads) {
         uint32_t word = 0;
 #pragma unroll
-        for (int t = 0; t < 17; t++) {
-            uint32_t q = c_tiny[t];
-            uint32_t o = (s_j0[t] + q - (32u * w) % q) % q;
-            if (o < 32) word |= tiny_pattern(q) << o;
+        for (int t = 0; t < kTinyCount; t++) {
+            const uint32_t q = tiny_q(t);
+            if (q < 32) word |= tiny_pattern(q) << o[t];
+            else if (o[t] < 32) word |= 1u << o[t];
+            const uint32_t d = wstep % q;
+            o[t] = o[t] >= d ? o[t] - d : o[t] + q - d;
         }
         bits[w] = word;
     }
     __syncthreads();
-    if (threadIdx.x < 17) {
+    if (threadIdx.x == 0 && seg_lo <= tiny_q(kTinyCount - 1)) {
         // the tiny primes themselves are prime
-        uint64_t q = c_tiny[threadIdx.x];
-        if (q >= seg_lo && q <= seg_hi) {
-            uint32_t j = (uint32_t)((q - seg_lo) / 2);
-            atomicAnd(&bits[j >> 5], ~(1u << (j & 31)));
+#pragma unroll
+        for (int t = 0; t < kTinyCount; t++) {
+            const uint64_t q = tiny_q(t);
+            if (q >= seg_lo && q <= seg_hi) {
+                const uint32_t j = (uint32_t)((q - seg_lo) / 2);
+                bits[j >> 5] &= ~(1u << (j & 31));
+            }
         }
     }
     if (threadIdx.x == 0 && seg_lo == 1) atomicOr(&bits[0], 1u);  // 1 is not prime
@@ -89,17 +117,12 @@ __device__ void sieve_segment(uint32_t *bits, uint64_t seg_lo, uint64_t seg_hi,
     // first prime >= 64 is 17, since 3..61 are the 17 odd primes below 64)
     const uint32_t first_mid = 17;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    const bool lo32 = seg_hi <= 0xFFFFFFFFull;
     // medium primes: one warp per prime
     for (uint32_t i = first_mid + warp; i < nq; i += nwarps) {
-        uint64_t q = base[i];
+        const uint32_t q = base[i];
         if (q >= 2048) break;
-        uint64_t start = q * q;
-        if (start < seg_lo) {
-            start = (seg_lo + q - 1) / q * q;
-            if ((start & 1) == 0) start += q;
-        }
-        if (start > seg_hi) continue;
-        for (uint64_t j = (start - seg_lo) / 2 + (uint64_t)lane * q; j < nbits; j += 32 * q)
+        for (uint32_t j = first_index(q, seg_lo, lo32) + lane * q; j < nbits; j += 32 * q)
             atomicOr(&bits[j >> 5], 1u << (j & 31));
     }
     // large primes: one thread per prime
@@ -115,25 +138,24 @@ __device__ void sieve_segment(uint32_t *bits, uint64_t seg_lo, uint64_t seg_hi,
         first_large = lo;
     }
     for (uint32_t i = first_large + threadIdx.x; i < nq; i += blockDim.x) {
-        uint64_t q = base[i];
-        uint64_t start = q * q;
-        if (start < seg_lo) {
-            start = (seg_lo + q - 1) / q * q;
-            if ((start & 1) == 0) start += q;
-        }
-        for (uint64_t j = (start - seg_lo) / 2; j < nbits; j += q)
+        const uint32_t q = base[i];
+        for (uint32_t j = first_index(q, seg_lo, lo32); j < nbits; j += q)
             atomicOr(&bits[j >> 5], 1u << (j & 31));
     }
     __syncthreads();
 }
 
-// Unordered compaction of a window's primes (offsets from win_lo).
+// Unordered compaction of a window's primes (offsets from win_lo).  Each
+// warp owns kSegWords / 16 consecutive words and writes their primes in
+// rounds of 32 words, one word per lane: a round's primes are contiguous in
+// the output, so its stores touch a few cache lines rather than one per lane.
 __global__ void __launch_bounds__(kSieveThreads)
     sieve_window_kernel(uint64_t win_lo, uint64_t win_hi, uint64_t first_odd, const uint32_t *base,
                         uint32_t nbase, uint32_t *out, uint64_t cap,
                         unsigned long long *count) {
+    constexpr uint32_t kWarps = kSieveThreads / 32, kWarpWords = kSegWords / kWarps;
     __shared__ uint32_t bits[kSegWords];
-    __shared__ uint32_t s_scan[kSieveThreads];
+    __shared__ uint32_t s_warp[kWarps];
     __shared__ unsigned long long s_base;
     const uint64_t seg_lo = first_odd + (uint64_t)blockIdx.x * kSegSpan;
     if (seg_lo > win_hi) return;
@@ -142,42 +164,49 @@ __global__ void __launch_bounds__(kSieveThreads)
     sieve_segment(bits, seg_lo, seg_hi, base, nbase);
 
     const uint32_t nbits = (uint32_t)((seg_hi - seg_lo) / 2 + 1);
-    // each thread owns a contiguous range of words
-    const uint32_t per = kSegWords / kSieveThreads;
-    const uint32_t w0 = threadIdx.x * per;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t wbeg = warp * kWarpWords;
+    // primes (clear bits below nbits) of word w
+    auto primes_of = [&](uint32_t w) -> uint32_t {
+        const uint32_t b0 = w * 32;
+        if (b0 >= nbits) return 0u;
+        const uint32_t valid = (nbits - b0 >= 32) ? 0xFFFFFFFFu : ((1u << (nbits - b0)) - 1);
+        return ~bits[w] & valid;
+    };
     uint32_t cnt = 0;
-    for (uint32_t w = w0; w < w0 + per; w++) {
-        uint32_t valid = 0;
-        uint32_t b0 = w * 32;
-        if (b0 < nbits) valid = (nbits - b0 >= 32) ? 0xFFFFFFFFu : ((1u << (nbits - b0)) - 1);
-        // exclude values below the window start (first segment of a window at 1)
-        uint32_t primes = ~bits[w] & valid;
-        cnt += __popc(primes);
-    }
-    s_scan[threadIdx.x] = cnt;
+    for (uint32_t w = wbeg + lane; w < wbeg + kWarpWords; w += 32) cnt += __popc(primes_of(w));
+    cnt = __reduce_add_sync(0xFFFFFFFFu, cnt);
+    if (lane == 0) s_warp[warp] = cnt;
     __syncthreads();
-    // block exclusive scan (Hillis-Steele on 512 entries)
-    for (int off = 1; off < kSieveThreads; off <<= 1) {
-        uint32_t v = threadIdx.x >= (uint32_t)off ? s_scan[threadIdx.x - off] : 0;
-        __syncthreads();
-        s_scan[threadIdx.x] += v;
-        __syncthreads();
-    }
-    if (threadIdx.x == kSieveThreads - 1) s_base = atomicAdd(count, (unsigned long long)s_scan[kSieveThreads - 1]);
-    __syncthreads();
-    uint64_t pos = s_base + s_scan[threadIdx.x] - cnt;
-    for (uint32_t w = w0; w < w0 + per; w++) {
-        uint32_t b0 = w * 32;
-        if (b0 >= nbits) break;
-        uint32_t valid = (nbits - b0 >= 32) ? 0xFFFFFFFFu : ((1u << (nbits - b0)) - 1);
-        uint32_t primes = ~bits[w] & valid;
-        while (primes) {
-            uint32_t b = __ffs(primes) - 1;
-            primes &= primes - 1;
-            uint64_t v = seg_lo + 2ull * (b0 + b);
-            if (pos < cap) out[pos] = (uint32_t)(v - win_lo);
-            pos++;
+    if (threadIdx.x == 0) {
+        uint32_t total = 0;
+        for (uint32_t k = 0; k < kWarps; k++) {
+            const uint32_t c = s_warp[k];
+            s_warp[k] = total;
+            total += c;
         }
+        s_base = atomicAdd(count, (unsigned long long)total);
+    }
+    __syncthreads();
+    uint64_t pos = s_base + s_warp[warp];
+    for (uint32_t w = wbeg + lane; w < wbeg + kWarpWords; w += 32) {
+        uint32_t primes = primes_of(w);
+        const uint32_t c = __popc(primes);
+        uint32_t incl = c;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+            if (lane >= (uint32_t)o) incl += v;
+        }
+        uint64_t at = pos + incl - c;
+        while (primes) {
+            const uint32_t b = __ffs(primes) - 1;
+            primes &= primes - 1;
+            const uint64_t v = seg_lo + 2ull * (w * 32 + b);
+            if (at < cap) out[at] = (uint32_t)(v - win_lo);
+            at++;
+        }
+        pos += __shfl_sync(0xFFFFFFFFu, incl, 31);
     }
 }
 
