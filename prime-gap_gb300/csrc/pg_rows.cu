@@ -83,21 +83,21 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
     // 2. other small primes, one thread per prime walking the CTA's m values
     const uint64_t sp_begin = rd.sp_range[0];
     const uint64_t ns = min((uint64_t)(rd.sp_range[1] - sp_begin), rd.sp_cap);
-    const uint32_t mi_first = s_mi[0], mi_last = s_mi[nrows - 1];
+    const uint32_t mi_first = s_mi[0];
     for (uint64_t i = threadIdx.x; i < ns; i += blockDim.x) {
         const uint32_t p = rd.sp_base + rd.sp[sp_begin + i], r = rd.sr[i];
         uint64_t m = job.mstart + mi_first;
         uint32_t mr = (uint32_t)(((m % p) * r) % p);
         uint32_t x0 = (sl % p + p - mr) % p;
-        uint32_t j = 0;
-        for (uint32_t mi = mi_first; mi <= mi_last; mi++) {
-            if (mi == s_mi[j]) {
-                uint32_t xs = x0 + (((x0 ^ x_par) & 1) ? p : 0);
-                for (uint32_t h = (xs - x_par) >> 1; h < rd.nb; h += p)
-                    atomicOr(&sh[j * nbw + (h >> 5)], 1u << (h & 31));
-                j++;
-            }
-            x0 = x0 >= r ? x0 - r : x0 + (p - r);
+        // row by row (the same row across the warp): step the residue over
+        // the m values since the previous row, then strike this row
+        uint32_t mi_at = mi_first;
+        for (uint32_t j = 0; j < nrows; j++) {
+            const uint32_t mi = s_mi[j];
+            for (; mi_at < mi; mi_at++) x0 = x0 >= r ? x0 - r : x0 + (p - r);
+            const uint32_t xs = x0 + (((x0 ^ x_par) & 1) ? p : 0);
+            for (uint32_t h = (xs - x_par) >> 1; h < rd.nb; h += p)
+                atomicOr(&sh[j * nbw + (h >> 5)], 1u << (h & 31));
         }
     }
     __syncthreads();
@@ -171,6 +171,10 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
         for (uint32_t side = 0; side < 2; side++) {
             uint32_t cnt = 0;
             uint32_t dsum = 0;
+            // digits of the distances: they ascend with h, so a round whose
+            // largest distance is below 10^D has D-digit distances only
+            // (D from the previous round); the others count per lane
+            uint32_t D = 1, T = 10;
             for (uint32_t h0 = 0; h0 < H; h0 += 32) {
                 uint32_t h = h0 + lane;
                 bool unknown = false;
@@ -185,9 +189,17 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
                     unknown = !(sb | gb);
                 }
                 uint32_t bal = __ballot_sync(0xFFFFFFFFu, unknown);
+                const uint32_t dmax = __reduce_max_sync(0xFFFFFFFFu, d);
+                uint32_t nd = D;
+                if (dmax >= T) {
+                    nd = ndigits(d);
+                    D = ndigits(dmax);
+                    for (T = 10; T <= dmax; T *= 10) {
+                    }
+                }
                 if (unknown) {
                     list[side * H + cnt + __popc(bal & lt_mask)] = d;
-                    dsum += ndigits(d);
+                    dsum += nd;
                 }
                 cnt += __popc(bal);
             }
