@@ -673,6 +673,47 @@ PG_HD void rotation_walk(uint64_t mi, uint32_t y, const ThreeGap<T> &g, uint32_t
     }
 }
 
+// rotation_at and rotation_walk in 32-bit arithmetic, for 32-bit primes and
+// walk indices below mi_hi < 2^31.  A step costing mi_hi or more ends the
+// walk whatever its exact cost, so kp and kn are clamped to mi_hi and mi
+// stays below 2^32; results equal the general forms'.
+PG_HD void rotation_at32(uint32_t mi0, uint32_t y0, const ThreeGap<uint32_t> &g, uint32_t n0,
+                         uint32_t mi_hi, uint32_t &y, uint32_t &mi) {
+    const uint32_t C = g.up + g.dn;
+    const uint64_t Y = y0 + (uint64_t)n0 * g.up;
+    uint64_t W;
+    if (n0 < (1u << 19)) {
+        // W = floor(Y / C) <= n0 + 1 < 2^19 + 1 (y0 < C, up < C): a
+        // single-precision quotient is within 2^-21 relative, so within one
+#if defined(__CUDA_ARCH__)
+        W = (uint64_t)((float)Y * __fdividef(1.0f, (float)C));
+#else
+        W = (uint64_t)((float)Y * (1.0f / (float)C));
+#endif
+        const int64_t rem = (int64_t)(Y - W * C);
+        if (rem < 0) W--;
+        else if (rem >= (int64_t)C) W++;
+    } else {
+        W = Y / C;
+    }
+    y = (uint32_t)(Y - W * C);
+    const uint64_t m = mi0 + (n0 - W) * (uint64_t)g.kp + W * (uint64_t)g.kn;
+    mi = m < mi_hi ? (uint32_t)m : mi_hi;
+}
+
+template <typename Emit>
+PG_HD void rotation_walk32(uint32_t mi, uint32_t y, const ThreeGap<uint32_t> &g, uint32_t w,
+                           uint32_t mi_hi, uint32_t steps, Emit &emit) {
+    const uint32_t up = g.up, dn = g.dn;
+    const uint32_t kp = g.kp < mi_hi ? g.kp : mi_hi, kn = g.kn < mi_hi ? g.kn : mi_hi;
+    for (uint32_t k = 0; k < steps && mi < mi_hi; k++) {
+        emit(mi, y, y < w);
+        const bool wrap = y >= dn;
+        y = wrap ? y - dn : y + up;
+        mi += wrap ? kn : kp;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // hit enumeration
 

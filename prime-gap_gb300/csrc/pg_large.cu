@@ -152,7 +152,10 @@ __global__ void __launch_bounds__(kLargeThreads)
                 bool local = true;
                 if (bound <= kDirectSteps) {
                     // few steps: walk the rotation here
-                    rotation_walk<T>(e.t, (uint32_t)e.y, e.g, (uint32_t)w, minc, bound, mark);
+                    if constexpr (sizeof(T) == 4)
+                        rotation_walk32((uint32_t)e.t, e.y, e.g, w, (uint32_t)minc, (uint32_t)bound, mark);
+                    else
+                        rotation_walk<T>(e.t, (uint32_t)e.y, e.g, (uint32_t)w, minc, bound, mark);
                     local = false;
                 } else if (bound > kHeavySteps) {
                     // very many steps: one CTA of heavy_kernel takes this prime
@@ -208,9 +211,15 @@ __global__ void __launch_bounds__(kLargeThreads)
             const uint64_t n0 = (uint64_t)(it - sl.start[s]) * kItemSteps;
             const ThreeGap<T> g{sl.kp[s], (T)sl.up[s], sl.kn[s], (T)sl.dn[s]};
             uint32_t y;
-            uint64_t mi;
-            rotation_at<T>(sl.mi0[s], sl.y0[s], g, n0, y, mi);
-            rotation_walk<T>(mi, y, g, (uint32_t)w, minc, kItemSteps, mark);
+            if constexpr (sizeof(T) == 4) {
+                uint32_t mi;
+                rotation_at32(sl.mi0[s], sl.y0[s], g, (uint32_t)n0, (uint32_t)minc, y, mi);
+                rotation_walk32(mi, y, g, w, (uint32_t)minc, kItemSteps, mark);
+            } else {
+                uint64_t mi;
+                rotation_at<T>(sl.mi0[s], sl.y0[s], g, n0, y, mi);
+                rotation_walk<T>(mi, y, g, (uint32_t)w, minc, kItemSteps, mark);
+            }
         }
         __syncthreads();
     }
