@@ -350,7 +350,9 @@ def run_gb300(args, rank, world, local):
     large_ms = stage_sum.get("large", 0.0) / (args.steps * n_windows)
     model_ops = large_kernel_model_ops(spec, stats, plan) / n_windows
     achieved = model_ops / (large_ms * 1e-3) if large_ms else None
-    traffic = _traffic_per_launch()
+    # the measured traffic is config 2's (profiles/large_kernel_traffic.txt)
+    traffic = (_traffic_per_launch() if args.workload == "config2"
+               and spec.max_prime == WORKLOADS["config2"]["max_prime"] else None)
     roofline_int = {"kernel": "large_kernel<uint32_t>", "bound": "int", "achieved": achieved,
                     "peak": imad_peak, "unit": "int ops/s",
                     "frac": achieved / imad_peak if achieved else None, "traffic": traffic,
