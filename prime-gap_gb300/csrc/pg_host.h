@@ -269,7 +269,7 @@ uint32_t rows_per_block(uint32_t nb, int compression);
 
 // The job's host tables (K limbs, row/column maps, valid m, distances, primes
 // of d, masks) to their device buffers, through one pinned staging block:
-// a copy from pageable memory is staged by the driver and waits for it.
+// a copy from pageable memory is staged by CUDA and waits for it.
 cudaError_t upload_tables(pgs_prepared *pr, cudaStream_t s);
 
 // Copy a finished job's text to pinned host memory (no context lock).

@@ -4,7 +4,7 @@
 // Replaces the reference's GPU Miller-Rabin (kernel_miller_rabin,
 // miller_rabin_t::miller_rabin and powm, miller_rabin.h:154-267: CGBN, eight
 // threads per number) with the one base gap_test_gpu uses (ROUNDS = 1 with
-// primes {2}, gap_test_gpu.cu:81, miller_rabin.h:269), and its driver threads
+// primes {2}, gap_test_gpu.cu:81, miller_rabin.h:269), and its host threads
 // (load_batch_thread, run_gpu_thread, run_overflow_thread,
 // gap_test_gpu.cu:213-640) with device rounds.
 //
