@@ -673,10 +673,11 @@ PG_HD void rotation_walk(uint64_t mi, uint32_t y, const ThreeGap<T> &g, uint32_t
     }
 }
 
-// rotation_at and rotation_walk in 32-bit arithmetic, for 32-bit primes and
-// walk indices below mi_hi < 2^31.  A step costing mi_hi or more ends the
-// walk whatever its exact cost, so kp and kn are clamped to mi_hi and mi
-// stays below 2^32; results equal the general forms'.
+// rotation_at and rotation_walk in 32-bit arithmetic, for walk indices
+// below mi_hi < 2^31 (any prime: gap32 below clamps a 64-bit prime's step
+// costs).  A step costing mi_hi or more ends the walk whatever its exact
+// cost, so kp and kn are clamped to mi_hi and mi stays below 2^32; results
+// equal the general forms'.
 PG_HD void rotation_at32(uint32_t mi0, uint32_t y0, const ThreeGap<uint32_t> &g, uint32_t n0,
                          uint32_t mi_hi, uint32_t &y, uint32_t &mi) {
     const uint32_t C = g.up + g.dn;
@@ -699,6 +700,15 @@ PG_HD void rotation_at32(uint32_t mi0, uint32_t y0, const ThreeGap<uint32_t> &g,
     y = (uint32_t)(Y - W * C);
     const uint64_t m = mi0 + (n0 - W) * (uint64_t)g.kp + W * (uint64_t)g.kn;
     mi = m < mi_hi ? (uint32_t)m : mi_hi;
+}
+
+// A rotation's three-gap data in 32 bits for walks below mi_hi < 2^31:
+// up, dn < w < 2^31, and step costs clamped to mi_hi (a step costing mi_hi
+// or more ends the walk, and rotation_at32 clamps mi to mi_hi).
+template <typename T>
+PG_HD ThreeGap<uint32_t> gap32(const ThreeGap<T> &g, uint32_t mi_hi) {
+    return ThreeGap<uint32_t>{g.kp < mi_hi ? (uint32_t)g.kp : mi_hi, (uint32_t)g.up,
+                              g.kn < mi_hi ? (uint32_t)g.kn : mi_hi, (uint32_t)g.dn};
 }
 
 template <typename Emit>

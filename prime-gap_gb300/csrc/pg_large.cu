@@ -152,10 +152,8 @@ __global__ void __launch_bounds__(kLargeThreads)
                 bool local = true;
                 if (bound <= kDirectSteps) {
                     // few steps: walk the rotation here
-                    if constexpr (sizeof(T) == 4)
-                        rotation_walk32((uint32_t)e.t, e.y, e.g, w, (uint32_t)minc, (uint32_t)bound, mark);
-                    else
-                        rotation_walk<T>(e.t, (uint32_t)e.y, e.g, (uint32_t)w, minc, bound, mark);
+                    rotation_walk32((uint32_t)e.t, (uint32_t)e.y, gap32(e.g, (uint32_t)minc), (uint32_t)w,
+                                    (uint32_t)minc, (uint32_t)bound, mark);
                     local = false;
                 } else if (bound > kHeavySteps) {
                     // very many steps: one CTA of heavy_kernel takes this prime
@@ -209,17 +207,11 @@ __global__ void __launch_bounds__(kLargeThreads)
             }
             const uint32_t s = lo;
             const uint64_t n0 = (uint64_t)(it - sl.start[s]) * kItemSteps;
-            const ThreeGap<T> g{sl.kp[s], (T)sl.up[s], sl.kn[s], (T)sl.dn[s]};
-            uint32_t y;
-            if constexpr (sizeof(T) == 4) {
-                uint32_t mi;
-                rotation_at32(sl.mi0[s], sl.y0[s], g, (uint32_t)n0, (uint32_t)minc, y, mi);
-                rotation_walk32(mi, y, g, w, (uint32_t)minc, kItemSteps, mark);
-            } else {
-                uint64_t mi;
-                rotation_at<T>(sl.mi0[s], sl.y0[s], g, n0, y, mi);
-                rotation_walk<T>(mi, y, g, (uint32_t)w, minc, kItemSteps, mark);
-            }
+            const ThreeGap<uint32_t> g =
+                gap32(ThreeGap<T>{sl.kp[s], (T)sl.up[s], sl.kn[s], (T)sl.dn[s]}, (uint32_t)minc);
+            uint32_t y, mi;
+            rotation_at32(sl.mi0[s], sl.y0[s], g, (uint32_t)n0, (uint32_t)minc, y, mi);
+            rotation_walk32(mi, y, g, (uint32_t)w, (uint32_t)minc, kItemSteps, mark);
         }
         __syncthreads();
     }
@@ -239,13 +231,13 @@ __global__ void __launch_bounds__(kLargeThreads)
     const uint32_t w = job.walk.w;
     for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
         const HeavyPrime hp = heavy[h];
-        const ThreeGap<uint64_t> g{hp.kp, hp.up, hp.kn, hp.dn};
+        const uint32_t jmax = (uint32_t)job.walk.jmax;
+        const ThreeGap<uint32_t> g = gap32(ThreeGap<uint64_t>{hp.kp, hp.up, hp.kn, hp.dn}, jmax);
         const uint64_t items = (hp.steps + kItemSteps - 1) / kItemSteps;
         for (uint64_t it = threadIdx.x; it < items; it += blockDim.x) {
-            uint32_t y;
-            uint64_t mi;
-            rotation_at<uint64_t>(hp.mi0, hp.y0, g, it * kItemSteps, y, mi);
-            rotation_walk<uint64_t>(mi, y, g, w, job.walk.jmax, kItemSteps, mark);
+            uint32_t y, mi;
+            rotation_at32(hp.mi0, hp.y0, g, (uint32_t)(it * kItemSteps), jmax, y, mi);
+            rotation_walk32(mi, y, g, w, jmax, kItemSteps, mark);
         }
     }
 }

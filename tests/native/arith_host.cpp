@@ -102,26 +102,17 @@ size_t ah_hits_items(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint6
         pg::Entry<T> e = pg::first_entry<T>(p_, r_, w, t0);
         if (e.t >= max_mi || e.y >= w) return;
         uint64_t bound = pg::rotation_steps_bound<T>(e.t, max_mi, e.g, p_);
-        // 32-bit primes take the kernel's 32-bit walk forms
+        // the kernel's 32-bit walk forms, step costs clamped to max_mi
+        const pg::ThreeGap<uint32_t> g = pg::gap32(e.g, max_mi);
         if (bound <= direct) {
-            if constexpr (sizeof(T) == 4)
-                pg::rotation_walk32((uint32_t)e.t, e.y, e.g, w, max_mi, (uint32_t)bound, c);
-            else
-                pg::rotation_walk<T>(e.t, (uint32_t)e.y, e.g, (uint32_t)w, max_mi, bound, c);
+            pg::rotation_walk32((uint32_t)e.t, (uint32_t)e.y, g, (uint32_t)w, max_mi, (uint32_t)bound, c);
             return;
         }
         uint64_t items = (bound + item_steps - 1) / item_steps;
         for (uint64_t it = 0; it < items; it++) {
-            uint32_t y;
-            if constexpr (sizeof(T) == 4) {
-                uint32_t mi;
-                pg::rotation_at32((uint32_t)e.t, e.y, e.g, (uint32_t)(it * item_steps), max_mi, y, mi);
-                pg::rotation_walk32(mi, y, e.g, w, max_mi, item_steps, c);
-            } else {
-                uint64_t mi;
-                pg::rotation_at<T>(e.t, (uint32_t)e.y, e.g, it * item_steps, y, mi);
-                pg::rotation_walk<T>(mi, y, e.g, (uint32_t)w, max_mi, item_steps, c);
-            }
+            uint32_t y, mi;
+            pg::rotation_at32((uint32_t)e.t, (uint32_t)e.y, g, (uint32_t)(it * item_steps), max_mi, y, mi);
+            pg::rotation_walk32(mi, y, g, (uint32_t)w, max_mi, item_steps, c);
         }
     };
     if (p < 0xFFFFFFFFull) {
@@ -266,4 +257,5 @@ uint64_t ah_mulmod(uint64_t a, uint64_t b, uint64_t p) { return pg::mulmod_u64(a
 // Montgomery reduction (R = 2^32) and -p^-1 mod 2^32 of the K mod p kernel.
 uint32_t ah_redc32(uint64_t t, uint32_t p) { return pg::redc32(t, p, pg::neg_inv32(p)); }
 uint32_t ah_neg_inv32(uint32_t p) { return pg::neg_inv32(p); }
+
 }
