@@ -56,6 +56,9 @@ void pgs_destroy(pgs_ctx *ctx) {
     ctx->heavy.release();
     batch_state_destroy(ctx);
     ctx->dpool.trim();
+    if (ctx->copy) cudaStreamDestroy(ctx->copy);
+    for (cudaStream_t c : ctx->chunk)
+        if (c) cudaStreamDestroy(c);
     if (ctx->own) cudaStreamDestroy(ctx->own);
     delete ctx;
 }
@@ -158,7 +161,7 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     CK(pr->row_bytes.ensure(rows * 8ull));
     CK(pr->offsets.ensure(rows * 8ull));
     CK(pr->scan_tmp.ensure(pg::scan_tmp_words(rows) * 8));
-    CK(pr->misc.ensure((3 + 2 * pr->windows.size()) * 8));
+    CK(pr->misc.ensure((3 + 2 * pr->windows.size() + kTextChunks) * 8));
     {
         const uint64_t mmax = h.job.mstart + h.job.minc;
         uint64_t per_row = ndigits(mmax) + 2ull * ndigits(h.H) + 16;
@@ -179,9 +182,142 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     return PGS_OK;
 }
 
-int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
-    if (!ctx || !pr || pr->ctx != ctx) return PGS_EINVAL;
-    std::lock_guard<std::mutex> g(ctx->mu);
+namespace {
+
+// The rows, their offsets and their text in kTextChunks chunks of rows, each
+// chunk's text copied to pinned host memory on the context's copy stream as
+// soon as it is written, while the next chunks' rows are sieved.  The chunk
+// ends (running text offsets) are scanned on the device with a carry-in; the
+// host reads each end from the chunk's event and sizes the host buffer from
+// the first chunk (rows are alike), moving to an exact buffer in the rare
+// case that a later chunk overruns the estimate.
+int text_pipeline(pgs_ctx *ctx, pgs_prepared *pr, const pg::RowsDev &rd, uint32_t rpb, cudaStream_t s,
+                  HostText &sink) {
+    const uint32_t rows = (uint32_t)pr->hj.valid_mi.size();
+    const uint32_t nblk = (rows + rpb - 1) / rpb;
+    const int C = (int)std::min<uint32_t>(kTextChunks, std::max<uint32_t>(nblk, 1));
+    std::vector<uint32_t> rb(C + 1);
+    for (int c = 0; c <= C; c++)
+        rb[c] = (uint32_t)std::min<uint64_t>(rows, (uint64_t)nblk * c / C * rpb);
+    uint64_t *misc = pr->misc.as<uint64_t>();
+    uint64_t *ends = misc + 3 + 2 * pr->windows.size();
+    if (!ctx->copy) CK(cudaStreamCreateWithFlags(&ctx->copy, cudaStreamNonBlocking));
+    if (!ctx->chunk[0]) {
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        for (int c = 0; c < kTextChunks; c++)
+            CK(cudaStreamCreateWithPriority(&ctx->chunk[c], cudaStreamNonBlocking, std::min(least, greatest + c)));
+    }
+    cudaStream_t cs = ctx->copy;
+    PinnedPool &pool = pinned_pool();
+    size_t ecap = 0, cap = 0;
+    uint64_t *h_ends = (uint64_t *)pool.get(kTextChunks * 8, &ecap);
+    if (!h_ends) {
+        ctx->err = "cudaMallocHost failed";
+        return PGS_ENOMEM;
+    }
+    char *host = nullptr;
+    // each chunk on its own stream: the rows kernels of all chunks run
+    // together (earlier chunks' CTAs first), so no chunk ends in a partial
+    // wave; the scans run in chunk order (each adds the previous chunk's end)
+    std::vector<cudaEvent_t> ev(C, nullptr), scanned(C, nullptr);
+    cudaEvent_t t0 = nullptr, t1 = nullptr, ready = nullptr;
+    cudaError_t e = cudaSuccess;
+    int rc = PGS_OK;
+    for (int c = 0; c < C && e == cudaSuccess; c++) {
+        e = cudaEventCreateWithFlags(&ev[c], cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&scanned[c], cudaEventDisableTiming);
+    }
+    if (e == cudaSuccess) e = cudaEventCreate(&t0);
+    if (e == cudaSuccess) e = cudaEventCreate(&t1);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ready, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventRecord(ready, s);
+    for (int c = 0; c < C && e == cudaSuccess; c++) {
+        cudaStream_t sc = ctx->chunk[c];
+        e = cudaStreamWaitEvent(sc, ready, 0);
+        if (e == cudaSuccess) e = pg::rows_extract(rd, rpb, sc, rb[c], rb[c + 1]);
+        if (e == cudaSuccess && c) e = cudaStreamWaitEvent(sc, scanned[c - 1], 0);
+        if (e == cudaSuccess)
+            e = pg::scan_u64(pr->row_bytes.as<uint64_t>() + rb[c], pr->offsets.as<uint64_t>() + rb[c], ends + c,
+                             rb[c + 1] - rb[c], pr->scan_tmp.as<uint64_t>(), sc, c ? ends + c - 1 : nullptr);
+        if (e == cudaSuccess) e = cudaEventRecord(scanned[c], sc);
+        if (e == cudaSuccess)
+            e = pg::format_rows(rd, pr->offsets.as<uint64_t>(), pr->text.as<char>(), sc, rb[c], rb[c + 1]);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(h_ends + c, ends + c, 8, cudaMemcpyDeviceToHost, sc);
+        if (e == cudaSuccess) e = cudaEventRecord(ev[c], sc);
+        pr->launches += 5;
+    }
+    // the job's stream continues after every chunk
+    for (int c = 0; c < C && e == cudaSuccess; c++) e = cudaStreamWaitEvent(s, ev[c], 0);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(misc, ends + C - 1, 8, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaEventRecord(t0, cs);
+    for (int c = 0; c < C && e == cudaSuccess && rc == PGS_OK; c++) {
+        if ((e = cudaEventSynchronize(ev[c]))) break;
+        const uint64_t lo = c ? h_ends[c - 1] : 0, hi = h_ends[c];
+        if (hi > pr->text_cap) {
+            ctx->err = "text larger than its bound";
+            rc = PGS_ECUDA;
+            break;
+        }
+        if (!host) {
+            // text of the whole job, estimated from its first chunk (the
+            // factor can be lowered through PGSIEVE_TEXT_ESTIMATE, which the
+            // tests use to take the exact-buffer path)
+            const char *fe = getenv("PGSIEVE_TEXT_ESTIMATE");
+            const double f = fe ? atof(fe) : 1.1;
+            uint64_t est = (uint64_t)((double)hi * rows / std::max<uint32_t>(rb[c + 1], 1) * f) +
+                           (f >= 1.0 ? 65536 : 0);
+            est = std::min<uint64_t>(std::max<uint64_t>(est, hi), pr->text_cap);
+            if (!(host = pool.get(est + 1, &cap))) rc = PGS_ENOMEM;
+        } else if (hi + 1 > cap) {
+            // the estimate was short: wait for the whole text, then move the
+            // part copied so far to a buffer of the exact size
+            uint64_t total = 0;
+            if ((e = cudaEventSynchronize(ev[C - 1])) || (e = cudaStreamSynchronize(cs))) break;
+            total = h_ends[C - 1];
+            size_t ncap = 0;
+            char *nh = pool.get(total + 1, &ncap);
+            if (!nh) {
+                rc = PGS_ENOMEM;
+                break;
+            }
+            memcpy(nh, host, lo);
+            pool.put(host, cap);
+            host = nh, cap = ncap;
+        }
+        if (rc == PGS_OK && hi > lo)
+            e = cudaMemcpyAsync(host + lo, pr->text.as<char>() + lo, hi - lo, cudaMemcpyDeviceToHost, cs);
+    }
+    if (e == cudaSuccess && rc == PGS_OK) e = cudaEventRecord(t1, cs);
+    if (e == cudaSuccess && rc == PGS_OK) e = cudaStreamSynchronize(cs);
+    if (e == cudaSuccess && rc == PGS_OK) {
+        sink.total = C ? h_ends[C - 1] : 0;
+        host[sink.total] = 0;
+        sink.text = host, sink.cap = cap;
+        cudaEventElapsedTime(&sink.ms_d2h, t0, t1);
+        host = nullptr;
+    }
+    cudaStreamSynchronize(cs);
+    if (host) pool.put(host, cap);
+    pool.put((char *)h_ends, ecap);
+    for (int c = 0; c < C; c++) {
+        if (ev[c]) cudaEventDestroy(ev[c]);
+        if (scanned[c]) cudaEventDestroy(scanned[c]);
+    }
+    if (ready) cudaEventDestroy(ready);
+    if (t0) cudaEventDestroy(t0);
+    if (t1) cudaEventDestroy(t1);
+    if (e != cudaSuccess) {
+        ctx->err = cudaGetErrorString(e);
+        return PGS_ECUDA;
+    }
+    if (rc == PGS_ENOMEM) ctx->err = "cudaMallocHost failed";
+    return rc;
+}
+
+// One run of a prepared job (context locked).  With `sink`, the rows and
+// text are pipelined with their copy to the host (text_pipeline).
+int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     HostJob &h = pr->hj;
@@ -258,6 +394,16 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
     }
     // rows, text
     CK(mark(a));
+    if (sink) {
+        // rows and text interleave with the copy: one span for both
+        const int rc = text_pipeline(ctx, pr, rd, rows_per_block(h.nb, h.job.compression), s, *sink);
+        if (rc) return rc;
+        CK(mark(b));
+        span(PGS_STAGE_ROWS, a, b);
+        span(-1, first, b);
+        pr->ran = true;
+        return PGS_OK;
+    }
     CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression), s));
     CK(mark(b));
     span(PGS_STAGE_ROWS, a, b);
@@ -270,6 +416,14 @@ int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
     pr->launches += 5;
     pr->ran = true;
     return PGS_OK;
+}
+
+}  // namespace
+
+int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
+    if (!ctx || !pr || pr->ctx != ctx) return PGS_EINVAL;
+    std::lock_guard<std::mutex> g(ctx->mu);
+    return run_job(ctx, pr, record_stages, nullptr);
 }
 
 int pgs_fetch(pgs_ctx *ctx, pgs_prepared *pr, pgs_result *out) {
@@ -334,8 +488,16 @@ int pgs_method2(pgs_ctx *ctx, const pgs_job *job, pgs_result *out) {
     pgs_prepared *pr = nullptr;
     int rc = pgs_prepare(ctx, job, &pr);
     if (rc) return rc;
-    rc = pgs_run(ctx, pr, 1);
-    if (rc == PGS_OK) rc = pgs_fetch(ctx, pr, out);
+    {
+        // the text goes to the host chunk by chunk while later rows run
+        std::lock_guard<std::mutex> g(ctx->mu);
+        HostText ht;
+        rc = run_job(ctx, pr, 1, &ht);
+        if (rc == PGS_OK) {
+            rc = fetch_job(ctx, pr, ctx->stream, out, &ht);
+            if (rc != PGS_OK) pinned_pool().put(ht.text, ht.cap);
+        }
+    }
     pgs_prepared_free(pr);
     return rc;
 }

@@ -341,7 +341,7 @@ size_t job_ranges(const pgs_prepared *pr) {
     return 1 + (pr->table_mode ? pr->tbl_windows.size() : pr->windows.size());
 }
 
-int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out) {
+int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out, const HostText *given) {
     memset(out, 0, sizeof(*out));
     const HostJob &h = pr->hj;
     // misc: [0] text bytes, then {begin, end} pairs: small primes, then windows
@@ -349,29 +349,36 @@ int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out) {
     std::vector<uint64_t> misc(1 + 2 * nr);
     CK(cudaMemcpyAsync(misc.data(), pr->misc.p, misc.size() * 8, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
-    const uint64_t total = misc[0];
+    const uint64_t total = given ? given->total : misc[0];
     if (total > pr->text_cap) {
         ctx->err = "text larger than its bound";
         return PGS_ECUDA;
     }
     size_t cap = 0;
-    char *host = pinned_pool().get(total + 1, &cap);
-    if (!host) {
-        ctx->err = "cudaMallocHost failed";
-        return PGS_ENOMEM;
-    }
-    cudaEvent_t t0, t1;
-    CK(cudaEventCreate(&t0));
-    CK(cudaEventCreate(&t1));
-    CK(cudaEventRecord(t0, s));
-    if (total) CK(cudaMemcpyAsync(host, pr->text.p, total, cudaMemcpyDeviceToHost, s));
-    CK(cudaEventRecord(t1, s));
-    CK(cudaStreamSynchronize(s));
-    host[total] = 0;
+    char *host = nullptr;
     float ms_d2h = 0;
-    cudaEventElapsedTime(&ms_d2h, t0, t1);
-    cudaEventDestroy(t0);
-    cudaEventDestroy(t1);
+    if (given) {
+        host = given->text;
+        cap = given->cap;
+        ms_d2h = given->ms_d2h;
+    } else {
+        host = pinned_pool().get(total + 1, &cap);
+        if (!host) {
+            ctx->err = "cudaMallocHost failed";
+            return PGS_ENOMEM;
+        }
+        cudaEvent_t t0, t1;
+        CK(cudaEventCreate(&t0));
+        CK(cudaEventCreate(&t1));
+        CK(cudaEventRecord(t0, s));
+        if (total) CK(cudaMemcpyAsync(host, pr->text.p, total, cudaMemcpyDeviceToHost, s));
+        CK(cudaEventRecord(t1, s));
+        CK(cudaStreamSynchronize(s));
+        host[total] = 0;
+        cudaEventElapsedTime(&ms_d2h, t0, t1);
+        cudaEventDestroy(t0);
+        cudaEventDestroy(t1);
+    }
 
     out->text = host;
     out->text_len = total;

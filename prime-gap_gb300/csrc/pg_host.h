@@ -184,10 +184,16 @@ struct Window {
 struct PrimeTable;
 struct Lane;
 
+// Chunks of rows whose text is copied to the host while later chunks run.
+constexpr int kTextChunks = 4;
+
 struct pgs_ctx {
     int device = 0;
     cudaStream_t own = nullptr;
     cudaStream_t stream = nullptr;
+    cudaStream_t copy = nullptr;  // text copies to the host beside the job's kernels
+    // one stream per chunk of rows, earlier chunks at higher priority
+    cudaStream_t chunk[kTextChunks] = {};
     std::mutex mu;
     std::string err;
     pg::BasePrimes base;
@@ -272,8 +278,17 @@ uint32_t rows_per_block(uint32_t nb, int compression);
 // a copy from pageable memory is staged by CUDA and waits for it.
 cudaError_t upload_tables(pgs_prepared *pr, cudaStream_t s);
 
-// Copy a finished job's text to pinned host memory (no context lock).
-int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out);
+// Text already copied to pinned host memory (the pipelined one-call path).
+struct HostText {
+    char *text = nullptr;
+    size_t cap = 0;       // pinned pool capacity
+    uint64_t total = 0;   // bytes
+    float ms_d2h = 0;
+};
+// A finished job's result: its text copied to pinned host memory, or the
+// text given, and its counts and stage times (no context lock).
+int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out,
+              const HostText *given = nullptr);
 // Number of {begin, end} prime ranges in a prepared job's misc buffer.
 size_t job_ranges(const pgs_prepared *pr);
 // Free the resident prime table and the lanes (pg_batch.cu).

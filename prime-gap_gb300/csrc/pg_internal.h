@@ -134,15 +134,19 @@ struct RowsDev {
     int compression;       // 0 plain, 1 RLE
 };
 
-cudaError_t rows_extract(const RowsDev &rd, uint32_t rows_per_block, cudaStream_t stream);
+// Rows [row_lo, row_hi) (row_lo a multiple of rows_per_block; all by default).
+cudaError_t rows_extract(const RowsDev &rd, uint32_t rows_per_block, cudaStream_t stream,
+                         uint32_t row_lo = 0, uint32_t row_hi = ~0u);
 
-// Exclusive scan of n 64-bit values; total written to *d_total.
+// Exclusive scan of n 64-bit values, plus *d_base when given; base + total
+// written to *d_total.
 cudaError_t scan_u64(const uint64_t *d_in, uint64_t *d_out, uint64_t *d_total, uint64_t n,
-                     uint64_t *d_tmp, cudaStream_t stream);
+                     uint64_t *d_tmp, cudaStream_t stream, const uint64_t *d_base = nullptr);
 uint64_t scan_tmp_words(uint64_t n);
 
-cudaError_t format_rows(const RowsDev &rd, const uint64_t *d_offsets, char *d_text,
-                        cudaStream_t stream);
+// Text of rows [row_lo, row_hi) (all by default) at their offsets.
+cudaError_t format_rows(const RowsDev &rd, const uint64_t *d_offsets, char *d_text, cudaStream_t stream,
+                        uint32_t row_lo = 0, uint32_t row_hi = ~0u);
 
 // ---- C-ABI helpers (pg_tools.cu) -----------------------------------------------
 

@@ -18,6 +18,8 @@
 // prefix sum of the per-row byte counts.
 #include "pg_internal.h"
 
+#include <algorithm>
+
 namespace pg {
 
 namespace {
@@ -40,11 +42,12 @@ __device__ __forceinline__ uint32_t word_pattern(uint32_t q) {
     return m;
 }
 
-__global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t rows_per_block) {
+__global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t rows_per_block,
+                                                            uint32_t block0) {
     extern __shared__ uint32_t sh[];
     const JobDev &job = rd.job;
     const uint32_t nbw = (rd.nb + 31) / 32;
-    const uint32_t r0 = blockIdx.x * rows_per_block;
+    const uint32_t r0 = (blockIdx.x + block0) * rows_per_block;
     if (r0 >= job.rows) return;
     const uint32_t nrows = min(rows_per_block, job.rows - r0);
     uint32_t *s_mi = sh + (size_t)rows_per_block * nbw;  // rows_per_block entries
@@ -269,9 +272,9 @@ __global__ void __launch_bounds__(kScanThreads) scan_reduce_kernel(const uint64_
 }
 
 __global__ void __launch_bounds__(kScanThreads) scan_blocks_kernel(uint64_t *block_sums, uint64_t nb,
-                                                                   uint64_t *total) {
+                                                                   uint64_t *total, const uint64_t *base) {
     __shared__ uint64_t s_carry;
-    if (threadIdx.x == 0) s_carry = 0;
+    if (threadIdx.x == 0) s_carry = base ? *base : 0;
     __syncthreads();
     for (uint64_t b0 = 0; b0 < nb; b0 += kScanThreads) {
         uint64_t i = b0 + threadIdx.x;
@@ -323,12 +326,12 @@ __device__ __forceinline__ uint32_t put_u64(char *dst, uint64_t v) {
 // One warp per row.  Plain rows: "m : -nl +nh | -d1 -d2 | +d1 +d2\n"
 // (combined_sieve.cpp:1387-1438); RLE rows encode each distance step as two
 // characters 48 + (delta >> 7), 48 + (delta & 127) (combined_sieve.cpp:1396-1417).
-__global__ void __launch_bounds__(256) format_kernel(RowsDev rd, const uint64_t *offsets,
-                                                     char *text) {
+__global__ void __launch_bounds__(256) format_kernel(RowsDev rd, const uint64_t *offsets, char *text,
+                                                     uint32_t row_lo, uint32_t row_hi) {
     const JobDev &job = rd.job;
-    const uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const uint32_t row = row_lo + ((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
-    if (row >= job.rows) return;
+    if (row >= row_hi) return;
     const uint32_t H = job.half_cols;
     const uint32_t *list = rd.lists + (uint64_t)row * 2 * H;
     const uint32_t cnt[2] = {rd.counts[2 * row], rd.counts[2 * row + 1]};
@@ -416,8 +419,11 @@ __global__ void __launch_bounds__(256) format_kernel(RowsDev rd, const uint64_t 
 
 }  // namespace
 
-cudaError_t rows_extract(const RowsDev &rd, uint32_t rows_per_block, cudaStream_t stream) {
-    if (rd.job.rows == 0) return cudaSuccess;
+cudaError_t rows_extract(const RowsDev &rd, uint32_t rows_per_block, cudaStream_t stream, uint32_t row_lo,
+                         uint32_t row_hi) {
+    row_hi = std::min(row_hi, (uint32_t)rd.job.rows);
+    if (row_lo >= row_hi) return cudaSuccess;
+    if (row_lo % rows_per_block) return cudaErrorInvalidValue;
     if (rd.nd > (uint32_t)kMaxDPrimes) return cudaErrorInvalidValue;
     const uint32_t nbw = (rd.nb + 31) / 32;
     size_t smem = ((size_t)rows_per_block * nbw * (rd.compression == 2 ? 2 : 1) + rows_per_block +
@@ -427,30 +433,33 @@ cudaError_t rows_extract(const RowsDev &rd, uint32_t rows_per_block, cudaStream_
                                              (int)smem);
         if (e) return e;
     }
-    uint32_t blocks = (rd.job.rows + rows_per_block - 1) / rows_per_block;
-    rows_kernel<<<blocks, kRowThreads, smem, stream>>>(rd, rows_per_block);
+    uint32_t blocks = (row_hi - row_lo + rows_per_block - 1) / rows_per_block;
+    rows_kernel<<<blocks, kRowThreads, smem, stream>>>(rd, rows_per_block, row_lo / rows_per_block);
     return cudaGetLastError();
 }
 
 uint64_t scan_tmp_words(uint64_t n) { return (n + kScanChunk - 1) / kScanChunk + 1; }
 
 cudaError_t scan_u64(const uint64_t *d_in, uint64_t *d_out, uint64_t *d_total, uint64_t n,
-                     uint64_t *d_tmp, cudaStream_t stream) {
+                     uint64_t *d_tmp, cudaStream_t stream, const uint64_t *d_base) {
     if (n == 0) {
+        if (d_base) return cudaMemcpyAsync(d_total, d_base, sizeof(uint64_t), cudaMemcpyDeviceToDevice, stream);
         return cudaMemsetAsync(d_total, 0, sizeof(uint64_t), stream);
     }
     uint64_t nb = (n + kScanChunk - 1) / kScanChunk;
     scan_reduce_kernel<<<(unsigned)nb, kScanThreads, 0, stream>>>(d_in, n, d_tmp);
-    scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(d_tmp, nb, d_total);
+    scan_blocks_kernel<<<1, kScanThreads, 0, stream>>>(d_tmp, nb, d_total, d_base);
     scan_apply_kernel<<<(unsigned)nb, kScanThreads, 0, stream>>>(d_in, n, d_tmp, d_out);
     return cudaGetLastError();
 }
 
-cudaError_t format_rows(const RowsDev &rd, const uint64_t *d_offsets, char *d_text,
-                        cudaStream_t stream) {
-    if (rd.job.rows == 0) return cudaSuccess;
-    uint64_t threads = (uint64_t)rd.job.rows * 32;
-    format_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(rd, d_offsets, d_text);
+cudaError_t format_rows(const RowsDev &rd, const uint64_t *d_offsets, char *d_text, cudaStream_t stream,
+                        uint32_t row_lo, uint32_t row_hi) {
+    row_hi = std::min(row_hi, (uint32_t)rd.job.rows);
+    if (row_lo >= row_hi) return cudaSuccess;
+    uint64_t threads = (uint64_t)(row_hi - row_lo) * 32;
+    format_kernel<<<(unsigned)((threads + 255) / 256), 256, 0, stream>>>(rd, d_offsets, d_text, row_lo,
+                                                                          row_hi);
     return cudaGetLastError();
 }
 

@@ -45,7 +45,7 @@ def test_method2_matches_reference_golden(sieve, goldens, name):
 
 
 def test_config2_full_size_matches_reference(sieve, goldens):
-    """BASELINE config 2 (P=1511, d=2190, minc=1e5, SL=2e4, max_prime=2e9)."""
+    """Config 2 (P=1511, d=2190, minc=1e5, SL=2e4, max_prime=2e9)."""
     g = goldens["config2"]
     data = sieve.method2(_spec(g))
     assert hashlib.md5(data).hexdigest() == g["md5"]
@@ -91,6 +91,19 @@ def test_method2_masks_near_shared_memory_limits(sieve, minc):
     got = sieve.method2(spec)
     want = pgo.method2(89, 105, 1000003, minc, 1000, 2_000_000, 1, threads=16)
     assert got == want, _first_diff(got, want)
+
+
+@pytest.mark.parametrize("name", ["fn1", "config1", "small_bc_d30", "small_rle_d210"])
+def test_method2_text_pipeline_short_estimate(sieve, goldens, name, monkeypatch):
+    """The one-call path copies each chunk of rows' text to the host while
+    later chunks run, into a buffer sized from the first chunk; with the
+    estimate cut to 5 % every later chunk overruns it and the text moves to
+    an exact buffer part way.  The bytes must not change."""
+    monkeypatch.setenv("PGSIEVE_TEXT_ESTIMATE", "0.05")
+    g = goldens[name]
+    data = sieve.method2(_spec(g))
+    assert hashlib.md5(data).hexdigest() == g["md5"]
+    assert len(data) == g["bytes"]
 
 
 def test_prepare_run_fetch_repeatable(sieve, goldens):
