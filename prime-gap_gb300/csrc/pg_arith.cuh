@@ -645,39 +645,14 @@ PG_HD uint64_t rotation_steps_bound(uint64_t mi0, uint64_t mi_hi, const ThreeGap
     return b < cap ? b : cap;
 }
 
-// Position of rotation step n0 from the first hit (mi0, y0): residue and mi.
-template <typename T>
-PG_HD void rotation_at(uint64_t mi0, uint32_t y0, const ThreeGap<T> &g, uint64_t n0,
-                       uint32_t &y, uint64_t &mi) {
-    const uint32_t up = (uint32_t)g.up, C = (uint32_t)(g.up + g.dn);
-    const uint64_t Y = y0 + n0 * up;
-    const uint64_t W = Y / C;
-    y = (uint32_t)(Y - W * C);
-    mi = mi0 + (n0 - W) * (uint64_t)g.kp + W * (uint64_t)g.kn;
-}
-
-// Up to `steps` rotation steps from (mi, y) while mi < mi_hi, calling
-// emit(mi, y, y < w) at every step (the emitter acts on hits; calling it
-// unconditionally keeps the warp's lanes on one path).  A step wraps when
-// y + up >= C, i.e. y >= dn.  up, dn < w < 2^31 so residues fit 32 bits.
-template <typename T, typename Emit>
-PG_HD void rotation_walk(uint64_t mi, uint32_t y, const ThreeGap<T> &g, uint32_t w, uint64_t mi_hi,
-                         uint64_t steps, Emit &emit) {
-    const uint32_t up = (uint32_t)g.up, dn = (uint32_t)g.dn;
-    const uint64_t kp = g.kp, kn = g.kn;
-    for (uint64_t k = 0; k < steps && mi < mi_hi; k++) {
-        emit(mi, y, y < w);
-        const bool wrap = y >= dn;
-        y = wrap ? y - dn : y + up;
-        mi += wrap ? kn : kp;
-    }
-}
-
-// rotation_at and rotation_walk in 32-bit arithmetic, for walk indices
-// below mi_hi < 2^31 (any prime: gap32 below clamps a 64-bit prime's step
-// costs).  A step costing mi_hi or more ends the walk whatever its exact
-// cost, so kp and kn are clamped to mi_hi and mi stays below 2^32; results
-// equal the general forms'.
+// The rotation's walk in 32-bit arithmetic, for walk indices below
+// mi_hi < 2^31 (any prime: gap32 below clamps a 64-bit prime's step costs).
+// A step costing mi_hi or more ends the walk whatever its exact cost, so kp
+// and kn are clamped to mi_hi and mi stays below 2^32.
+//
+// rotation_at32: position of rotation step n0 from the first hit (mi0, y0):
+// Y = y0 + n0*up, residue Y mod C, mi = mi0 + (n0 - W)*kp + W*kn with
+// W = floor(Y / C), clamped to mi_hi.
 PG_HD void rotation_at32(uint32_t mi0, uint32_t y0, const ThreeGap<uint32_t> &g, uint32_t n0,
                          uint32_t mi_hi, uint32_t &y, uint32_t &mi) {
     const uint32_t C = g.up + g.dn;
@@ -711,6 +686,10 @@ PG_HD ThreeGap<uint32_t> gap32(const ThreeGap<T> &g, uint32_t mi_hi) {
                               g.kn < mi_hi ? (uint32_t)g.kn : mi_hi, (uint32_t)g.dn};
 }
 
+// rotation_walk32: up to `steps` rotation steps from (mi, y) while
+// mi < mi_hi, calling emit(mi, y, y < w) at every step (the emitter acts on
+// hits; calling it unconditionally keeps a warp's lanes on one path).  A step
+// wraps when y + up >= C, i.e. y >= dn.
 template <typename Emit>
 PG_HD void rotation_walk32(uint32_t mi, uint32_t y, const ThreeGap<uint32_t> &g, uint32_t w,
                            uint32_t mi_hi, uint32_t steps, Emit &emit) {
