@@ -297,6 +297,9 @@ int text_pipeline(pgs_ctx *ctx, pgs_prepared *pr, const pg::RowsDev &rd, uint32_
         cudaEventElapsedTime(&sink.ms_d2h, t0, t1);
         host = nullptr;
     }
+    // nothing of this job may still run once it returns (an error can leave
+    // chunks queued that the job's stream does not wait for)
+    for (int c = 0; c < C; c++) cudaStreamSynchronize(ctx->chunk[c]);
     cudaStreamSynchronize(cs);
     if (host) pool.put(host, cap);
     pool.put((char *)h_ends, ecap);
