@@ -10,24 +10,34 @@ which shows up as extra unknowns: misc/tests.sh's FN2 hashes to
 540add3a... instead of a8d85c96... with -t 8 on an 8-core host.  Entries marked "published" carry md5 values printed in the
 reference's own test script / docs; the script checks they still reproduce.
 
-    python tests/golden/make_goldens.py [--with-large]
+With --mix it writes tests/golden/mix_goldens.json instead: the reference's
+md5 for every job of the seeded 64-job mix (workloads.mixed_jobs(64, seed=4))
+and for jobs whose primes cross 2^32, run as concurrent one-thread reference
+processes.  Jobs with gcd(d, 210) = 30 and SL > 30,583 go through the
+wheel-fixed copy, because the unmodified reference aborts on them
+(combined_sieve.cpp:1229); its bytes equal the unmodified --method1 output
+(checked on config 3, golden 1781f036...).
+
+    python tests/golden/make_goldens.py [--with-large] [--mix] [-j 8]
 """
 from __future__ import annotations
 
 import argparse
+import concurrent.futures as cf
 import hashlib
 import json
-import sqlite3
+import math
 import subprocess
+import sys
 import tempfile
 import time
 from pathlib import Path
 
 ROOT = Path(__file__).resolve().parents[2]
-REF_DIR = Path("/root/reference")
 REF_BIN = ROOT / "oracle" / "_ref" / "combined_sieve"
 REF_FIX = ROOT / "oracle" / "_ref" / "combined_sieve_wheelfix"
 OUT = Path(__file__).resolve().parent / "goldens.json"
+MIX_OUT = Path(__file__).resolve().parent / "mix_goldens.json"
 
 # (name, p, d, mstart, minc, SL, max_prime_millions, flags, published md5 or None, source)
 JOBS = [
@@ -54,31 +64,86 @@ LARGE_JOBS = [
     ("config2", 1511, 2190, 12345679, 100000, 20000, 2000, [], None, "reference run"),
 ]
 
+# Jobs whose sieving primes cross 2^32 (64-bit K mod p and walk starts):
+# (name, p, d, mstart, minc, SL, max_prime_millions, flags)
+WIDE_JOBS = [
+    ("w64_503_210", 503, 210, 1234567, 300, 5000, 4400, []),
+    ("w64_1009_2190_rle", 1009, 2190, 777, 200, 9000, 4300, ["--rle"]),
+    ("w64_797_30030", 797, 30030, 5550001, 3000, 11500, 6000, []),
+    ("w64_1511_1_bc", 1511, 1, 424242, 1500, 23500, 5000, ["--bitcompressed"]),
+    ("w64_2003_2190", 2003, 2190, 31415926, 2000, 32000, 8000, []),
+    ("w64_3001_210", 3001, 210, 2718281, 1000, 40000, 12000, []),
+    ("w64_1009_2", 1009, 2, 99991, 2500, 15000, 5000, []),
+    ("w64_601_7", 601, 7, 8675309, 1200, 6500, 4500, []),
+]
+
 
 def run_ref(binary: Path, p, d, mstart, minc, sl, mp, flags, threads=1) -> tuple[bytes, float]:
     with tempfile.TemporaryDirectory() as td:
         tdp = Path(td)
         (tdp / "unknowns").mkdir()
-        db = tdp / "test.db"
-        con = sqlite3.connect(db)
-        con.executescript((REF_DIR / "schema.sql").read_text())
-        con.commit()
-        con.close()
         cmd = [str(binary), "-qqq", "--save", "-p", str(p), "-d", str(d), "--mstart", str(mstart),
                "--minc", str(minc), "--sieve-length", str(sl), "--max-prime", str(mp),
-               "--search-db", str(db), "-t", str(threads), *flags]
+               "-t", str(threads), *flags]
         t = time.perf_counter()
-        subprocess.run(cmd, cwd=td, check=True, capture_output=True)
+        # exits 1 after saving the file when there is no search database to record the range in
+        subprocess.run(cmd, cwd=td, check=False, capture_output=True)
         dt = time.perf_counter() - t
         files = list((tdp / "unknowns").iterdir())
         assert len(files) == 1, files
         return files[0].read_bytes(), dt
 
 
+def _needs_wheelfix(d: int, sl: int) -> bool:
+    """The unmodified reference aborts for gcd(d, 210) = 30 and SL > 30,583."""
+    return math.gcd(d, 210) == 30 and sl > 30583
+
+
+def _mix_entry(job) -> dict:
+    name, p, d, ms, mi, sl, mp, flags, source = job
+    binary = REF_FIX if _needs_wheelfix(d, sl) else REF_BIN
+    data, dt = run_ref(binary, p, d, ms, mi, sl, mp, flags)
+    return {
+        "name": name, "p": p, "d": d, "mstart": ms, "minc": mi, "sieve_length": sl,
+        "max_prime": mp * 1_000_000,
+        "compression": 1 if "--rle" in flags else 2 if "--bitcompressed" in flags else 0,
+        "md5": hashlib.md5(data).hexdigest(), "bytes": len(data),
+        "source": source + (" (wheel-fixed copy)" if binary == REF_FIX else ""),
+        "ref_seconds_1t": round(dt, 3),
+    }
+
+
+def make_mix(workers: int) -> None:
+    sys.path.insert(0, str(ROOT / "prime-gap_gb300"))
+    import workloads
+
+    jobs = []
+    for i, j in enumerate(workloads.mixed_jobs(64, seed=4)):
+        assert j.max_prime % 1_000_000 == 0 and j.compression == 0
+        jobs.append((f"mix64_{i:02d}", j.p, j.d, j.mstart, j.minc, j.sieve_length, j.max_prime // 1_000_000,
+                     [], "reference run, workloads.mixed_jobs(64, seed=4)"))
+    jobs += [(*w, "reference run, primes past 2^32") for w in WIDE_JOBS]
+    # longest first so the pool's tail is short
+    jobs.sort(key=lambda t: -(t[4] * t[5] * math.log(t[6]) + 30 * t[6] * t[1] / 1000))
+    out = {}
+    with cf.ProcessPoolExecutor(max_workers=workers) as ex:
+        for e in ex.map(_mix_entry, jobs):
+            out[e.pop("name")] = e
+            print(f"{len(out):3d}/{len(jobs)} {e['md5']} {e['bytes']:>10d} B {e['ref_seconds_1t']:8.2f} s",
+                  flush=True)
+    ordered = {k: out[k] for k in sorted(out)}
+    MIX_OUT.write_text(json.dumps(ordered, indent=1) + "\n")
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--with-large", action="store_true")
+    ap.add_argument("--mix", action="store_true")
+    ap.add_argument("-j", type=int, default=8)
     a = ap.parse_args()
+    if a.mix:
+        make_mix(a.j)
+        return
     jobs = JOBS + (LARGE_JOBS if a.with_large else [])
     old = json.loads(OUT.read_text()) if OUT.exists() else {}
     out = {}

@@ -2,12 +2,14 @@
 (tests/golden/cli.json, made by tests/golden/make_cli_goldens.py from the
 reference built in oracle/_ref): set_defaults -- the d optimizer, the
 automatic sieve length and max_prime (combined_sieve.cpp:160-344) -- and
-main()'s validation (combined_sieve.cpp:86-135).  None of these cases reaches
-the device: the runs that go on to sieve are compared on the lines printed
-before it."""
+main()'s validation (combined_sieve.cpp:86-135).  None of these cases sieves:
+the CLI runs with no visible device, so the runs that would go on to sieve
+(the automatic max_prime cases reach 1e11) stop with exit 1 at context
+creation, and are compared on the lines printed before it."""
 from __future__ import annotations
 
 import json
+import os
 import subprocess
 from pathlib import Path
 
@@ -26,13 +28,10 @@ def _auto(lines):
 def test_cli_matches_reference_before_sieving(built, tmp_path, name):
     case = CASES[name]
     (tmp_path / "unknowns").mkdir()
-    p = subprocess.Popen(["stdbuf", "-oL", str(CLI), *case["args"].split()], cwd=tmp_path,
-                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
-    try:
-        out, _ = p.communicate(timeout=120)
-    except subprocess.TimeoutExpired:  # a device run sieving to 1e11
-        p.kill()
-        out, _ = p.communicate()
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")  # no device: nothing sieves
+    p = subprocess.run(["stdbuf", "-oL", str(CLI), *case["args"].split()], cwd=tmp_path, env=env,
+                       stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True, timeout=120)
+    out = p.stdout
     lines = out.splitlines()
     if case["compare"] == "all":
         assert lines == case["lines"]

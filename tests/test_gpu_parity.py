@@ -51,6 +51,17 @@ def test_config2_full_size_matches_reference(sieve, goldens):
     assert hashlib.md5(data).hexdigest() == g["md5"]
 
 
+def test_config3_full_size_matches_reference(sieve, goldens):
+    """Config 3 (P=3001, d=2190, minc=1e5, SL=4e4, max_prime=1e10): 2.52e8 of
+    its 4.55e8 primes lie above 2^32 (64-bit K mod p and walk starts).  The
+    golden is the reference's --method1 file (its method2 aborts on this job,
+    combined_sieve.cpp:1229; the two methods write the same bytes)."""
+    g = goldens["config3"]
+    data = sieve.method2(_spec(g))
+    assert hashlib.md5(data).hexdigest() == g["md5"]
+    assert len(data) == g["bytes"]
+
+
 def _random_jobs(n, seed):
     rng = random.Random(seed)
     jobs = []
