@@ -44,6 +44,7 @@ WORKLOADS = {
                     max_prime=10_000_000_000),
 }
 GOLDEN = ROOT / "tests" / "golden" / "goldens.json"
+MIX_GOLDEN = ROOT / "tests" / "golden" / "mix_goldens.json"
 PROFILE_TRAFFIC = ROOT / "profiles" / "large_kernel_traffic.txt"
 
 
@@ -124,9 +125,10 @@ def _traffic_per_launch() -> float | None:
     return None
 
 
-def _cpu_sample(job: dict, threads: int, rows_fraction: float = 0.1) -> dict:
-    """The oracle port of the reference's method2 on a bounded sample of the
-    workload (the first minc/10 values of m): pairs/s on all host threads."""
+def _cpu_sample(job: dict, threads: int, rows_fraction: float = 1.0) -> dict:
+    """The oracle port of the reference's method2 on the workload (the whole
+    job by default; rows_fraction < 1 keeps only the first part of m, for
+    warm-up): pairs/s on all host threads."""
     import pgo
 
     minc = max(1, int(job["minc"] * rows_fraction))
@@ -136,8 +138,18 @@ def _cpu_sample(job: dict, threads: int, rows_fraction: float = 0.1) -> dict:
                 threads=threads)
     dt = time.perf_counter() - t
     primes = _count_primes(pl["prime_limit"])
+    what = "whole job" if minc == job["minc"] else f"first {rows_fraction:.0%} of m (minc={minc})"
     return {"seconds": dt, "pairs": pl["valid_ms"] * primes, "primes": primes,
-            "sample": f"{job} with minc={minc} (first {rows_fraction:.0%} of m)"}
+            "sample": f"{job}: {what}"}
+
+
+def _percentiles(ms: list[float]) -> dict:
+    """p50/p99 (nearest rank) of per-step times in ms."""
+    v = sorted(ms)
+    if not v:
+        return {}
+    rank = lambda q: v[min(len(v) - 1, max(0, int(round(q * len(v) + 0.5)) - 1))]
+    return {"p50": rank(0.50), "p99": rank(0.99), "min": v[0], "max": v[-1], "n": len(v)}
 
 
 _PI = {100_000_000: 5_761_455, 2_000_000_000: 98_222_287, 10_000_000_000: 455_052_511}
@@ -217,38 +229,51 @@ def run_reference(args, rank, world):
         print(json.dumps(line), flush=True)
         return 0
     if args.workload in ("batch64", "served"):
+        # every job of the 64-job mix, one after another on all host threads
         import workloads
 
-        jobs = workloads.mixed_jobs(64, seed=4)[:3]
+        jobs = workloads.mixed_jobs(64, seed=4)
         _cpu_sample_jobs(jobs[:1], threads, 0.02)
-        r = _cpu_sample_jobs(jobs, threads)
+        steps = []
+        r = None
+        for _ in range(max(1, args.steps)):
+            r = _cpu_sample_jobs(jobs, threads)
+            steps.append(r)
+        secs = sum(x["seconds"] for x in steps)
+        value = sum(x["pairs"] for x in steps) / secs
+        r = dict(r, value=value)
         line = {
-            "impl": "reference", "metric": "method2 sieve (m,p) pairs/s", "value": r["value"],
-            "unit": "pairs/s", "n_gpus": world, "steps": 1, "warmup": 1,
-            "ms_per_step": r["seconds"] * 1e3, "higher_is_better": True, "scaling": "weak",
+            "impl": "reference", "metric": "method2 sieve (m,p) pairs/s", "value": value,
+            "unit": "pairs/s", "n_gpus": world, "steps": len(steps), "warmup": 1,
+            "ms_per_step": secs / len(steps) * 1e3, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "u32/u64 integer", "data": "synthetic",
-            "config": {"workload": args.workload, "jobs": "first 3 of the 64-job mix (seed 4)"},
-            "cpu_baseline": r,
-            "e2e": {"value": r["value"], "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "config": {"workload": args.workload, "jobs": len(jobs), "seed": 4},
+            "same_config": True, "cpu_baseline": r,
+            "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         }
         print(json.dumps(line), flush=True)
         return 0
     job = WORKLOADS[args.workload]
+    # warm-up: a 1% slice of m (loads the oracle and its threads); every
+    # timed step is the whole job, the same config as the device arm
     for _ in range(args.warmup):
-        _cpu_sample(job, threads)
-    secs, pairs, sample = 0.0, 0, ""
+        _cpu_sample(job, threads, 0.01)
+    secs, pairs, sample, per_step = 0.0, 0, "", []
     for _ in range(args.steps):
         r = _cpu_sample(job, threads)
         secs += r["seconds"]
         pairs += r["pairs"]
         sample = r["sample"]
+        per_step.append(r["seconds"] * 1e3)
     value = pairs / secs
     line = {
         "impl": "reference", "metric": "method2 sieve (m,p) pairs/s", "value": value,
         "unit": "pairs/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": secs / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u32/u64 integer", "data": "synthetic",
-        "config": {"workload": args.workload, **job},
+        "config": {"workload": args.workload, **job}, "same_config": True,
+        "warmup_sample": "first 1% of m per warm-up step",
+        "latency_ms": _percentiles(per_step),
         "cpu_baseline": {"value": value, "unit": "pairs/s", "cores": threads, "kind": "port",
                          "sample": sample},
         "e2e": {"value": value, "unit": "pairs/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -340,7 +365,8 @@ def run_gb300(args, rank, world, local):
            + 4 * plan["valid_ms"] + 2 * spec.sieve_length)
     e2e = {"value": pairs_per_step * world * args.steps / e2e_total, "unit": "pairs/s",
            "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(out_len + 64),
-           "ms_per_step": e2e_total / args.steps * 1e3}
+           "ms_per_step": e2e_total / args.steps * 1e3,
+           "latency_ms": _percentiles([x * 1e3 for x in e2e_s])}
 
     # roofline of the dominant kernel (large-prime marks): integer-pipe bound.
     # Algorithmic integer ops per launch: 8 per continued-fraction level and
@@ -375,7 +401,8 @@ def run_gb300(args, rank, world, local):
     if world == 1 and not args.no_cpu:
         r = _cpu_sample(job, os.cpu_count() or 1)
         cpu = {"value": r["pairs"] / r["seconds"], "unit": "pairs/s", "cores": os.cpu_count(),
-               "kind": "port", "sample": r["sample"], "seconds": round(r["seconds"], 2)}
+               "kind": "port", "sample": r["sample"], "seconds": round(r["seconds"], 2),
+               "same_config": True}
     line = {
         "metric": "method2 sieve (m,p) pairs/s", "value": value, "unit": "pairs/s",
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -384,6 +411,7 @@ def run_gb300(args, rank, world, local):
         "config": {"workload": args.workload, **WORKLOADS[args.workload],
                    "l2": "flushed between steps (256 MiB write)", "parallelism": f"replicas x{world}"},
         "primes_per_s": primes_per_s, "bit_exact": bit_exact, "output_md5": md5,
+        "latency_ms": _percentiles(step_ms),
         "stage_ms_per_step": {k: v / args.steps for k, v in stage_sum.items()},
         "e2e": e2e, "roofline": roofline, "roofline_int": roofline_int, "cpu_baseline": cpu,
         "clocks": clock_info,
@@ -437,7 +465,8 @@ def _rank_job(job: dict, rank: int) -> dict:
     return dict(job, mstart=job["mstart"] + rank * job["minc"])
 
 
-def _cpu_sample_jobs(jobs, threads: int, rows_fraction: float = 0.1) -> dict:
+def _cpu_sample_jobs(jobs, threads: int, rows_fraction: float = 1.0) -> dict:
+    """The oracle on each of `jobs` in turn (whole jobs by default)."""
     secs, pairs, parts = 0.0, 0, []
     for j in jobs:
         r = _cpu_sample(dict(p=j.p, d=j.d, mstart=j.mstart, minc=j.minc, sieve_length=j.sieve_length,
@@ -446,9 +475,25 @@ def _cpu_sample_jobs(jobs, threads: int, rows_fraction: float = 0.1) -> dict:
         pairs += r["pairs"]
         parts.append(f"P={j.p} d={j.d} minc={max(1, int(j.minc * rows_fraction))} SL={j.sieve_length} "
                      f"max_prime={j.max_prime}")
-    return {"value": pairs / secs, "unit": "pairs/s", "cores": threads, "kind": "port",
-            "sample": f"first {rows_fraction:.0%} of the m of {len(jobs)} mix jobs: " + "; ".join(parts),
+    what = "whole jobs" if rows_fraction >= 1 else f"first {rows_fraction:.0%} of the m"
+    return {"value": pairs / secs, "unit": "pairs/s", "cores": threads, "kind": "port", "pairs": pairs,
+            "sample": f"{what} of {len(jobs)} mix jobs" + (": " + "; ".join(parts) if len(parts) <= 4 else ""),
             "seconds": round(secs, 2)}
+
+
+def _mix_reference_md5(jobs) -> dict:
+    """Reference md5 of each job of the seed-4 mix (tests/golden/mix_goldens.json),
+    keyed by job index; jobs whose parameters differ are left out."""
+    if not MIX_GOLDEN.exists():
+        return {}
+    g = json.loads(MIX_GOLDEN.read_text())
+    out = {}
+    for i, j in enumerate(jobs):
+        e = g.get(f"mix64_{i:02d}")
+        if e and (e["p"], e["d"], e["mstart"], e["minc"], e["sieve_length"], e["max_prime"]) == (
+                j.p, j.d, j.mstart, j.minc, j.sieve_length, j.max_prime):
+            out[i] = e["md5"]
+    return out
 
 
 def run_batch(args, rank, world, local):
@@ -481,6 +526,13 @@ def run_batch(args, rank, world, local):
             e1.record(ext)
         e1.synchronize()
         plain_ms += e0.elapsed_time(e1)
+    # the plain path's stages summed over the jobs (one more pass, timed per stage)
+    plain_stages: dict[str, float] = {}
+    for p in preps:
+        p.run(True)
+        st, _ = p.stage_ms()
+        for k, v in st.items():
+            plain_stages[k] = plain_stages.get(k, 0.0) + v
     plain_md5 = []
     for p in preps:
         plain_md5.append(hashlib.md5(p.fetch()).hexdigest())
@@ -504,11 +556,16 @@ def run_batch(args, rank, world, local):
     total_ms = _max_over_ranks(torch, dist, local, sum(step_ms))
     pairs = 0
     bit_exact = True
+    batch_md5 = []
     for i in range(len(jobs)):
         with batch.fetch_view(i) as v:
             pairs += _pairs(v.res)
-            bit_exact &= hashlib.md5(v.bytes()).hexdigest() == plain_md5[i]
+            batch_md5.append(hashlib.md5(v.bytes()).hexdigest())
+            bit_exact &= batch_md5[-1] == plain_md5[i]
     batch.close()
+    ref_md5 = _mix_reference_md5(jobs)
+    vs_ref = ({"checked": len(ref_md5), "equal": sum(batch_md5[i] == m for i, m in ref_md5.items())}
+              if ref_md5 else None)
     value = pairs * world * args.steps / (total_ms * 1e-3)
 
     # end to end: pgs_method2_batch (tables up, every text down) per step
@@ -546,8 +603,10 @@ def run_batch(args, rank, world, local):
                    "l2": "flushed between steps (256 MiB write); prime table 760 MB > L2",
                    "parallelism": f"replicas x{world}"},
         "plain_ms_per_batch": plain_ms, "plain_pairs_per_s": pairs * world / (plain_ms * 1e-3),
+        "plain_stage_ms_sum": plain_stages,
         "batched_vs_plain": plain_ms / (total_ms / args.steps),
-        "table_setup_s": table_s, "bit_exact_vs_plain": bit_exact,
+        "latency_ms": _percentiles(step_ms),
+        "table_setup_s": table_s, "bit_exact_vs_plain": bit_exact, "bit_exact_vs_reference": vs_ref,
         "e2e": {"value": pairs * world * args.steps / e2e_s, "unit": "pairs/s",
                 "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(out_bytes),
                 "ms_per_step": e2e_s / args.steps * 1e3},
@@ -783,9 +842,20 @@ def run_served(args, rank, world, local):
     rng = random.Random(1000 + rank)
     jobs = [workloads.mixed_job(rng) for _ in range(args.requests)]
     arrivals = workloads.poisson_arrivals(len(jobs), rate, seed=7 + rank)
-    check = set(random.Random(3).sample(range(len(jobs)), min(48, len(jobs))))
-    want = {i: hashlib.md5(sieve.method2(jobs[i])).hexdigest() for i in check}
-    got = {}
+    import concurrent.futures
+
+    hasher = concurrent.futures.ThreadPoolExecutor(max_workers=8)  # md5 releases the GIL
+
+    def md5_close(v):
+        try:
+            return hashlib.md5(v.view).hexdigest()
+        finally:
+            v.close()
+
+    # every request's result alone on the plain path, hashed off the main thread
+    want_f = [hasher.submit(md5_close, sieve.method2_view(j)) for j in jobs]
+    want = [f.result() for f in want_f]
+    got_f = [None] * len(jobs)
     pairs = 0
     barrier_t = torch.cuda.synchronize
     barrier_t()
@@ -811,17 +881,16 @@ def run_served(args, rank, world, local):
             while tickets[i] is None:
                 time.sleep(0.0002)
             v, ms = srv.wait_view(tickets[i], timeout_ms=600_000)
-            with v:
-                pairs += _pairs(v.res)
-                if i in check:
-                    got[i] = v.bytes()  # hashed after the run
+            pairs += _pairs(v.res)
+            got_f[i] = hasher.submit(md5_close, v)  # hashed and freed by the pool
             lat.append(ms)
         th.join()
         wall = time.perf_counter() - t0
         st = srv.stats()
         clock_info = clocks.stop()
     wall = _max_over_ranks(torch, dist, local, wall)
-    got = {i: hashlib.md5(b).hexdigest() for i, b in got.items()}
+    got = [f.result() for f in got_f]
+    hasher.shutdown()
     if rank != 0:
         return 0
     lat.sort()
@@ -836,8 +905,9 @@ def run_served(args, rank, world, local):
         "jobs_per_s": len(jobs) * world / wall,
         "latency_ms": {"p50": lat[len(lat) // 2], "p99": lat[min(len(lat) - 1, int(0.99 * len(lat)))],
                        "mean": sum(lat) / len(lat), "max": lat[-1]},
-        "server": st, "bit_exact_sample": {"checked": len(check),
-                                           "equal": sum(got[i] == want[i] for i in check)},
+        "server": st, "bit_exact_vs_plain": {"checked": len(jobs),
+                                             "equal": sum(g == w for g, w in zip(got, want))},
+        "bit_exact_all": got == want,
         "table_setup_s": table_s, "clocks": clock_info,
         "e2e": {"value": pairs * world / wall, "unit": "pairs/s", "h2d_bytes_per_step": None,
                 "d2h_bytes_per_step": None},
