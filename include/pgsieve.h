@@ -304,7 +304,10 @@ int pgs_modulo_search(pgs_ctx *ctx, const uint64_t *p, const uint64_t *a, const 
  * Every mi < max_mi with (base_r*(M+mi) + SL) mod prime <= 2*SL, ascending,
  * with that residue (replaces modulo_search_euclid_all_large,
  * modulo_search.cpp:339-376).  Needs prime > 4*SL + 2.  Writes up to cap
- * pairs and the total count.
+ * pairs and the total count.  The walk after the first hit is spread over
+ * the grid (runs of steps started from their closed form), so a prime just
+ * above 4*SL + 2 with max_mi near 2^32 takes milliseconds, not one thread's
+ * 10^9 steps.
  */
 int pgs_large_hits(pgs_ctx *ctx, uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t prime,
                    uint64_t base_r, uint32_t *mi_out, uint64_t *mod_out, size_t cap,
@@ -327,7 +330,9 @@ int pgs_large_hits(pgs_ctx *ctx, uint64_t M, uint32_t max_mi, uint32_t SL, uint6
  * (cudaGetSymbolAddress, which may load the module): make that first call
  * before any stream capture on the device.  The buffer is shared by every
  * context on a device: calls that overlap in time race on it, so serialise
- * them (calls on one context are serialised by the context).
+ * them (calls on one context are serialised by the context).  The cached
+ * address, like every context's streams and buffers, does not survive a
+ * cudaDeviceReset: do not reset a device while the library is in use on it.
  */
 int pgs_large_hits_static(pgs_ctx *ctx, uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t prime,
                           uint64_t base_r, uint32_t *mi_out, uint64_t *mod_out, size_t cap,

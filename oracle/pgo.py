@@ -165,6 +165,14 @@ def all_large(M, max_mi, SL, prime, base_r, cap=1 << 20) -> list[tuple[int, int]
     return list(zip(mi[:k], md[:k]))
 
 
+def all_large_count(M, max_mi, SL, prime, base_r) -> int:
+    """Number of hits of modulo_search_euclid_all_large (none stored)."""
+    lib = load()
+    mi = (ctypes.c_uint32 * 1)()
+    md = (ctypes.c_uint64 * 1)()
+    return int(lib.pgo_modulo_search_all_large(M, max_mi, SL, prime, base_r, mi, md, 0))
+
+
 def trial_division(job: dict, ms: list[int], xs: list[int], threads=8) -> list[int]:
     """Smallest prime <= the sieve limit dividing m*K + X, or 0."""
     lib = load()

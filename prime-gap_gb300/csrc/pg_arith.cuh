@@ -788,4 +788,62 @@ PG_HD void enumerate_hits_cf(T p, T a, T y0, uint64_t mi_lo, uint64_t mi_hi, T t
     }
 }
 
+// ---------------------------------------------------------------------------
+// one prime's hits (modulo_search_euclid_all_large) spread over the grid.
+// The continued fraction gives the first hit (mi0, y0) and the rotation
+// after it: by `up` on a circle of C = up + dn points, a step costing kp
+// (no wrap) or kn (wrap) in mi, every point below w = 2*SL+1 a hit.  Step n
+// has the closed form Y = y0 + n*up, W = floor(Y / C) wraps, residue Y - W*C,
+// mi = mi0 + (n - W)*kp + W*kn, so threads start their runs of steps
+// anywhere.  Every CTA redoes the O(log p) set-up.
+struct HitWalk {
+    uint64_t mi0, y0, up, dn, kp, kn, w;
+    uint64_t steps;  // upper bound on the steps with mi < max_mi
+};
+
+PG_HD bool hit_walk(uint64_t M, uint32_t max_mi, uint32_t sl, uint64_t p, uint64_t r, HitWalk &hw) {
+    const uint64_t w = 2ull * sl + 1;
+    uint64_t y;  // y(0) = (r*M + SL) mod p
+    if (p < 0xFFFFFFFFull) {
+        y = (((M % p) * r) % p + sl) % p;
+    } else {
+        y = mulmod_u64(M % p, r, p, 1.0 / (double)p) + sl;
+        if (y >= p) y -= p;
+    }
+    const Entry<uint64_t> e = first_entry<uint64_t>(p, r, w, y, max_mi);
+    if (e.t >= max_mi || e.y >= w) return false;
+    hw = HitWalk{e.t, e.y, e.g.up, e.g.dn, e.g.kp, e.g.kn, w,
+                 rotation_steps_bound<uint64_t>(e.t, max_mi, e.g, p)};
+    return true;
+}
+
+// Position of rotation step n, mi clamped to mi_hi (a walk stops there).
+PG_HD void hit_walk_at(const HitWalk &hw, uint64_t n, uint64_t mi_hi, uint64_t &mi, uint64_t &y) {
+    const uint64_t C = hw.up + hw.dn;
+    const unsigned __int128 Y = (unsigned __int128)n * hw.up + hw.y0;
+    const uint64_t W = (uint64_t)(Y / C);  // W <= n: y0 < C and up < C
+    y = (uint64_t)(Y - (unsigned __int128)W * C);
+    const unsigned __int128 m =
+        (unsigned __int128)hw.mi0 + (unsigned __int128)(n - W) * hw.kp + (unsigned __int128)W * hw.kn;
+    mi = m < mi_hi ? (uint64_t)m : mi_hi;
+}
+
+// Walks up to `len` steps from (mi, y) while mi < mi_hi; calls emit(mi, y)
+// at each hit and returns the number of hits.
+template <typename Emit>
+PG_HD uint32_t hit_walk_run(const HitWalk &hw, uint64_t mi, uint64_t y, uint64_t len, uint64_t mi_hi,
+                                 Emit emit) {
+    uint32_t n = 0;
+    for (uint64_t k = 0; k < len && mi < mi_hi; k++) {
+        if (y < hw.w) {
+            emit(mi, y);
+            n++;
+        }
+        const bool wrap = y >= hw.dn;
+        y = wrap ? y - hw.dn : y + hw.up;
+        mi += wrap ? hw.kn : hw.kp;
+    }
+    return n;
+}
+
 }  // namespace pg

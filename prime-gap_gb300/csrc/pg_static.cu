@@ -6,7 +6,9 @@
 // allocating library call.  Its address comes from cudaGetSymbolAddress,
 // looked up once per device (with that device current) on the first call and
 // cached; that first lookup may load the module, so the first call on a
-// device belongs before any stream capture on it.
+// device belongs before any stream capture on it.  A cudaDeviceReset
+// invalidates the cached address (as it does every context's streams and
+// buffers): the library does not support a reset while it is in use.
 //
 // Limit: at most kStaticHitsMax hits are returned per call (cap above it is
 // rejected with PGS_EINVAL).  The buffer is shared by every context on the

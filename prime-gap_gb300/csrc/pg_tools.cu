@@ -1,7 +1,9 @@
 // Device batches of the reference's number-theory primitives, exposed through
 // the C ABI for callers that need them one by one (and for parity tests):
 // K mod q over an explicit prime list, the Euclid modulo search, and the hit
-// enumeration of one prime.
+// enumeration of one prime (its steps spread over the grid).
+#include <algorithm>
+
 #include "pg_arith.cuh"
 #include "pg_internal.h"
 
@@ -29,36 +31,76 @@ __global__ void modsearch_kernel(const uint64_t *p, const uint64_t *a, const uin
     k[i] = modsearch64(p[i], a[i], l[i], r[i]).k;
 }
 
-struct Collect {
-    uint32_t *mi_out;
-    uint64_t *mod_out;
-    size_t cap;
-    size_t n;
-    __device__ void operator()(uint64_t mi, uint64_t y) {
-        if (n < cap) {
-            mi_out[n] = (uint32_t)mi;
-            mod_out[n] = y;
-        }
-        n++;
-    }
-};
+constexpr int kHitThreads = 256;
 
-__global__ void large_hits_kernel(uint64_t M, uint32_t max_mi, uint32_t sl, uint64_t p,
-                                  uint64_t r, uint32_t *mi_out, uint64_t *mod_out, size_t cap,
-                                  unsigned long long *count) {
-    Collect c{mi_out, mod_out, cap, 0};
-    const uint64_t two_sl = 2ull * sl;
-    if (p < 0xFFFFFFFFull) {
-        uint32_t p32 = (uint32_t)p, r32 = (uint32_t)r;
-        // y(0) = (r*M + SL) mod p
-        uint32_t y = (uint32_t)((((M % p32) * (uint64_t)r32) % p32 + sl) % p32);
-        enumerate_hits_cf<uint32_t>(p32, r32, y, 0, max_mi, (uint32_t)two_sl, c);
-    } else {
-        uint64_t y = mulmod_u64(M % p, r, p, 1.0 / (double)p) + sl;
-        if (y >= p) y -= p;
-        enumerate_hits_cf<uint64_t>(p, r, y, 0, max_mi, two_sl, c);
+// Total number of hits: every thread counts one run of consecutive steps.
+__global__ void __launch_bounds__(kHitThreads)
+    large_hits_count_kernel(uint64_t M, uint32_t max_mi, uint32_t sl, uint64_t p, uint64_t r,
+                            unsigned long long *count) {
+    __shared__ HitWalk s_hw;
+    __shared__ int s_ok;
+    __shared__ unsigned long long s_sum;
+    if (threadIdx.x == 0) {
+        s_ok = hit_walk(M, max_mi, sl, p, r, s_hw);
+        s_sum = 0;
     }
-    *count = c.n;
+    __syncthreads();
+    if (!s_ok) return;
+    const HitWalk hw = s_hw;
+    const uint64_t threads = (uint64_t)gridDim.x * kHitThreads;
+    const uint64_t run = (hw.steps + threads - 1) / threads;
+    const uint64_t n0 = ((uint64_t)blockIdx.x * kHitThreads + threadIdx.x) * run;
+    uint32_t c = 0;
+    if (n0 < hw.steps) {
+        uint64_t mi, y;
+        hit_walk_at(hw, n0, max_mi, mi, y);
+        c = hit_walk_run(hw, mi, y, min(run, hw.steps - n0), max_mi, [](uint64_t, uint64_t) {});
+    }
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_down_sync(0xffffffffu, c, o);
+    if ((threadIdx.x & 31) == 0 && c) atomicAdd(&s_sum, (unsigned long long)c);
+    __syncthreads();
+    if (threadIdx.x == 0 && s_sum) atomicAdd(count, s_sum);
+}
+
+// The first `cap` hits in ascending mi, written in order by one CTA.  No two
+// consecutive steps miss (a miss y >= w > dn wraps to y - dn < up + dn - dn
+// < w), so the first 2*cap + 2 steps hold more than cap hits.
+__global__ void __launch_bounds__(kHitThreads)
+    large_hits_write_kernel(uint64_t M, uint32_t max_mi, uint32_t sl, uint64_t p, uint64_t r,
+                            uint32_t *mi_out, uint64_t *mod_out, uint64_t cap) {
+    __shared__ HitWalk s_hw;
+    __shared__ int s_ok;
+    __shared__ uint32_t s_warp[kHitThreads / 32];
+    if (threadIdx.x == 0) s_ok = hit_walk(M, max_mi, sl, p, r, s_hw);
+    __syncthreads();
+    if (!s_ok) return;
+    const HitWalk hw = s_hw;
+    const uint64_t span = min(hw.steps, 2 * cap + 2);
+    const uint64_t run = (span + kHitThreads - 1) / kHitThreads;
+    const uint64_t n0 = (uint64_t)threadIdx.x * run;
+    const uint64_t len = n0 < span ? min(run, span - n0) : 0;
+    uint64_t mi = 0, y = 0;
+    if (len) hit_walk_at(hw, n0, max_mi, mi, y);
+    const uint32_t c = len ? hit_walk_run(hw, mi, y, len, max_mi, [](uint64_t, uint64_t) {}) : 0u;
+    // exclusive scan of the runs' hit counts, in step order
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    if (lane == 31) s_warp[warp] = incl;
+    __syncthreads();
+    uint64_t pos = incl - c;
+    for (uint32_t k = 0; k < warp; k++) pos += s_warp[k];
+    if (len && pos < cap)
+        hit_walk_run(hw, mi, y, len, max_mi, [&](uint64_t m, uint64_t v) {
+            if (pos < cap) {
+                mi_out[pos] = (uint32_t)m;
+                mod_out[pos] = v;
+            }
+            pos++;
+        });
 }
 
 // Independent IMAD chains: 8 per thread, 16-way unrolled.
@@ -135,7 +177,16 @@ cudaError_t tools_modsearch(const uint64_t *p, const uint64_t *a, const uint64_t
 cudaError_t tools_large_hits(uint64_t M, uint32_t max_mi, uint32_t sl, uint64_t p, uint64_t r,
                              uint32_t *mi_out, uint64_t *mod_out, size_t cap,
                              unsigned long long *count, cudaStream_t stream) {
-    large_hits_kernel<<<1, 1, 0, stream>>>(M, max_mi, sl, p, r, mi_out, mod_out, cap, count);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // steps <= max_mi: at most one run of 64 steps per thread, four CTAs per SM
+    const uint64_t want = ((uint64_t)max_mi + 64 * kHitThreads - 1) / (64 * kHitThreads);
+    const unsigned blocks = (unsigned)std::max<uint64_t>(1, std::min<uint64_t>(want, 4ull * std::max(sms, 1)));
+    cudaError_t e = cudaMemsetAsync(count, 0, sizeof(unsigned long long), stream);
+    if (e) return e;
+    large_hits_count_kernel<<<blocks, kHitThreads, 0, stream>>>(M, max_mi, sl, p, r, count);
+    if (cap) large_hits_write_kernel<<<1, kHitThreads, 0, stream>>>(M, max_mi, sl, p, r, mi_out, mod_out, cap);
     return cudaGetLastError();
 }
 

@@ -258,4 +258,38 @@ uint64_t ah_mulmod(uint64_t a, uint64_t b, uint64_t p) { return pg::mulmod_u64(a
 uint32_t ah_redc32(uint64_t t, uint32_t p) { return pg::redc32(t, p, pg::neg_inv32(p)); }
 uint32_t ah_neg_inv32(uint32_t p) { return pg::neg_inv32(p); }
 
+// The grid form of pgs_large_hits (pg_tools.cu) run serially: the total
+// from `threads` runs of consecutive steps, and the first `cap` hits written
+// in order from the first 2*cap + 2 steps split over `cta` runs.  Returns
+// the total count.
+size_t ah_hits_grid(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint64_t r, uint64_t threads,
+                    uint64_t cta, uint32_t *mi_out, uint64_t *mod_out, size_t cap) {
+    pg::HitWalk hw;
+    if (!pg::hit_walk(M, max_mi, SL, p, r, hw)) return 0;
+    size_t total = 0;
+    const uint64_t run = (hw.steps + threads - 1) / threads;
+    for (uint64_t t = 0; t < threads; t++) {
+        const uint64_t n0 = t * run;
+        if (n0 >= hw.steps) break;
+        uint64_t mi, y;
+        pg::hit_walk_at(hw, n0, max_mi, mi, y);
+        total += pg::hit_walk_run(hw, mi, y, run < hw.steps - n0 ? run : hw.steps - n0, max_mi,
+                                  [](uint64_t, uint64_t) {});
+    }
+    const uint64_t span = hw.steps < 2 * (uint64_t)cap + 2 ? hw.steps : 2 * (uint64_t)cap + 2;
+    const uint64_t wrun = (span + cta - 1) / cta;
+    uint64_t pos = 0;
+    for (uint64_t t = 0; t < cta && cap; t++) {
+        const uint64_t n0 = t * wrun;
+        if (n0 >= span) break;
+        uint64_t mi, y;
+        pg::hit_walk_at(hw, n0, max_mi, mi, y);
+        pg::hit_walk_run(hw, mi, y, wrun < span - n0 ? wrun : span - n0, max_mi, [&](uint64_t m, uint64_t v) {
+            if (pos < cap) mi_out[pos] = (uint32_t)m, mod_out[pos] = v;
+            pos++;
+        });
+    }
+    return total;
+}
+
 }

@@ -36,6 +36,9 @@ def ah(built):
     lib.ah_hits_items.argtypes = [u64, ctypes.c_uint32, ctypes.c_uint32, u64, u64, ctypes.c_uint32,
                                   ctypes.c_uint32, ctypes.POINTER(ctypes.c_uint32),
                                   ctypes.POINTER(u64), ctypes.c_size_t]
+    lib.ah_hits_grid.restype = ctypes.c_size_t
+    lib.ah_hits_grid.argtypes = [u64, ctypes.c_uint32, ctypes.c_uint32, u64, u64, u64, u64,
+                                 ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
     lib.ah_first_entry.restype = None
     lib.ah_first_entry.argtypes = [u64, u64, u64, u64, ctypes.POINTER(u64)]
     lib.ah_first_entry_lim.restype = None
@@ -381,3 +384,29 @@ def test_mulmod(ah):
         p = _rand_prime(rng, 3, 2**46)
         a, b = rng.randrange(p), rng.randrange(p)
         assert ah.ah_mulmod(a, b, p) == a * b % p
+
+
+@pytest.mark.parametrize("threads,cta,cap", [(1, 1, 1 << 16), (155648, 256, 1 << 16), (7, 3, 1000), (1000, 256, 1),
+                                             (64, 256, 0)])
+def test_hits_grid_split_vs_oracle(ah, threads, cta, cap):
+    """pgs_large_hits' grid form: the total over runs of steps started from
+    the closed form, and the first cap hits written in order from the first
+    2*cap + 2 steps, against the reference enumeration (18- to 45-bit primes,
+    window up to 2e4)."""
+    rng = random.Random(77 + threads + cap)
+    cases = [(1234567, 100000, 5000, 20011, 7919)]
+    for bits in (18, 25, 31, 33, 40, 45):
+        for q in pgo.primes(2 ** (bits - 1), 2 ** (bits - 1) + 3000)[:3]:
+            SL = rng.choice([1000, 5000, 20000])
+            if q <= 4 * SL + 2:
+                continue
+            cases.append((rng.randrange(1, 10**9), rng.choice([1, 999, 100000, 3000000]), SL, q,
+                          rng.randrange(1, q)))
+    for M, max_mi, SL, q, r in cases:
+        want = pgo.all_large(M, max_mi, SL, q, r, cap=1 << 22)
+        mi = (ctypes.c_uint32 * max(1, cap))()
+        md = (ctypes.c_uint64 * max(1, cap))()
+        n = ah.ah_hits_grid(M, max_mi, SL, q, r, threads, cta, mi, md, cap)
+        k = min(n, cap)
+        assert n == len(want), (M, max_mi, SL, q, r)
+        assert list(zip(mi[:k], md[:k])) == [tuple(h) for h in want[:k]], (M, max_mi, SL, q, r)
