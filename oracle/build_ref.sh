@@ -10,7 +10,9 @@
 #                           gap_test_common.cpp)
 # Never built with -DNDEBUG: the reference has side effects inside assert().
 # Needs the runtime libgmp.so.10 and libsqlite3.so.0; exits 0 with a message
-# when the sources or libraries are absent.
+# when the sources or libraries are absent.  The sources are read from
+# PG_REFERENCE_DIR, by default the read-only mount of the build container
+# (this recipe is the one file that names it).
 set -eu
 HERE="$(cd "$(dirname "$0")" && pwd)"
 REF="${PG_REFERENCE_DIR:-/root/reference}"

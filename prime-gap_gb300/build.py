@@ -101,15 +101,12 @@ def build_oracle() -> Path:
 
 def build_reference() -> None:
     """Compile the reference itself from its own sources when they are present
-    (validation only; outputs stay in oracle/_ref)."""
-    script = ORACLE / "build_ref.sh"
-    ref = Path(os.environ.get("PG_REFERENCE_DIR", "/root/reference"))
-    if not (ref / "combined_sieve.cpp").exists():
-        return
+    (validation only; outputs stay in oracle/_ref).  oracle/build_ref.sh finds
+    the sources (PG_REFERENCE_DIR) and skips when they are absent."""
     outs = [ORACLE / "_ref" / name for name in ("combined_sieve", "combined_sieve_wheelfix", "gap_test_simple")]
     if all(o.exists() for o in outs):
         return
-    subprocess.run(["bash", str(script)], check=True, capture_output=True)
+    subprocess.run(["bash", str(ORACLE / "build_ref.sh")], check=True, capture_output=True)
 
 
 def build_arith_host() -> Path:

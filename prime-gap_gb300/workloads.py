@@ -62,3 +62,32 @@ def poisson_arrivals(n: int, rate_per_s: float, seed: int = 5) -> list[float]:
         t += rng.expovariate(rate_per_s)
         out.append(t)
     return out
+
+
+def main(argv: list[str] | None = None) -> int:
+    """python prime-gap_gb300/workloads.py batch64 [--lanes N] [--graph]: one
+    batched run of the 64-job mix over the resident table (a short command to
+    profile the batched path alone); prints the device time."""
+    import argparse
+
+    import pgsieve
+
+    ap = argparse.ArgumentParser()
+    ap.add_argument("workload", choices=["batch64"])
+    ap.add_argument("--lanes", type=int, default=8)
+    ap.add_argument("--graph", action="store_true")
+    a = ap.parse_args(argv)
+    s = pgsieve.Sieve(0)
+    try:
+        s.reserve_table(4_000_000_000)
+        with s.batch(mixed_jobs(64, seed=4), lanes=a.lanes) as b:
+            print(f"batch64: {b.run(graph=a.graph):.2f} ms")
+    finally:
+        s.close()
+    return 0
+
+
+if __name__ == "__main__":
+    import sys
+
+    sys.exit(main())

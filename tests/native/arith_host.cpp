@@ -292,4 +292,10 @@ size_t ah_hits_grid(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint64
     return total;
 }
 
+// Two quotients by one divisor through the shared reciprocal (the
+// continued fraction's division), with the reciprocal moved by `skew` ulps.
+void ah_udiv2(uint32_t n1, uint32_t n2, uint32_t d, int skew, uint32_t *out2) {
+    pg::udiv2_32(n1, n2, d, out2[0], out2[1], skew);
+}
+
 }

@@ -39,6 +39,9 @@ def ah(built):
     lib.ah_hits_grid.restype = ctypes.c_size_t
     lib.ah_hits_grid.argtypes = [u64, ctypes.c_uint32, ctypes.c_uint32, u64, u64, u64, u64,
                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
+    lib.ah_udiv2.restype = None
+    lib.ah_udiv2.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                             ctypes.POINTER(ctypes.c_uint32)]
     lib.ah_first_entry.restype = None
     lib.ah_first_entry.argtypes = [u64, u64, u64, u64, ctypes.POINTER(u64)]
     lib.ah_first_entry_lim.restype = None
@@ -410,3 +413,32 @@ def test_hits_grid_split_vs_oracle(ah, threads, cta, cap):
         k = min(n, cap)
         assert n == len(want), (M, max_mi, SL, q, r)
         assert list(zip(mi[:k], md[:k])) == [tuple(h) for h in want[:k]], (M, max_mi, SL, q, r)
+
+
+def test_udiv2_shared_reciprocal_exact(ah):
+    """The continued fraction's two quotients by one reciprocal equal the
+    exact quotients for every divisor size, small and large quotients (the
+    fast path and the fallback), with the reciprocal moved up to 2 ulps
+    either way (the device's rcp.approx is within 1 ulp)."""
+    rng = random.Random(3)
+    out = (ctypes.c_uint32 * 2)()
+    cases = []
+    for _ in range(40000):
+        d = rng.choice([1, 2, 3, rng.randrange(1, 1 << 8), rng.randrange(1, 1 << 16), rng.randrange(1, 1 << 24),
+                        rng.randrange(1, 1 << 32), (1 << 32) - 1, (1 << 24) + 1, (1 << 31) + 1])
+        qmax = rng.choice([3, 1 << 10, 1 << 17, 1 << 18, 1 << 32])
+        def num():
+            v = rng.randrange(0, qmax) * d + rng.randrange(0, d)
+            return v if v < (1 << 32) else rng.randrange(0, 1 << 32)
+        cases.append((num(), num(), d))
+    # quotients right at the fast-path edge and exact multiples
+    for d in (1, 2, 7, 1000003, 65537):
+        for q in ((1 << 17) - 1, 1 << 17, (1 << 17) + 1, (1 << 18) - 1):
+            for dr in (0, d - 1):
+                n = q * d + dr
+                if n < (1 << 32):
+                    cases.append((n, n, d))
+    for n1, n2, d in cases:
+        for skew in (-2, -1, 0, 1, 2):
+            ah.ah_udiv2(n1, n2, d, skew, out)
+            assert (out[0], out[1]) == (n1 // d, n2 // d), (n1, n2, d, skew)
