@@ -919,6 +919,68 @@ def run_served(args, rank, world, local):
     return 0
 
 
+def run_tune(args, rank, world, local):
+    """The autotuner: each job class of configs 1-3 and of the 64-job mix
+    tuned on this device (pgs_tune: one knob at a time, median of 5 runs),
+    then the mix batched with the default knobs and with the tuned ones."""
+    import torch
+
+    import pgsieve
+    import workloads
+
+    torch.cuda.set_device(local)
+    table = []
+    t0 = time.perf_counter()
+    with pgsieve.Sieve(local, load_tuning=False) as s:
+        for name in ("config1", "config2", "config3"):
+            spec = pgsieve.JobSpec(**WORKLOADS[name])
+            knobs, ms_def, ms_tuned = s.tune(spec, reps=5)
+            table.append({"job": name, "class": pgsieve.tuning_class(spec), "knobs": knobs,
+                          "ms_default": ms_def, "ms_tuned": ms_tuned})
+        jobs = workloads.mixed_jobs(64, seed=4)
+        seen = set()
+        for j in jobs:
+            c = pgsieve.tuning_class(j)
+            if c in seen:
+                continue
+            seen.add(c)
+            knobs, ms_def, ms_tuned = s.tune(j, reps=5)
+            table.append({"job": "mix64", "class": c, "knobs": knobs, "ms_default": ms_def,
+                          "ms_tuned": ms_tuned})
+        tune_s = time.perf_counter() - t0
+        if args.tuning_out:
+            s.tuning_save(args.tuning_out)
+        s.reserve_table(4_000_000_000)
+        with s.batch(jobs, lanes=args.lanes) as b:  # tuned knobs (this context's entries)
+            for _ in range(args.warmup):
+                b.run(graph=True)
+            tuned = [b.run(graph=True) for _ in range(args.steps)]
+            pairs = 0
+            for i in range(len(jobs)):
+                with b.fetch_view(i) as v:
+                    pairs += _pairs(v.res)
+    with pgsieve.Sieve(local, load_tuning=False) as s:
+        s.reserve_table(4_000_000_000)
+        with s.batch(jobs, lanes=args.lanes) as b:
+            for _ in range(args.warmup):
+                b.run(graph=True)
+            default = [b.run(graph=True) for _ in range(args.steps)]
+    mix = [r for r in table if r["job"] == "mix64"]
+    line = {
+        "metric": "method2 sieve (m,p) pairs/s", "value": pairs * args.steps / (sum(tuned) * 1e-3),
+        "unit": "pairs/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sum(tuned) / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "u32/u64 integer", "data": "synthetic",
+        "config": {"workload": "tune", "value_is": "batch64 with tuned knobs"},
+        "batch64_ms": {"default": _percentiles(default), "tuned": _percentiles(tuned)},
+        "tuning_s": tune_s, "classes": len(table),
+        "mix_sum_ms": {"default": sum(r["ms_default"] for r in mix), "tuned": sum(r["ms_tuned"] for r in mix)},
+        "table": table,
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def large_kernel_model_ops(spec, stats, plan) -> float:
     """Model of the large-prime phase's integer work (ops per job).
 
@@ -946,10 +1008,11 @@ def main() -> int:
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default="config2",
-                    choices=sorted(WORKLOADS) + ["batch64", "served", "ingest", "prp"])
+                    choices=sorted(WORKLOADS) + ["batch64", "served", "ingest", "prp", "tune"])
     ap.add_argument("--lanes", type=int, default=8, help="streams of the batched/served paths")
     ap.add_argument("--requests", type=int, default=1000, help="served requests")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline sample")
+    ap.add_argument("--tuning-out", default="", help="tune workload: write the tuning cache file here")
     ap.add_argument("--max-prime", type=int, default=0,
                     help="override the workload's max_prime (small profiling runs)")
     args = ap.parse_args()
@@ -960,6 +1023,11 @@ def main() -> int:
         return run_prp(args, rank, world, local)
     if args.workload in ("batch64", "served") and args.impl == "gb300":
         return (run_batch if args.workload == "batch64" else run_served)(args, rank, world, local)
+    if args.workload == "tune":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the tuner has no CPU counterpart"}))
+            return 0
+        return run_tune(args, rank, world, local)
     if args.max_prime:
         WORKLOADS[args.workload] = dict(WORKLOADS[args.workload], max_prime=args.max_prime)
         args.workload_note = "max_prime overridden"

@@ -338,6 +338,53 @@ int pgs_large_hits_static(pgs_ctx *ctx, uint64_t M, uint32_t max_mi, uint32_t SL
                           uint64_t base_r, uint32_t *mi_out, uint64_t *mod_out, size_t cap,
                           size_t *count);
 
+/*
+ * Tuning: the launch knobs of the sieve kernels, picked per job class by
+ * measurement on the live device.  No counterpart in the reference, whose
+ * nearest analogue is the hand cost model calculate_thresholds_method2
+ * (gap_common.cpp:345-375) choosing its phase thresholds per job.  Every
+ * value gives the same output; only the time changes.
+ */
+typedef struct {
+    uint32_t direct_steps;   /* large-prime walks of at most this many steps run in their
+                                continued-fraction thread (default 24) */
+    uint32_t item_steps;     /* steps per item when a walk is spread over its CTA: 32, 64
+                                or 128 (default 64) */
+    uint32_t heavy_steps;    /* walks of more steps get a CTA of their own (default 4096) */
+    uint32_t rows_per_cta;   /* most rows per CTA of the small-prime kernel, 1..32
+                                (default 16; shared memory may allow fewer) */
+    uint32_t text_chunks;    /* chunks of pgs_method2's rows/text/copy pipeline, 1..4
+                                (default 4) */
+    uint32_t kmod_lsb_limbs; /* K mod p least significant limb first from this many limbs
+                                (default 32) */
+} pgs_tuning;
+
+void pgs_tuning_default(pgs_tuning *out);
+/* The job's tuning class, "P<p>.SL<floor(log2 SL)>.minc<floor(log2 minc)>";
+ * returns the length (without the NUL), or PGS_EINVAL if cap is too small. */
+int pgs_tuning_class(const pgs_job *job, char *buf, size_t cap);
+/* Knobs for the job's class on this context (PGS_EINVAL for values outside
+ * the ranges above).  Jobs prepared afterwards use them. */
+int pgs_tuning_set(pgs_ctx *ctx, const pgs_job *job, const pgs_tuning *t);
+/* The knobs jobs of this class get: returns 1 when the class is tuned, 0
+ * when it gets the defaults. */
+int pgs_tuning_get(pgs_ctx *ctx, const pgs_job *job, pgs_tuning *out);
+/* Load the file's entries for this device (by name); returns how many, or
+ * PGS_EINVAL when the file cannot be read. */
+int pgs_tuning_load(pgs_ctx *ctx, const char *path);
+/* Write this context's entries, keeping other devices' lines of the file. */
+int pgs_tuning_save(pgs_ctx *ctx, const char *path);
+/*
+ * Tune the job's class: the job is prepared once and run `reps` times per
+ * candidate (device time of pgs_run, median; pgs_method2's pipeline for
+ * text_chunks), one knob at a time from the defaults, keeping a change that
+ * is at least 2 % faster; the pick is then timed against the defaults three
+ * times alternately and kept only if it is at least 1 % faster.  Stores and
+ * returns the result, and the median times with the defaults and with it.
+ */
+int pgs_tune(pgs_ctx *ctx, const pgs_job *job, int reps, pgs_tuning *out, double *ms_default,
+             double *ms_tuned);
+
 /* Library version string. */
 const char *pgs_version(void);
 

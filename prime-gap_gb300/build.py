@@ -32,7 +32,7 @@ NVCC_FLAGS = ARCH + [
     f"-I{INCLUDE}", f"-I{CSRC}",
 ]
 CU_SOURCES = ["pg_primes.cu", "pg_kmod.cu", "pg_large.cu", "pg_rows.cu", "pg_tools.cu", "pg_host.cu",
-              "pg_api.cu", "pg_batch.cu", "pg_static.cu", "pg_unknowns.cu", "pg_prp.cu"]
+              "pg_api.cu", "pg_batch.cu", "pg_static.cu", "pg_unknowns.cu", "pg_prp.cu", "pg_tune.cu"]
 
 LIB = BUILD / "libpgsieve.so"
 CLI = BUILD / "combined_sieve"
@@ -40,6 +40,7 @@ GAP_TEST_CLI = BUILD / "gap_test"
 ORACLE_LIB = ORACLE_BUILD / "libm2oracle.so"
 ORACLE_BIN = ORACLE_BUILD / "m2_oracle"
 ARITH_HOST_LIB = BUILD / "libpgarith_host.so"
+TUNE_HOST_LIB = BUILD / "libpgtune_host.so"
 
 
 def _run(cmd: list[str]) -> None:
@@ -119,10 +120,20 @@ def build_arith_host() -> Path:
     return ARITH_HOST_LIB
 
 
+def build_tune_host() -> Path:
+    """Host build of the tuning cache logic, for CPU unit tests."""
+    BUILD.mkdir(parents=True, exist_ok=True)
+    src = TESTS_NATIVE / "tune_host.cpp"
+    if src.exists() and _stale(TUNE_HOST_LIB, [src] + _headers()):
+        _run(["g++", "-O2", "-std=c++17", "-shared", "-fPIC", f"-I{CSRC}", f"-I{INCLUDE}", str(src),
+              "-o", str(TUNE_HOST_LIB)])
+    return TUNE_HOST_LIB
+
+
 def build_all(jobs: int = 8, verbose: bool = False, reference: bool = True) -> None:
     with cf.ThreadPoolExecutor(max_workers=3) as ex:
         futs = [ex.submit(build_lib, jobs, verbose), ex.submit(build_oracle),
-                ex.submit(build_arith_host)]
+                ex.submit(build_arith_host), ex.submit(build_tune_host)]
         if reference:
             futs.append(ex.submit(build_reference))
         for f in futs:

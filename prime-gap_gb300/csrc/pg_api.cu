@@ -40,6 +40,8 @@ int pgs_create(int device, pgs_ctx **out) {
         return PGS_ECUDA;
     }
     ctx->stream = ctx->own;
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, device) == cudaSuccess) ctx->device_name = prop.name;
     *out = ctx;
     return PGS_OK;
 }
@@ -118,6 +120,7 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
         delete pr;
         return rc;
     }
+    pr->tune = tuning_for(ctx, *job);
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     HostJob &h = pr->hj;
@@ -195,7 +198,8 @@ int text_pipeline(pgs_ctx *ctx, pgs_prepared *pr, const pg::RowsDev &rd, uint32_
                   HostText &sink) {
     const uint32_t rows = (uint32_t)pr->hj.valid_mi.size();
     const uint32_t nblk = (rows + rpb - 1) / rpb;
-    const int C = (int)std::min<uint32_t>(kTextChunks, std::max<uint32_t>(nblk, 1));
+    const uint32_t want = std::max<uint32_t>(1, std::min<uint32_t>(kTextChunks, pr->tune.text_chunks));
+    const int C = (int)std::min<uint32_t>(want, std::max<uint32_t>(nblk, 1));
     std::vector<uint32_t> rb(C + 1);
     for (int c = 0; c <= C; c++)
         rb[c] = (uint32_t)std::min<uint64_t>(rows, (uint64_t)nblk * c / C * rpb);
@@ -381,7 +385,7 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
         CK(mark(e_b));
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
                            ctx->win_off.as<uint32_t>(), rng, win.bound, &h.walk, ctx->win_r.p,
-                           ctx->win_t0.p, win.wide, s));
+                           ctx->win_t0.p, win.wide, s, (int)pr->tune.kmod_lsb_limbs));
         CK(mark(e_c));
         CK(pg::large_window(job, win.lo, ctx->win_off.as<uint32_t>(), rng, win.bound, ctx->win_r.p,
                             ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint2>(),
@@ -399,7 +403,7 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
     CK(mark(a));
     if (sink) {
         // rows and text interleave with the copy: one span for both
-        const int rc = text_pipeline(ctx, pr, rd, rows_per_block(h.nb, h.job.compression), s, *sink);
+        const int rc = text_pipeline(ctx, pr, rd, rows_per_block(h.nb, h.job.compression, pr->tune.rows_per_cta), s, *sink);
         if (rc) return rc;
         CK(mark(b));
         span(PGS_STAGE_ROWS, a, b);
@@ -407,7 +411,7 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
         pr->ran = true;
         return PGS_OK;
     }
-    CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression), s));
+    CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression, pr->tune.rows_per_cta), s));
     CK(mark(b));
     span(PGS_STAGE_ROWS, a, b);
     CK(pg::scan_u64(pr->row_bytes.as<uint64_t>(), pr->offsets.as<uint64_t>(), pr->misc.as<uint64_t>(),
@@ -422,6 +426,14 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
 }
 
 }  // namespace
+
+extern "C++" {
+namespace pgh {
+int run_prepared(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
+    return run_job(ctx, pr, record_stages, sink);
+}
+}  // namespace pgh
+}
 
 int pgs_run(pgs_ctx *ctx, pgs_prepared *pr, int record_stages) {
     if (!ctx || !pr || pr->ctx != ctx) return PGS_EINVAL;

@@ -22,6 +22,7 @@
 #include <deque>
 #include <map>
 #include <thread>
+#include <tuple>
 
 #include "pg_host.h"
 
@@ -186,6 +187,7 @@ int prepare_table_job(pgs_ctx *ctx, const pgs_job &job, cudaStream_t s, pgs_prep
         }
     }
     HostJob &h = pr->hj;
+    pr->tune = tuning_for(ctx, job);
     PrimeTable &t = *ctx->table;
     const uint64_t rows = h.valid_mi.size();
     const uint64_t shi = std::min<uint64_t>(h.s1, h.prime_limit);
@@ -366,7 +368,7 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
         rd.sp_base = 0;
         rd.sp_range = pr->misc.as<unsigned long long>() + 1;
         rd.sp_cap = pr->sp_bound;
-        CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression), s));
+        CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression, pr->tune.rows_per_cta), s));
         CK(pg::scan_u64(pr->row_bytes.as<uint64_t>(), pr->offsets.as<uint64_t>(), pr->misc.as<uint64_t>(),
                         rows, pr->scan_tmp.as<uint64_t>(), s));
         CK(pg::format_rows(rd, pr->offsets.as<uint64_t>(), pr->text.as<char>(), s));
@@ -374,17 +376,6 @@ int run_group(pgs_ctx *ctx, const std::vector<pgs_prepared *> &jobs, Lane *lane,
         pr->ran = true;
     }
     return PGS_OK;
-}
-
-int run_table_job(pgs_ctx *ctx, pgs_prepared *pr, Lane *lane) {
-    return run_group(ctx, std::vector<pgs_prepared *>{pr}, lane, nullptr);
-}
-
-uint64_t job_cost(const HostJob &h) {
-    const double lim = (double)h.prime_limit;
-    const double primes = lim / std::log(std::max(lim, 3.0));
-    return (uint64_t)(primes * ((double)h.klimbs.size() + 150.0) +
-                      (double)h.valid_mi.size() * h.H * 2.0);
 }
 
 }  // namespace
@@ -439,65 +430,124 @@ uint64_t gcd64(uint64_t a, uint64_t b) {
     return a;
 }
 
-// Jobs with the same P form a group sharing K' = P#/L (L = lcm of their d)
-// when every L/d fits 32 bits; otherwise jobs group by their exact K.
-// Groups go longest first onto the least-loaded lane; the result is in that
-// (launch) order.
-std::vector<GroupPlan> plan_groups(const std::vector<const HostJob *> &hj, int lanes) {
-    std::map<uint32_t, std::vector<int>> by_p;
-    for (int i = 0; i < (int)hj.size(); i++) by_p[hj[i]->job.p].push_back(i);
-    std::vector<GroupPlan> out;
-    for (auto &kv : by_p) {
-        uint64_t L = 1;
-        bool ok = kv.second.size() > 1;
-        for (int i : kv.second) {
-            const uint64_t d = hj[i]->job.d;
-            const uint64_t g = gcd64(L, d);
-            if (L / g > (~0ull >> 1) / d) {
-                ok = false;
-                break;
-            }
-            L = L / g * d;
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// batch: every job's large-prime work in one tile-queue launch
+//
+// Jobs are grouped into chains: jobs whose P ascend P_1 < ... < P_G and whose
+// d all divide one L (L | P_1#, every L/d below 2^32).  Per prime-table
+// window one kmod_chain launch computes K'_g = P_g#/L mod p for every group
+// of a chain in one pass over K'_G's limbs, and one large_multi launch then
+// runs every job's primes of every window as tiles of 256 primes pulled from
+// a device counter, each job starting its walks from its group's K' mod p
+// scaled by L/d.  Ranges of every job in every window are found once at
+// prepare time, so the launches have host-known tile counts and the whole
+// batch is capturable as one CUDA graph.
+
+namespace {
+
+struct ChainPlan {
+    std::vector<uint32_t> P;        // group primes, ascending
+    uint64_t L = 1;
+    std::vector<uint32_t> limbs;    // segments concatenated
+    std::vector<uint32_t> seg_off;  // G + 1 limb offsets
+    std::vector<int> jobs;
+};
+
+bool primes_of_L_below(uint64_t L, uint32_t P) {
+    for (uint32_t q = 2; L > 1 && (uint64_t)q * q <= L; q++)
+        while (L % q == 0) {
+            if (q > P) return false;
+            L /= q;
         }
-        for (int i : kv.second) ok = ok && L / hj[i]->job.d <= 0xFFFFFFFFull;
-        if (ok) {
-            GroupPlan gp;
-            gp.jobs = kv.second;
-            gp.klimbs = primorial_quotient(kv.first, L);
-            for (int i : kv.second) gp.kmul.push_back((uint32_t)(L / hj[i]->job.d));
-            out.push_back(std::move(gp));
-            continue;
-        }
-        std::map<uint32_t, GroupPlan> by_d;  // same K
-        for (int i : kv.second) {
-            GroupPlan &gp = by_d[hj[i]->job.d];
-            gp.jobs.push_back(i);
-            gp.kmul.push_back(1);
-            gp.klimbs = hj[i]->klimbs;
-        }
-        for (auto &dg : by_d) out.push_back(std::move(dg.second));
-    }
-    for (GroupPlan &gp : out)
-        for (int i : gp.jobs) gp.cost += job_cost(*hj[i]);
-    std::sort(out.begin(), out.end(), [](const GroupPlan &a, const GroupPlan &b) { return a.cost > b.cost; });
-    std::vector<uint64_t> load(lanes, 0);
-    for (GroupPlan &gp : out) {
-        gp.lane = (int)(std::min_element(load.begin(), load.end()) - load.begin());
-        load[gp.lane] += gp.cost;
-    }
-    return out;
+    return L <= P;
 }
 
-// Device copies of the groups' K' limbs, packed; offsets per group.
-cudaError_t upload_group_limbs(const std::vector<GroupPlan> &groups, DevBuf &buf,
-                               std::vector<size_t> &offset, cudaStream_t s) {
-    std::vector<uint32_t> all;
-    offset.clear();
-    for (const GroupPlan &gp : groups) {
-        offset.push_back(all.size());
-        all.insert(all.end(), gp.klimbs.begin(), gp.klimbs.end());
+// Chains over the distinct P ascending; a chain grows while the lcm of its d
+// stays a divisor of P_1# with every L/d below 2^32 and its limbs fit the
+// kernel's shared memory.
+std::vector<ChainPlan> plan_chains(const std::vector<const HostJob *> &hj, std::vector<int> &chain_of,
+                                   std::vector<int> &group_of, std::vector<uint32_t> &kmul) {
+    std::map<uint32_t, std::vector<int>> by_p;
+    for (int i = 0; i < (int)hj.size(); i++) by_p[hj[i]->job.p].push_back(i);
+    std::vector<ChainPlan> out;
+    chain_of.assign(hj.size(), -1);
+    group_of.assign(hj.size(), 0);
+    kmul.assign(hj.size(), 1);
+    ChainPlan cur;
+    auto fits = [&](const ChainPlan &c, uint64_t L, const std::vector<int> &more) {
+        if (L == 0 || !primes_of_L_below(L, c.P.empty() ? hj[more[0]]->job.p : c.P.front())) return false;
+        for (int i : c.jobs)
+            if (L / hj[i]->job.d > 0xFFFFFFFFull) return false;
+        for (int i : more)
+            if (L / hj[i]->job.d > 0xFFFFFFFFull) return false;
+        return true;
+    };
+    auto close = [&] {
+        if (cur.jobs.empty()) return;
+        // segment 0: P_1#/L; segment g: the primes in (P_(g-1), P_g]
+        cur.limbs.clear();
+        cur.seg_off.assign(1, 0);
+        std::vector<uint32_t> seg = primorial_quotient(cur.P[0], cur.L);
+        for (size_t g = 0; g < cur.P.size(); g++) {
+            if (g) {
+                seg.assign(1, 1);
+                for (uint32_t q : primes_upto(cur.P[g])) {
+                    if (q <= cur.P[g - 1]) continue;
+                    uint64_t carry = 0;
+                    for (auto &l : seg) {
+                        const uint64_t t = (uint64_t)l * q + carry;
+                        l = (uint32_t)t;
+                        carry = t >> 32;
+                    }
+                    if (carry) seg.push_back((uint32_t)carry);
+                }
+            }
+            cur.limbs.insert(cur.limbs.end(), seg.begin(), seg.end());
+            cur.seg_off.push_back((uint32_t)cur.limbs.size());
+        }
+        const int c = (int)out.size();
+        for (size_t g = 0; g < cur.P.size(); g++)
+            for (int i : cur.jobs)
+                if (hj[i]->job.p == cur.P[g]) chain_of[i] = c, group_of[i] = (int)g, kmul[i] = (uint32_t)(cur.L / hj[i]->job.d);
+        out.push_back(std::move(cur));
+        cur = ChainPlan();
+    };
+    for (auto &kv : by_p) {
+        uint64_t L = cur.L;
+        for (int i : kv.second) {
+            const uint64_t d = hj[i]->job.d, g = gcd64(L, d);
+            L = (L / g > (~0ull >> 1) / d) ? 0 : L / g * d;
+            if (!L) break;
+        }
+        // the limbs of K'_G grow with P: keep well inside the kernel's shared memory
+        const bool room = cur.limbs.size() + kv.first / 8 + 64 < 12000;
+        if (!cur.jobs.empty() && !(room && fits(cur, L, kv.second))) {
+            close();
+            L = 1;
+            for (int i : kv.second) {
+                const uint64_t d = hj[i]->job.d, g = gcd64(L, d);
+                L = (L / g > (~0ull >> 1) / d) ? 0 : L / g * d;
+                if (!L) break;
+            }
+        }
+        if (cur.jobs.empty() && !fits(cur, L, kv.second)) {
+            // a P whose own d do not share one L: each d alone (L = d)
+            for (int i : kv.second) {
+                cur.P = {kv.first};
+                cur.L = hj[i]->job.d;
+                cur.jobs = {i};
+                close();
+            }
+            continue;
+        }
+        cur.P.push_back(kv.first);
+        cur.L = L;
+        cur.jobs.insert(cur.jobs.end(), kv.second.begin(), kv.second.end());
     }
-    return upload(buf, all, s);
+    close();
+    return out;
 }
 
 }  // namespace
@@ -506,35 +556,356 @@ struct pgs_batch {
     pgs_ctx *ctx = nullptr;
     std::vector<pgs_prepared *> jobs;
     std::vector<int> lane_of;
-    std::vector<GroupPlan> groups;         // in launch order
-    std::vector<size_t> group_urange;      // offset (words) of each group's hull ranges
-    std::vector<size_t> group_limbs;       // offset of each group's K' limbs
-    DevBuf urange, glimbs;
     int nlanes = 1;
+    // chains and their residues: per (chain, window) the union index range
+    // of the chain's jobs in the window and G + 1 arrays of that length
+    std::vector<ChainPlan> chains;
+    std::vector<int> chain_of, group_of;
+    std::vector<uint32_t> kmul;
+    struct ChainWindow {
+        int chain, window;
+        uint64_t begin, count;
+        bool wide;
+        DevBuf r;  // G * count residues, then count R^2 values
+    };
+    std::vector<ChainWindow *> cw;
+    DevBuf chain_limbs, chain_off;            // all chains' segments, offsets
+    std::vector<size_t> limb_base, off_base;  // per chain
+    // the tile launches in chunks of jobs: the rows of one chunk's jobs run
+    // on the other lanes while the next chunk's large primes run
+    struct Chunk {
+        std::vector<int> jobs;
+        DevBuf items32, items64;
+        uint32_t n32 = 0, n64 = 0, tiles32 = 0, tiles64 = 0;
+        cudaEvent_t done = nullptr;
+    };
+    std::vector<Chunk *> chunks;
+    DevBuf d_jobs, counters, heavy;
+    size_t smem = 0;
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
-    cudaEvent_t t0 = nullptr, t1 = nullptr, fork = nullptr;
-    std::vector<cudaEvent_t> joins;
+    cudaEvent_t t0 = nullptr, t1 = nullptr, fork = nullptr, setup_done = nullptr;
+    std::vector<cudaEvent_t> joins, job_done;
+    ~pgs_batch() {
+        for (auto *c : cw) {
+            c->r.release();
+            delete c;
+        }
+        for (auto *c : chunks) {
+            c->items32.release();
+            c->items64.release();
+            if (c->done) cudaEventDestroy(c->done);
+            delete c;
+        }
+        for (DevBuf *d : {&chain_limbs, &chain_off, &d_jobs, &counters, &heavy}) d->release();
+    }
 };
 
 namespace {
 
+// Index ranges {begin, end} of [lo_val, hi_val] in table windows, found on
+// the device and read back (prepare time).
+int table_ranges(pgs_ctx *ctx, const std::vector<std::tuple<int, uint64_t, uint64_t>> &q,
+                 std::vector<std::pair<uint64_t, uint64_t>> &out, cudaStream_t s) {
+    out.assign(q.size(), {0, 0});
+    if (q.empty()) return PGS_OK;
+    DevBuf buf;
+    buf.pool = &ctx->dpool;
+    CK(buf.ensure(q.size() * 16));
+    for (size_t i = 0; i < q.size(); i++) {
+        const TableWindow &w = *ctx->table->windows[std::get<0>(q[i])];
+        CK(pg::find_range(w.off.as<uint32_t>(), w.count, w.lo, std::get<1>(q[i]), std::get<2>(q[i]),
+                          buf.as<unsigned long long>() + 2 * i, s));
+    }
+    std::vector<unsigned long long> h(2 * q.size());
+    CK(cudaMemcpyAsync(h.data(), buf.p, h.size() * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    for (size_t i = 0; i < q.size(); i++) out[i] = {h[2 * i], std::max(h[2 * i], h[2 * i + 1])};
+    buf.release();
+    return PGS_OK;
+}
+
+// Chains, residue buffers, jobs and tile items of a batch whose jobs are
+// prepared (b->jobs) over the context's table.
+int plan_batch(pgs_ctx *ctx, pgs_batch *b, cudaStream_t s) {
+    PrimeTable &t = *ctx->table;
+    const int n = (int)b->jobs.size();
+    std::vector<const HostJob *> hp;
+    for (auto *pr : b->jobs) hp.push_back(&pr->hj);
+    b->chains = plan_chains(hp, b->chain_of, b->group_of, b->kmul);
+    // chain x window union ranges, then every job's own range per window
+    std::vector<std::tuple<int, uint64_t, uint64_t>> q;
+    std::vector<std::pair<int, int>> qcw;
+    for (int c = 0; c < (int)b->chains.size(); c++)
+        for (int k = 0; k < (int)t.windows.size(); k++) {
+            uint64_t lo = ~0ull, hi = 0;
+            for (int j : b->chains[c].jobs)
+                for (int w : b->jobs[j]->tbl_windows)
+                    if (w == k) lo = std::min(lo, b->jobs[j]->hj.s1 + 1), hi = std::max(hi, b->jobs[j]->hj.prime_limit);
+            if (lo <= hi) q.emplace_back(k, lo, hi), qcw.push_back({c, k});
+        }
+    const size_t nq_chain = q.size();
+    std::vector<std::pair<int, int>> qjob;
+    for (int j = 0; j < n; j++)
+        for (int w : b->jobs[j]->tbl_windows) {
+            q.emplace_back(w, b->jobs[j]->hj.s1 + 1, b->jobs[j]->hj.prime_limit);
+            qjob.push_back({j, w});
+        }
+    std::vector<std::pair<uint64_t, uint64_t>> rg;
+    int rc = table_ranges(ctx, q, rg, s);
+    if (rc) return rc;
+    std::map<std::pair<int, int>, pgs_batch::ChainWindow *> cw_of;
+    for (size_t i = 0; i < nq_chain; i++) {
+        auto *c = new pgs_batch::ChainWindow();
+        c->chain = qcw[i].first;
+        c->window = qcw[i].second;
+        c->begin = rg[i].first;
+        c->count = rg[i].second - rg[i].first;
+        c->wide = t.windows[c->window]->lo >= (1ull << 32);
+        c->r.pool = &ctx->dpool;
+        b->cw.push_back(c);
+        const size_t G = b->chains[c->chain].P.size();
+        CK(c->r.ensure(std::max<uint64_t>(1, (G + 1) * c->count) * (c->wide ? 8 : 4)));
+        cw_of[qcw[i]] = c;
+    }
+    // segments of every chain, packed
+    std::vector<uint32_t> limbs, offs;
+    for (const ChainPlan &c : b->chains) {
+        b->limb_base.push_back(limbs.size());
+        b->off_base.push_back(offs.size());
+        limbs.insert(limbs.end(), c.limbs.begin(), c.limbs.end());
+        offs.insert(offs.end(), c.seg_off.begin(), c.seg_off.end());
+    }
+    b->chain_limbs.pool = b->chain_off.pool = &ctx->dpool;
+    CK(upload(b->chain_limbs, limbs, s));
+    CK(upload(b->chain_off, offs, s));
+    // jobs and items
+    std::vector<pg::LargeJob> lj(n);
+    size_t smem = 0;
+    for (int j = 0; j < n; j++) {
+        pgs_prepared *pr = b->jobs[j];
+        lj[j].job = job_dev(pr);
+        lj[j].job.kmul = b->kmul[j];
+        lj[j].mmask = pr->mmask.as<uint2>();
+        lj[j].ymask = pr->ymask.as<uint2>();
+        const size_t mb = 8ull * ((lj[j].job.walk.jmax + 31) / 32 + (lj[j].job.walk.w + 31) / 32);
+        lj[j].masks_in_shared = mb <= 96 * 1024;
+        if (lj[j].masks_in_shared) smem = std::max(smem, mb);
+    }
+    b->smem = smem;
+    // chunks: jobs by rows work, longest first, cut where the cumulative
+    // large-prime work (primes to the limit) passes each quarter
+    std::vector<int> order(n);
+    for (int j = 0; j < n; j++) order[j] = j;
+    auto rows_work = [&](int j) { return (double)b->jobs[j]->hj.valid_mi.size() * (b->jobs[j]->hj.H + 64); };
+    auto large_work = [&](int j) {
+        const double lim = (double)b->jobs[j]->hj.prime_limit;
+        return lim / std::log(std::max(lim, 3.0));
+    };
+    std::stable_sort(order.begin(), order.end(), [&](int x, int y) { return rows_work(x) > rows_work(y); });
+    double total = 0;
+    for (int j = 0; j < n; j++) total += large_work(j);
+    const int nchunks = std::max(1, std::min(4, n));
+    double acc = 0;
+    for (int j : order) {
+        const int c = std::min(nchunks - 1, (int)(acc / total * nchunks));
+        while ((int)b->chunks.size() <= c) b->chunks.push_back(new pgs_batch::Chunk());
+        b->chunks[c]->jobs.push_back(j);
+        acc += large_work(j);
+    }
+    std::map<int, std::vector<size_t>> q_of_job;
+    for (size_t i = 0; i < qjob.size(); i++) q_of_job[qjob[i].first].push_back(i);
+    for (pgs_batch::Chunk *ch : b->chunks) {
+        std::vector<pg::LargeItem> it32, it64;
+        for (int j : ch->jobs)
+            for (size_t i : q_of_job[j]) {
+                const int w = qjob[i].second;
+                const auto r = rg[nq_chain + i];
+                if (r.second <= r.first) continue;
+                pgs_batch::ChainWindow *c = cw_of.at({b->chain_of[j], w});
+                const TableWindow &tw = *t.windows[w];
+                const size_t width = c->wide ? 8 : 4;
+                const size_t G = b->chains[c->chain].P.size();
+                pg::LargeItem it{};
+                it.job = (uint32_t)j;
+                it.count = (uint32_t)(r.second - r.first);
+                it.base = tw.lo;
+                it.off = tw.off.as<uint32_t>() + r.first;
+                it.a = (const char *)c->r.p + ((uint64_t)b->group_of[j] * c->count + (r.first - c->begin)) * width;
+                it.b = (const char *)c->r.p + ((uint64_t)G * c->count + (r.first - c->begin)) * width;
+                uint32_t &tiles = c->wide ? ch->tiles64 : ch->tiles32;
+                it.tile0 = tiles;
+                tiles += (it.count + pg::kLargeTile - 1) / pg::kLargeTile;
+                (c->wide ? it64 : it32).push_back(it);
+            }
+        ch->n32 = (uint32_t)it32.size();
+        ch->n64 = (uint32_t)it64.size();
+        ch->items32.pool = ch->items64.pool = &ctx->dpool;
+        CK(upload(ch->items32, it32, s));
+        CK(upload(ch->items64, it64, s));
+        CK(cudaEventCreateWithFlags(&ch->done, cudaEventDisableTiming));
+    }
+    // each job's setup, rows and text on one lane: the lanes other than lane
+    // 0 (which runs the chunks' large primes), in chunk order
+    const int first_rows_lane = b->nlanes > 1 ? 1 : 0;
+    int next_lane = 0;
+    b->lane_of.assign(n, 0);
+    for (pgs_batch::Chunk *ch : b->chunks)
+        for (int j : ch->jobs) b->lane_of[j] = first_rows_lane + next_lane++ % (b->nlanes - first_rows_lane);
+    for (DevBuf *d : {&b->d_jobs, &b->counters, &b->heavy}) d->pool = &ctx->dpool;
+    CK(upload(b->d_jobs, lj, s));
+    CK(b->counters.ensure(16));
+    CK(b->heavy.ensure((size_t)pg::heavy_capacity() * pg::kHeavyPrimeBytes));
+    CK(cudaStreamSynchronize(s));
+    return PGS_OK;
+}
+
+// Per-job kernels before the large phase: the bitset and range words
+// cleared, K mod p of the job's small primes and of the primes of d.
+int job_setup(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s) {
+    PrimeTable &t = *ctx->table;
+    HostJob &h = pr->hj;
+    const uint64_t rows = h.valid_mi.size();
+    unsigned long long *misc = pr->misc.as<unsigned long long>();
+    const int nl = (int)h.klimbs.size();
+    pr->launches = 0;
+    CK(cudaMemsetAsync(pr->comp.p, 0, rows * h.pitch * 4ull, s));
+    CK(cudaMemsetAsync(pr->misc.p, 0, (1 + 2 * job_ranges(pr)) * 8, s));
+    CK(pg::set_pair(misc + 1, pr->tbl_a, pr->tbl_b, s));
+    pr->launches++;
+    if (pr->sp_bound) {
+        CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, 0, t.small.as<uint32_t>(), misc + 1, pr->sp_bound, nullptr,
+                           pr->sr.p, nullptr, false, s));
+        pr->launches++;
+    }
+    if (!h.dq.empty()) {
+        CK(pg::kmod_list32(pr->klimbs.as<uint32_t>(), nl, pr->dq.as<uint32_t>(), (uint32_t)h.dq.size(),
+                           pr->dr.as<uint32_t>(), s));
+        pr->launches++;
+    }
+    return PGS_OK;
+}
+
+// Rows, offsets and text of one job.
+int job_rows(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s) {
+    PrimeTable &t = *ctx->table;
+    HostJob &h = pr->hj;
+    const uint64_t rows = h.valid_mi.size();
+    pg::RowsDev rd = rows_dev(pr);
+    rd.sp = t.small.as<uint32_t>();
+    rd.sp_base = 0;
+    rd.sp_range = pr->misc.as<unsigned long long>() + 1;
+    rd.sp_cap = pr->sp_bound;
+    CK(pg::rows_extract(rd, rows_per_block(h.nb, h.job.compression, pr->tune.rows_per_cta), s));
+    CK(pg::scan_u64(pr->row_bytes.as<uint64_t>(), pr->offsets.as<uint64_t>(), pr->misc.as<uint64_t>(), rows,
+                    pr->scan_tmp.as<uint64_t>(), s));
+    CK(pg::format_rows(rd, pr->offsets.as<uint64_t>(), pr->text.as<char>(), s));
+    pr->launches += 5;
+    pr->ran = true;
+    return PGS_OK;
+}
+
+// The whole batch, asynchronous and capturable: job setups over the lanes;
+// on lane 0 the chains' K' mod p and the two tile-queue launches (32-bit and
+// 64-bit windows); then rows and text over the lanes, each job's done event
+// recorded, all lanes joined back into lane 0.
 int launch_batch(pgs_ctx *ctx, pgs_batch *b) {
     Lane *l0 = ctx->lanes[0];
-    CK(cudaEventRecord(b->fork, l0->stream));
+    const cudaStream_t s0 = l0->stream;
+    CK(cudaEventRecord(b->fork, s0));
     for (int l = 1; l < b->nlanes; l++) CK(cudaStreamWaitEvent(ctx->lanes[l]->stream, b->fork, 0));
-    for (size_t g = 0; g < b->groups.size(); g++) {
-        const GroupPlan &gp = b->groups[g];
-        std::vector<pgs_prepared *> jobs;
-        for (int j : gp.jobs) jobs.push_back(b->jobs[j]);
-        int rc = run_group(ctx, jobs, ctx->lanes[gp.lane], b->urange.as<unsigned long long>() + b->group_urange[g],
-                           b->glimbs.as<uint32_t>() + b->group_limbs[g], (int)gp.klimbs.size(), gp.kmul);
+    for (size_t j = 0; j < b->jobs.size(); j++) {
+        int rc = job_setup(ctx, b->jobs[j], ctx->lanes[b->lane_of[j]]->stream);
         if (rc) return rc;
     }
     for (int l = 1; l < b->nlanes; l++) {
         CK(cudaEventRecord(b->joins[l], ctx->lanes[l]->stream));
-        CK(cudaStreamWaitEvent(l0->stream, b->joins[l], 0));
+        CK(cudaStreamWaitEvent(s0, b->joins[l], 0));
     }
+    PrimeTable &t = *ctx->table;
+    for (pgs_batch::ChainWindow *c : b->cw) {
+        const ChainPlan &ch = b->chains[c->chain];
+        const TableWindow &w = *t.windows[c->window];
+        const size_t width = c->wide ? 8 : 4;
+        CK(pg::kmod_chain(b->chain_limbs.as<uint32_t>() + b->limb_base[c->chain],
+                          b->chain_off.as<uint32_t>() + b->off_base[c->chain], (int)ch.P.size(), (int)ch.limbs.size(),
+                          w.lo, w.off.as<uint32_t>() + c->begin, c->count, c->r.p,
+                          (char *)c->r.p + ch.P.size() * c->count * width, c->wide, s0));
+    }
+    const pg::LargeScratch scr{b->counters.as<unsigned long long>(), b->heavy.as<pg::HeavyPrime>(),
+                               pg::heavy_capacity()};
+    for (pgs_batch::Chunk *ch : b->chunks) {
+        CK(pg::large_multi(b->d_jobs.as<pg::LargeJob>(), ch->items32.as<pg::LargeItem>(), ch->n32, ch->tiles32,
+                           b->smem, false, scr, s0));
+        if (ch->tiles64)
+            CK(pg::large_multi(b->d_jobs.as<pg::LargeJob>(), ch->items64.as<pg::LargeItem>(), ch->n64, ch->tiles64,
+                               b->smem, true, scr, s0));
+        CK(cudaEventRecord(ch->done, s0));
+        for (int j : ch->jobs) {
+            const cudaStream_t s = ctx->lanes[b->lane_of[j]]->stream;
+            CK(cudaStreamWaitEvent(s, ch->done, 0));
+            int rc = job_rows(ctx, b->jobs[j], s);
+            if (rc) return rc;
+            b->jobs[j]->launches += 4;  // its share of the chain and tile launches
+            CK(cudaEventRecord(b->job_done[j], s));
+        }
+    }
+    for (int l = 1; l < b->nlanes; l++) {
+        CK(cudaEventRecord(b->joins[l], ctx->lanes[l]->stream));
+        CK(cudaStreamWaitEvent(s0, b->joins[l], 0));
+    }
+    return PGS_OK;
+}
+
+// Prepare a batch: derive (host threads), extend the table, prepare every
+// job (uploads on the context stream), plan chains and tiles.
+int batch_create(pgs_ctx *ctx, const pgs_job *jobs, int n, int lanes, pgs_batch **out) {
+    *out = nullptr;
+    std::vector<HostJob> hj;
+    int rc = derive_all(jobs, n, hj, true, ctx->err);
+    if (rc) return rc;
+    uint64_t limit = 3, small = kSmallMin;
+    for (const HostJob &h : hj) {
+        limit = std::max(limit, h.prime_limit);
+        small = std::max(small, std::min<uint64_t>(h.s1, h.prime_limit));
+    }
+    rc = table_extend(ctx, limit, small, ctx->stream);
+    if (rc) return rc;
+    const int L = std::max(1, std::min(lanes, n));
+    rc = ensure_lanes(ctx, L);
+    if (rc) return rc;
+    auto *b = new pgs_batch();
+    b->ctx = ctx;
+    b->nlanes = L;
+    b->lane_of.assign(n, 0);
+    for (int i = 0; i < n; i++) {
+        pgs_prepared *pr = nullptr;
+        rc = prepare_table_job(ctx, jobs[i], ctx->stream, &pr, &hj[i]);
+        if (rc) {
+            pgs_batch_free(b);
+            return rc;
+        }
+        b->jobs.push_back(pr);
+    }
+    rc = plan_batch(ctx, b, ctx->stream);
+    if (rc) {
+        pgs_batch_free(b);
+        return rc;
+    }
+    cudaError_t e = cudaEventCreate(&b->t0);
+    if (!e) e = cudaEventCreate(&b->t1);
+    if (!e) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
+    if (!e) e = cudaEventCreateWithFlags(&b->setup_done, cudaEventDisableTiming);
+    b->joins.assign(L, nullptr);
+    b->job_done.assign(n, nullptr);
+    for (int l = 1; l < L && !e; l++) e = cudaEventCreateWithFlags(&b->joins[l], cudaEventDisableTiming);
+    for (int j = 0; j < n && !e; j++) e = cudaEventCreateWithFlags(&b->job_done[j], cudaEventDisableTiming);
+    if (!e) e = cudaStreamSynchronize(ctx->stream);
+    if (e) {
+        pgs_batch_free(b);
+        return fail(ctx, e, "batch events");
+    }
+    *out = b;
     return PGS_OK;
 }
 
@@ -553,65 +924,7 @@ int pgs_batch_prepare(pgs_ctx *ctx, const pgs_job *jobs, int n, int lanes, pgs_b
     if (!ctx || !jobs || n <= 0 || !out) return PGS_EINVAL;
     std::lock_guard<std::mutex> g(ctx->mu);
     CK(cudaSetDevice(ctx->device));
-    *out = nullptr;
-    std::vector<HostJob> hj;
-    int rc = derive_all(jobs, n, hj, true, ctx->err);
-    if (rc) return rc;
-    // cover every job: large primes up to the largest limit, small up to the largest S1
-    uint64_t limit = 3, small = kSmallMin;
-    for (const HostJob &h : hj) {
-        limit = std::max(limit, h.prime_limit);
-        small = std::max(small, std::min<uint64_t>(h.s1, h.prime_limit));
-    }
-    rc = table_extend(ctx, limit, small, ctx->stream);
-    if (rc) return rc;
-    const int L = std::max(1, std::min(lanes, n));
-    rc = ensure_lanes(ctx, L);
-    if (rc) return rc;
-    auto *b = new pgs_batch();
-    b->ctx = ctx;
-    b->nlanes = L;
-    std::vector<const HostJob *> hp;
-    for (const HostJob &h : hj) hp.push_back(&h);
-    b->groups = plan_groups(hp, L);
-    const int G = (int)b->groups.size();
-    b->lane_of.assign(n, 0);
-    for (int g = 0; g < G; g++)
-        for (int j : b->groups[g].jobs) b->lane_of[j] = b->groups[g].lane;
-    b->glimbs.pool = &ctx->dpool;
-    cudaError_t le = upload_group_limbs(b->groups, b->glimbs, b->group_limbs, ctx->stream);
-    if (le != cudaSuccess) {
-        pgs_batch_free(b);
-        return fail(ctx, le, "batch group limbs");
-    }
-    for (int i = 0; i < n; i++) {
-        pgs_prepared *pr = nullptr;
-        rc = prepare_table_job(ctx, jobs[i], ctx->stream, &pr, &hj[i]);
-        if (rc) {
-            pgs_batch_free(b);
-            return rc;
-        }
-        b->jobs.push_back(pr);
-    }
-    size_t words = 0;
-    for (int g = 0; g < G; g++) {
-        b->group_urange.push_back(words);
-        words += 2 * ctx->table->windows.size();
-    }
-    b->urange.pool = &ctx->dpool;
-    cudaError_t ue = b->urange.ensure(std::max<size_t>(words, 2) * 8);
-    if (ue != cudaSuccess) {
-        pgs_batch_free(b);
-        return fail(ctx, ue, "batch ranges");
-    }
-    CK(cudaEventCreate(&b->t0));
-    CK(cudaEventCreate(&b->t1));
-    CK(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
-    b->joins.assign(L, nullptr);
-    for (int l = 1; l < L; l++) CK(cudaEventCreateWithFlags(&b->joins[l], cudaEventDisableTiming));
-    CK(cudaStreamSynchronize(ctx->stream));
-    *out = b;
-    return PGS_OK;
+    return batch_create(ctx, jobs, n, lanes, out);
 }
 
 int pgs_batch_run(pgs_ctx *ctx, pgs_batch *b, int use_graph, double *ms) {
@@ -663,103 +976,60 @@ void pgs_batch_free(pgs_batch *b) {
     }
     if (b->exec) cudaGraphExecDestroy(b->exec);
     if (b->graph) cudaGraphDestroy(b->graph);
-    if (b->t0) cudaEventDestroy(b->t0);
-    if (b->t1) cudaEventDestroy(b->t1);
-    if (b->fork) cudaEventDestroy(b->fork);
+    for (cudaEvent_t e : {b->t0, b->t1, b->fork, b->setup_done})
+        if (e) cudaEventDestroy(e);
     for (auto e : b->joins)
         if (e) cudaEventDestroy(e);
+    for (auto e : b->job_done)
+        if (e) cudaEventDestroy(e);
     for (auto *pr : b->jobs) delete pr;
-    b->urange.release();
-    b->glimbs.release();
     delete b;
 }
 
-// One pass, pipelined: host work (job tables) is done up front on several
-// threads, each group's uploads go on the context stream and its kernels on
-// its lane as soon as they are enqueued, and results are copied back group by
-// group as each finishes, while the other lanes still compute.
+// One pass: the batch prepared and launched without a graph, and each job's
+// text copied to the host on the context stream as soon as its rows and text
+// are done on its lane (in launch order of completion events), while other
+// lanes still run.
 int pgs_method2_batch(pgs_ctx *ctx, const pgs_job *jobs, int n, pgs_result *outs) {
     if (!ctx || !jobs || n <= 0 || !outs) return PGS_EINVAL;
     for (int i = 0; i < n; i++) memset(&outs[i], 0, sizeof(pgs_result));
     std::lock_guard<std::mutex> g(ctx->mu);
     CK(cudaSetDevice(ctx->device));
-    std::vector<HostJob> hj;
-    int rc = derive_all(jobs, n, hj, true, ctx->err);
+    pgs_batch *b = nullptr;
+    int rc = batch_create(ctx, jobs, n, 8, &b);
     if (rc) return rc;
-    uint64_t limit = 3, small = kSmallMin;
-    for (const HostJob &h : hj) {
-        limit = std::max(limit, h.prime_limit);
-        small = std::max(small, std::min<uint64_t>(h.s1, h.prime_limit));
-    }
-    rc = table_extend(ctx, limit, small, ctx->stream);
-    if (rc) return rc;
-    const int L = std::max(1, std::min(8, n));
-    rc = ensure_lanes(ctx, L);
-    if (rc) return rc;
-    std::vector<const HostJob *> hp;
-    for (const HostJob &h : hj) hp.push_back(&h);
-    const std::vector<GroupPlan> groups = plan_groups(hp, L);
-    const int G = (int)groups.size();
-    const size_t nwin = ctx->table->windows.size();
-    DevBuf urange, glimbs;
-    urange.pool = glimbs.pool = &ctx->dpool;
-    std::vector<size_t> limb_off;
-    std::vector<pgs_prepared *> prs(n, nullptr);
-    std::vector<cudaEvent_t> up_done(G, nullptr), done(G, nullptr);
-    cudaStream_t up = ctx->stream;
-    auto cleanup = [&] {
-        for (Lane *l : ctx->lanes) cudaStreamSynchronize(l->stream);
-        cudaStreamSynchronize(up);
-        for (auto *pr : prs) delete pr;
-        for (auto e : up_done)
-            if (e) cudaEventDestroy(e);
-        for (auto e : done)
-            if (e) cudaEventDestroy(e);
-        urange.release();
-        glimbs.release();
-    };
-    cudaError_t e = urange.ensure(std::max<size_t>(2 * nwin * G, 2) * 8);
-    if (e == cudaSuccess) e = upload_group_limbs(groups, glimbs, limb_off, up);
-    for (int k = 0; k < G && e == cudaSuccess; k++) {
-        e = cudaEventCreateWithFlags(&up_done[k], cudaEventDisableTiming);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&done[k], cudaEventDisableTiming);
-    }
-    if (e != cudaSuccess) {
-        cleanup();
-        return fail(ctx, e, "batch setup");
-    }
-    for (int grp = 0; grp < G && rc == PGS_OK; grp++) {
-        const GroupPlan &gp = groups[grp];
-        Lane *lane = ctx->lanes[gp.lane];
-        std::vector<pgs_prepared *> members;
-        for (int j : gp.jobs) {
-            rc = prepare_table_job(ctx, jobs[j], up, &prs[j], &hj[j]);
-            if (rc) break;
-            members.push_back(prs[j]);
+    rc = launch_batch(ctx, b);
+    // fetch in the order the jobs' lanes finish them: lane by lane, each
+    // lane's jobs in launch order
+    std::vector<std::vector<int>> per_lane(b->nlanes);
+    for (int j = 0; j < n; j++) per_lane[b->lane_of[j]].push_back(j);
+    std::vector<size_t> next(b->nlanes, 0);
+    for (int done = 0; rc == PGS_OK && done < n;) {
+        bool any = false;
+        for (int l = 0; l < b->nlanes && rc == PGS_OK; l++) {
+            if (next[l] >= per_lane[l].size()) continue;
+            const int j = per_lane[l][next[l]];
+            const cudaError_t q = cudaEventQuery(b->job_done[j]);
+            if (q == cudaErrorNotReady) continue;
+            if (q != cudaSuccess) {
+                rc = fail(ctx, q, "batch job event");
+                break;
+            }
+            cudaError_t e = cudaStreamWaitEvent(ctx->stream, b->job_done[j], 0);
+            if (e) {
+                rc = fail(ctx, e, "batch fetch order");
+                break;
+            }
+            rc = fetch_job(ctx, b->jobs[j], ctx->stream, &outs[j]);
+            next[l]++;
+            done++;
+            any = true;
         }
-        if (rc) break;
-        if ((e = cudaEventRecord(up_done[grp], up)) || (e = cudaStreamWaitEvent(lane->stream, up_done[grp], 0))) {
-            rc = fail(ctx, e, "batch upload order");
-            break;
-        }
-        rc = run_group(ctx, members, lane, urange.as<unsigned long long>() + 2 * nwin * grp,
-                       glimbs.as<uint32_t>() + limb_off[grp], (int)gp.klimbs.size(), gp.kmul);
-        if (rc == PGS_OK && (e = cudaEventRecord(done[grp], lane->stream))) rc = fail(ctx, e, "batch event");
-    }
-    // results, group by group in launch order, on the upload stream
-    for (int grp = 0; grp < G && rc == PGS_OK; grp++) {
-        if ((e = cudaStreamWaitEvent(up, done[grp], 0))) {
-            rc = fail(ctx, e, "batch fetch order");
-            break;
-        }
-        for (int j : groups[grp].jobs) {
-            rc = fetch_job(ctx, prs[j], up, &outs[j]);
-            if (rc) break;
-        }
+        if (!any && rc == PGS_OK) std::this_thread::sleep_for(std::chrono::microseconds(50));
     }
     if (rc != PGS_OK)
         for (int i = 0; i < n; i++) pgs_result_free(&outs[i]);
-    cleanup();
+    pgs_batch_free(b);
     return rc;
 }
 

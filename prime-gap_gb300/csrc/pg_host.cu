@@ -11,6 +11,7 @@
 #include <cstring>
 
 #include "pg_host.h"
+#include "pg_tuning.h"
 
 namespace pgh {
 
@@ -265,6 +266,9 @@ pg::JobDev job_dev(pgs_prepared *pr) {
     j.y_lo = h.y_lo;
     j.walk = h.walk;
     j.kmul = 1;
+    j.direct_steps = pr->tune.direct_steps;
+    j.item_shift = (uint32_t)pgt::ilog2(pr->tune.item_steps);
+    j.heavy_steps = pr->tune.heavy_steps;
     return j;
 }
 
@@ -294,12 +298,15 @@ pg::RowsDev rows_dev(pgs_prepared *pr) {
 
 // Rows per CTA of rows_kernel: as many as keep four 512-thread CTAs (2048
 // threads, the SM's limit) resident, with their bitmaps in shared memory
-// (55 KiB each), and at most 16.  Config 2 (626 bitmap words per row):
-// 16 rows run 12 % faster than 32 rows at two CTAs per SM.
-uint32_t rows_per_block(uint32_t nb, int compression) {
-    uint32_t nbw = (nb + 31) / 32;
-    uint32_t r = 56320u / (nbw * 4u * (compression == 2 ? 2u : 1u) + 4u + 64u);
-    if (r > 16) r = 16;
+// (55 KiB each), and at most `cap` (the job's tuning, 16 by default).
+// Config 2 (626 bitmap words per row): 16 rows run 12 % faster than 32 rows
+// at two CTAs per SM.  A cap above 16 trades resident CTAs for rows: up to
+// the 220 KiB a CTA may hold.
+uint32_t rows_per_block(uint32_t nb, int compression, uint32_t cap) {
+    const uint32_t nbw = (nb + 31) / 32;
+    const uint32_t per_row = nbw * 4u * (compression == 2 ? 2u : 1u) + 4u + 64u;
+    uint32_t r = (cap > 16 ? 225280u : 56320u) / per_row;
+    if (r > cap) r = cap;
     if (r < 1) r = 1;
     return r;
 }

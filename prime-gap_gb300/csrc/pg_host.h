@@ -5,11 +5,13 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
 
 #include "pg_internal.h"
+#include "pg_tuning.h"
 #include "pgsieve.h"
 
 namespace pgh {
@@ -202,11 +204,16 @@ struct pgs_ctx {
     // batched / served paths (pg_batch.cu)
     PrimeTable *table = nullptr;
     std::vector<Lane *> lanes;
+    // tuning by class (pg_tune.cu); device name for the cache file
+    std::mutex tune_mu;
+    std::map<std::string, pgt::Entry> tuning;
+    std::string device_name;
 };
 
 struct pgs_prepared {
     pgs_ctx *ctx = nullptr;
     pgh::HostJob hj;
+    pgs_tuning tune{24, 64, 4096, 16, 4, 32};  // the job's class tuning (defaults)
     std::vector<pgh::Window> windows;
     uint64_t sp_lo = 0, sp_hi = 0, sp_bound = 0;
     uint64_t text_cap = 0;
@@ -270,8 +277,10 @@ cudaError_t upload(DevBuf &b, const std::vector<T> &v, cudaStream_t s) {
 }
 
 pg::JobDev job_dev(pgs_prepared *pr);
+// The tuning jobs of this class get on the context (defaults when untuned).
+pgs_tuning tuning_for(pgs_ctx *ctx, const pgs_job &job);
 pg::RowsDev rows_dev(pgs_prepared *pr);
-uint32_t rows_per_block(uint32_t nb, int compression);
+uint32_t rows_per_block(uint32_t nb, int compression, uint32_t cap = 16);
 
 // The job's host tables (K limbs, row/column maps, valid m, distances, primes
 // of d, masks) to their device buffers, through one pinned staging block:
@@ -289,6 +298,9 @@ struct HostText {
 // text given, and its counts and stage times (no context lock).
 int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out,
               const HostText *given = nullptr);
+// One run of a prepared job with the context locked (the body of pgs_run;
+// with `sink`, pgs_method2's pipelined rows, text and copy to the host).
+int run_prepared(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink);
 // Number of {begin, end} prime ranges in a prepared job's misc buffer.
 size_t job_ranges(const pgs_prepared *pr);
 // Free the resident prime table and the lanes (pg_batch.cu).

@@ -59,9 +59,20 @@ cudaError_t set_pair(unsigned long long *d_out, uint64_t a, uint64_t b, cudaStre
 // a walk, a = the walk step and b = its start residue (all words of the
 // primes' width).  Primes below 2^32 use 32-bit words, others 64-bit
 // (wide).  K limbs on the device.
+// lsb_min_limbs > 0: the least-significant-first chain from that many limbs
+// (32-bit primes; 64-bit primes from three quarters of it), else the built-in
+// thresholds.
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
                         const unsigned long long *d_range, uint64_t max_count,
-                        const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream);
+                        const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream,
+                        int lsb_min_limbs = 0);
+
+// K'_g mod p for the G groups of a chain (K'_g = K'_(g-1) * S_g, segment g's
+// limbs at d_seg_limbs[d_seg_off[g] .. d_seg_off[g+1]), little-endian) for
+// the n primes base + d_off[i]: r_g at d_r[g * n + i], R^2 mod p at
+// d_r2[i], words of the primes' width.  nlimbs + G + 1 <= 12288.
+cudaError_t kmod_chain(const uint32_t *d_seg_limbs, const uint32_t *d_seg_off, int G, int nlimbs, uint64_t base,
+                       const uint32_t *d_off, uint64_t n, void *d_r, void *d_r2, bool wide, cudaStream_t stream);
 
 // K mod q for an explicit list of 32-bit primes (d-primes, tests).
 cudaError_t kmod_list32(const uint32_t *d_klimbs, int nlimbs, const uint32_t *d_q, uint32_t n,
@@ -82,6 +93,10 @@ struct JobDev {
     uint32_t y_lo;             // walk residues y >= y_lo are offsets X < 0
     WalkParams walk;           // parity-reduced large-prime walk
     uint32_t kmul;             // K = K' * kmul when the walk starts from K' mod p (else 1)
+    // tuning: walks of at most direct_steps steps run in the continued
+    // fraction's thread, of more than heavy_steps in a CTA of their own, the
+    // rest in items of 2^item_shift steps over the CTA
+    uint32_t direct_steps, item_shift, heavy_steps;
 };
 
 struct HeavyPrime;
@@ -93,7 +108,7 @@ struct LargeScratch {
     uint32_t heavy_cap;
 };
 uint32_t heavy_capacity();
-constexpr size_t kHeavyPrimeBytes = 40;
+constexpr size_t kHeavyPrimeBytes = 48;
 
 // d_mmask: valid-m bitmask over walk indices j (walk.jmax bits), d_ymask:
 // live-offset bitmask over walk residues y (walk.w bits), each as {bits, set
@@ -107,6 +122,30 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
                          const void *d_b, const unsigned long long *d_rrange, bool wide,
                          bool start_in_kernel, const uint2 *d_mmask, const uint2 *d_ymask,
                          LargeScratch scratch, cudaStream_t stream);
+
+// Many jobs in one launch (the batch).  A job: its descriptor (kmul set:
+// walks start from K' mod p) and masks; masks_in_shared when they fit the
+// launch's dynamic shared memory.
+struct LargeJob {
+    JobDev job;
+    const uint2 *mmask, *ymask;
+    int masks_in_shared;
+};
+// An item: the primes of one job in one prime-table window, in job order;
+// tile0 = tiles (kLargeThreads primes) of the items before it.  off, a, b
+// point at the item's first prime, its K' mod p (the job's group) and its
+// R^2 mod p, all of the primes' width.
+struct LargeItem {
+    uint32_t job, tile0, count, pad;
+    uint64_t base;
+    const uint32_t *off;
+    const void *a, *b;
+};
+constexpr uint32_t kLargeTile = 256;
+// Both kernels (tiles, then the heavy primes of every job) on one stream;
+// smem = the largest job's mask bytes among those with masks_in_shared.
+cudaError_t large_multi(const LargeJob *d_jobs, const LargeItem *d_items, uint32_t n_items, uint32_t n_tiles,
+                        size_t smem, bool wide, LargeScratch scratch, cudaStream_t stream);
 
 // ---- rows: small primes, merge, extract, format (pg_rows.cu) -----------------
 

@@ -13,6 +13,8 @@
 // by the primes' width), from which a kernel can start any job's walk over
 // this K without a division; or, for one job, its walk step and start residue directly
 // ((base_r * M + SL) % prime, modulo_search.cpp:345; see WalkParams).
+#include <algorithm>
+
 #include "pg_arith.cuh"
 #include "pg_internal.h"
 
@@ -79,6 +81,101 @@ __global__ void __launch_bounds__(kKmodThreads)
     }
 }
 
+// K'_g mod p for every group g of a chain (jobs of a batch sharing one L,
+// their P ascending): K'_1 = P_1#/L, K'_g = K'_(g-1) * S_g with S_g the
+// product of the primes in (P_(g-1), P_g] that do not divide L.  Per prime:
+// Horner over each segment's limbs, most significant first (u <- REDC(u R^2
+// + limb) leaves S_g R^-1; one more REDC with R^2 gives S_g), and the
+// running product r_g = REDC(acc * S_g) with acc = r_(g-1) R (Montgomery
+// form, one REDC with R^2).  One pass over K'_G's limbs serves every group,
+// instead of one reduction of each K'_g.  Writes r_g at r_out[g * stride + i]
+// and R^2 mod p at r2_out[i] (R = 2^32 or 2^64, the primes' width).
+template <bool kWide>
+__global__ void __launch_bounds__(kKmodThreads)
+    kmod_chain_kernel(const uint32_t *__restrict__ seg_limbs, const uint32_t *__restrict__ seg_off, int G,
+                      int nlimbs, uint64_t base, const uint32_t *__restrict__ off, uint64_t n, void *r_out,
+                      void *r2_out) {
+    extern __shared__ uint32_t s_limbs[];  // nlimbs limbs, then G + 1 segment offsets
+    for (int i = threadIdx.x; i < nlimbs; i += blockDim.x) s_limbs[i] = seg_limbs[i];
+    for (int i = threadIdx.x; i <= G; i += blockDim.x) s_limbs[nlimbs + i] = seg_off[i];
+    __syncthreads();
+    const uint32_t *so = s_limbs + nlimbs;
+    if (!kWide) {
+        uint32_t *ro = (uint32_t *)r_out;
+        const uint64_t idx0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kPrimesPerThread;
+        if (idx0 >= n) return;
+        uint32_t p[kPrimesPerThread], pinv[kPrimesPerThread], r2[kPrimesPerThread], acc[kPrimesPerThread];
+        bool lazy = true;
+#pragma unroll
+        for (int k = 0; k < kPrimesPerThread; k++) {
+            p[k] = idx0 + k < n ? (uint32_t)(base + off[idx0 + k]) : 3u;  // pad with a prime
+            pinv[k] = neg_inv32(p[k]);
+            r2[k] = r2_from_r1((0u - p[k]) % p[k], p[k], pinv[k]);
+            acc[k] = 0;
+            lazy = lazy && p[k] < 0x80000000u;
+        }
+        for (int g = 0; g < G; g++) {
+            uint32_t u[kPrimesPerThread];
+#pragma unroll
+            for (int k = 0; k < kPrimesPerThread; k++) u[k] = 0;
+            const int lo = (int)so[g], hi = (int)so[g + 1];
+            if (lazy) {
+                for (int i = hi - 1; i >= lo; i--) {
+                    const uint32_t l = s_limbs[i];
+#pragma unroll
+                    for (int k = 0; k < kPrimesPerThread; k++)
+                        u[k] = redc32_lazy((uint64_t)u[k] * r2[k] + l, p[k], pinv[k]);
+                }
+#pragma unroll
+                for (int k = 0; k < kPrimesPerThread; k++)
+                    if (u[k] >= p[k]) u[k] -= p[k];
+            } else {
+                for (int i = hi - 1; i >= lo; i--) {
+                    const uint32_t l = s_limbs[i];
+#pragma unroll
+                    for (int k = 0; k < kPrimesPerThread; k++)
+                        u[k] = redc32((uint64_t)u[k] * r2[k] + l, p[k], pinv[k]);
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < kPrimesPerThread; k++) {
+                const uint32_t sg = redc32((uint64_t)u[k] * r2[k], p[k], pinv[k]);       // S_g mod p
+                const uint32_t r = g ? redc32((uint64_t)acc[k] * sg, p[k], pinv[k]) : sg;  // K'_g mod p
+                if (idx0 + k < n) ro[(uint64_t)g * n + idx0 + k] = r;
+                acc[k] = redc32((uint64_t)r * r2[k], p[k], pinv[k]);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < kPrimesPerThread; k++)
+            if (idx0 + k < n) ((uint32_t *)r2_out)[idx0 + k] = r2[k];
+    } else {
+        uint64_t *ro = (uint64_t *)r_out;
+        const uint64_t idx = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (idx >= n) return;
+        const uint64_t p = base + off[idx];
+        const uint64_t pinv = neg_inv64(p);
+        const uint64_t r1 = (0ull - p) % p;                          // 2^64 mod p
+        const uint64_t r2 = mulmod_u64(r1, r1, p, 1.0 / (double)p);  // 2^128 mod p
+        uint64_t acc = 0;
+        for (int g = 0; g < G; g++) {
+            const int lo = (int)so[g], nl = (int)so[g + 1] - lo;
+            uint64_t u = 0;
+            for (int i = (nl + 1) / 2 - 1; i >= 0; i--) {
+                uint64_t w = s_limbs[lo + 2 * i];
+                if (2 * i + 1 < nl) w |= (uint64_t)s_limbs[lo + 2 * i + 1] << 32;
+                const uint64_t lo2 = u * r2 + w;
+                const uint64_t hi = umulhi64(u, r2) + (lo2 < w);
+                u = redc64(hi, lo2, p, pinv);
+            }
+            const uint64_t sg = montmul64(u, r2, p, pinv);
+            const uint64_t r = g ? montmul64(acc, sg, p, pinv) : sg;
+            ro[(uint64_t)g * n + idx] = r;
+            acc = montmul64(r, r2, p, pinv);
+        }
+        ((uint64_t *)r2_out)[idx] = r2;
+    }
+}
+
 __global__ void __launch_bounds__(kKmodThreads)
     kmod_list_kernel(const uint32_t *__restrict__ klimbs, int nlimbs, const uint32_t *q, uint32_t n,
                      uint32_t *r) {
@@ -92,7 +189,8 @@ __global__ void __launch_bounds__(kKmodThreads)
 
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
                         const unsigned long long *d_range, uint64_t max_count,
-                        const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream) {
+                        const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream,
+                        int lsb_min_limbs) {
     if (max_count == 0) return cudaSuccess;
     const WalkParams wp = walk ? *walk : WalkParams{};
     const int ww = walk != nullptr;
@@ -103,7 +201,9 @@ cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, con
     // least significant limb first once the cheaper step (an add, a multiply
     // and a multiply-add, against a multiply-add, a multiply and a
     // multiply-add) outweighs the R^(n+1) power
-    const bool lsb = nlimbs >= (wide ? kLsbMinLimbsWide : kLsbMinLimbs);
+    const int lsb_min = lsb_min_limbs > 0 ? (wide ? std::max(1, lsb_min_limbs * 3 / 4) : lsb_min_limbs)
+                                          : (wide ? kLsbMinLimbsWide : kLsbMinLimbs);
+    const bool lsb = nlimbs >= lsb_min;
     if (wide && lsb)
         kmod_kernel<true, true><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
                                                                         d_range, max_count, wp, ww, d_a, d_b);
@@ -124,6 +224,23 @@ cudaError_t kmod_list32(const uint32_t *d_klimbs, int nlimbs, const uint32_t *d_
     if (n == 0) return cudaSuccess;
     kmod_list_kernel<<<(n + kKmodThreads - 1) / kKmodThreads, kKmodThreads, 0, stream>>>(
         d_klimbs, nlimbs, d_q, n, d_r);
+    return cudaGetLastError();
+}
+
+cudaError_t kmod_chain(const uint32_t *d_seg_limbs, const uint32_t *d_seg_off, int G, int nlimbs, uint64_t base,
+                       const uint32_t *d_off, uint64_t n, void *d_r, void *d_r2, bool wide, cudaStream_t stream) {
+    if (n == 0 || G == 0) return cudaSuccess;
+    const uint64_t per_thread = wide ? 1 : kPrimesPerThread;
+    const uint64_t threads = (n + per_thread - 1) / per_thread;
+    const unsigned blocks = (unsigned)((threads + kKmodThreads - 1) / kKmodThreads);
+    const size_t smem = (size_t)(nlimbs + G + 1) * sizeof(uint32_t);
+    if (nlimbs + G + 1 > kMaxSharedLimbs) return cudaErrorInvalidValue;
+    if (wide)
+        kmod_chain_kernel<true><<<blocks, kKmodThreads, smem, stream>>>(d_seg_limbs, d_seg_off, G, nlimbs, base,
+                                                                        d_off, n, d_r, d_r2);
+    else
+        kmod_chain_kernel<false><<<blocks, kKmodThreads, smem, stream>>>(d_seg_limbs, d_seg_off, G, nlimbs, base,
+                                                                         d_off, n, d_r, d_r2);
     return cudaGetLastError();
 }
 

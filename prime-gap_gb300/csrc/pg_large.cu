@@ -21,11 +21,14 @@
 // fraction; primes with few steps finish right there, primes with very many
 // steps (the smallest ones) go to a device list for heavy_kernel, one CTA per
 // prime, and the rest publish their rotation in shared memory for phase 2,
-// which spreads their steps over the CTA in items of kItemSteps.  Hits go
+// which spreads their steps over the CTA in items (2^item_shift steps; the
+// three step thresholds are the job's tuning, JobDev).  Hits go
 // through a valid-m bitmask and a live-offset bitmask held in shared memory;
 // only the survivors (a few percent) take their bitset row and column as
 // ranks in those masks (rank counts beside them, no table reads) and set one
 // bit of the L2-resident composite bitset with a global atomicOr.
+#include <algorithm>
+
 #include "pg_arith.cuh"
 #include "pg_internal.h"
 
@@ -34,9 +37,6 @@ namespace pg {
 namespace {
 
 constexpr int kLargeThreads = 256;
-constexpr uint64_t kDirectSteps = 24;
-constexpr uint32_t kItemSteps = 64;
-constexpr uint64_t kHeavySteps = 4096;
 
 // A walk hit (j, Y) is m = mstart + mi_base + stride*j, x = X + SL = xc - 2Y.
 // The masks are indexed by j and Y and stored as {bits, set bits before the
@@ -69,6 +69,7 @@ struct Marker {
 struct HeavyPrime {
     uint32_t mi0, y0, up, dn;
     uint64_t kp, kn, steps;
+    uint32_t job, pad;  // job index in a multi-job launch (0 for one job)
 };
 static_assert(sizeof(HeavyPrime) == kHeavyPrimeBytes, "heavy list stride");
 
@@ -108,6 +109,100 @@ __device__ __forceinline__ void load_masks(const JobDev &job, const uint2 *g_mma
     __syncthreads();
 }
 
+// One group of up to kLargeThreads primes of one job; the whole CTA calls it.
+// has: this thread holds a prime p with walk inputs a, b (the walk step and
+// start residue, or with kStartIn K' mod p and R^2 mod p, from which the
+// walk of K = K' * job.kmul starts here).  Phase 1 runs each prime's
+// continued fraction; few steps are walked at once, very many go to the
+// heavy list (tagged with job_tag), the rest are spread over the CTA as
+// items of 2^job.item_shift steps (phase 2).
+template <typename T, bool kStartIn>
+__device__ __forceinline__ void large_group(const JobDev &job, const Marker &mark, Slots<T> &sl, bool has,
+                                            T p, T a, T b, HeavyPrime *heavy,
+                                            unsigned long long *heavy_count, uint32_t heavy_cap,
+                                            uint32_t job_tag) {
+    const T w = (T)job.walk.w;
+    const uint64_t minc = job.walk.jmax;  // the walk runs over j, not mi
+    uint32_t items = 0;
+    if (has) {
+        T step, t0;
+        if constexpr (!kStartIn)
+            step = a, t0 = b;
+        else if constexpr (sizeof(T) == 4)
+            walk_start(job.walk, p, a, b, step, t0, job.kmul);
+        else
+            walk_start(job.walk, p, a, neg_inv64(p), b, step, t0, job.kmul);
+        const Entry<T> e = first_entry<T>(p, step, w, t0, minc);
+        if (e.t < minc && e.y < w) {
+            const uint64_t bound = rotation_steps_bound<T>(e.t, minc, e.g, p);
+            bool local = true;
+            if (bound <= job.direct_steps) {
+                // few steps: walk the rotation here
+                rotation_walk32((uint32_t)e.t, (uint32_t)e.y, gap32(e.g, (uint32_t)minc), (uint32_t)w,
+                                (uint32_t)minc, (uint32_t)bound, mark);
+                local = false;
+            } else if (bound > job.heavy_steps) {
+                // very many steps: one CTA of the heavy kernel takes this prime
+                const unsigned long long h = atomicAdd(heavy_count, 1ull);
+                if (h < heavy_cap) {
+                    heavy[h] = HeavyPrime{(uint32_t)e.t, (uint32_t)e.y, (uint32_t)e.g.up,
+                                          (uint32_t)e.g.dn, (uint64_t)e.g.kp,
+                                          (uint64_t)e.g.kn, bound, job_tag, 0u};
+                    local = false;
+                }
+            }
+            if (local) {
+                sl.mi0[threadIdx.x] = (uint32_t)e.t;
+                sl.y0[threadIdx.x] = (uint32_t)e.y;
+                sl.up[threadIdx.x] = (uint32_t)e.g.up;
+                sl.dn[threadIdx.x] = (uint32_t)e.g.dn;
+                sl.kp[threadIdx.x] = e.g.kp;
+                sl.kn[threadIdx.x] = e.g.kn;
+                items = (uint32_t)((bound + (1u << job.item_shift) - 1) >> job.item_shift);
+            }
+        }
+    }
+    // exclusive scan of item counts (skipped when the group has none):
+    // shuffle scan within each warp, then the warps' totals
+    if (!__syncthreads_or(items != 0)) return;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    uint32_t incl = items;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= (uint32_t)o) incl += v;
+    }
+    if (lane == 31) sl.warp_total[warp] = incl;
+    __syncthreads();
+    uint32_t before = 0, total = 0;
+#pragma unroll
+    for (int k = 0; k < kLargeThreads / 32; k++) {
+        const uint32_t t = sl.warp_total[k];
+        before += k < (int)warp ? t : 0u;
+        total += t;
+    }
+    sl.start[threadIdx.x + 1] = before + incl;
+    if (threadIdx.x == 0) sl.start[0] = 0;
+    __syncthreads();
+    for (uint32_t it = threadIdx.x; it < total; it += kLargeThreads) {
+        uint32_t lo = 0, hi = kLargeThreads;
+        while (hi - lo > 1) {
+            uint32_t mid = (lo + hi) >> 1;
+            if (sl.start[mid] <= it) lo = mid;
+            else hi = mid;
+        }
+        const uint32_t s = lo;
+        const uint32_t shift = job.item_shift;
+        const uint64_t n0 = (uint64_t)(it - sl.start[s]) << shift;
+        const ThreeGap<uint32_t> g =
+            gap32(ThreeGap<T>{sl.kp[s], (T)sl.up[s], sl.kn[s], (T)sl.dn[s]}, (uint32_t)minc);
+        uint32_t y, mi;
+        rotation_at32(sl.mi0[s], sl.y0[s], g, (uint32_t)n0, (uint32_t)minc, y, mi);
+        rotation_walk32(mi, y, g, (uint32_t)w, (uint32_t)minc, 1u << shift, mark);
+    }
+    __syncthreads();
+}
+
 template <typename T, bool kStartIn>
 __global__ void __launch_bounds__(kLargeThreads)
     large_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
@@ -127,8 +222,6 @@ __global__ void __launch_bounds__(kLargeThreads)
     off += range[0];
     a_in += range[0] - rrange[0];
     const T *b = (const T *)b_in + (range[0] - rrange[0]);  // R^2 mod p, or the start residue
-    const T w = (T)job.walk.w;
-    const uint64_t minc = job.walk.jmax;  // the walk runs over j, not mi
 
     for (;;) {
         if (threadIdx.x == 0) s_group = atomicAdd(group_ctr, 1ull);
@@ -136,84 +229,71 @@ __global__ void __launch_bounds__(kLargeThreads)
         const uint64_t group = s_group;
         if (group * kLargeThreads >= n) break;
         const uint64_t i = group * kLargeThreads + threadIdx.x;
-        uint32_t items = 0;
-        if (i < n) {
-            const T p = (T)(base + off[i]);
-            T step, t0;
-            if constexpr (!kStartIn)
-                step = a_in[i], t0 = b[i];
-            else if constexpr (sizeof(T) == 4)
-                walk_start(job.walk, p, a_in[i], b[i], step, t0, job.kmul);
-            else
-                walk_start(job.walk, p, a_in[i], neg_inv64(p), b[i], step, t0, job.kmul);
-            const Entry<T> e = first_entry<T>(p, step, w, t0, minc);
-            if (e.t < minc && e.y < w) {
-                const uint64_t bound = rotation_steps_bound<T>(e.t, minc, e.g, p);
-                bool local = true;
-                if (bound <= kDirectSteps) {
-                    // few steps: walk the rotation here
-                    rotation_walk32((uint32_t)e.t, (uint32_t)e.y, gap32(e.g, (uint32_t)minc), (uint32_t)w,
-                                    (uint32_t)minc, (uint32_t)bound, mark);
-                    local = false;
-                } else if (bound > kHeavySteps) {
-                    // very many steps: one CTA of heavy_kernel takes this prime
-                    const unsigned long long h = atomicAdd(heavy_count, 1ull);
-                    if (h < heavy_cap) {
-                        heavy[h] = HeavyPrime{(uint32_t)e.t, (uint32_t)e.y, (uint32_t)e.g.up,
-                                              (uint32_t)e.g.dn, (uint64_t)e.g.kp,
-                                              (uint64_t)e.g.kn, bound};
-                        local = false;
-                    }
+        const bool has = i < n;
+        const T p = has ? (T)(base + off[i]) : (T)0;
+        large_group<T, kStartIn>(job, mark, sl, has, p, has ? a_in[i] : (T)0, has ? b[i] : (T)0, heavy,
+                                 heavy_count, heavy_cap, 0u);
+    }
+}
+
+// Many jobs in one launch: CTAs claim tiles of kLargeThreads primes from a
+// device counter over the items (a job's primes in one prime-table window,
+// items in job order, tiles numbered consecutively), load the job's masks
+// into shared memory when the tile's job differs from their last one, and
+// run the group as the single-job kernel does, with the job's walk started
+// from K' mod p.  Every item has the same prime width (T).
+template <typename T>
+__global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
+    large_multi_kernel(const LargeJob *__restrict__ jobs, const LargeItem *__restrict__ items, uint32_t n_items,
+                       uint32_t n_tiles, unsigned long long *tile_ctr, HeavyPrime *heavy,
+                       unsigned long long *heavy_count, uint32_t heavy_cap) {
+    extern __shared__ uint2 s_masks[];
+    __shared__ Slots<T> sl;
+    __shared__ JobDev s_job;
+    __shared__ uint32_t s_tile, s_item;
+    __shared__ const uint2 *s_mm, *s_ym;
+    uint32_t loaded = ~0u;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            const uint32_t t = (uint32_t)atomicAdd(tile_ctr, 1ull);
+            s_tile = t;
+            if (t < n_tiles) {
+                uint32_t lo = 0, hi = n_items;  // last item with tile0 <= t
+                while (hi - lo > 1) {
+                    const uint32_t mid = (lo + hi) >> 1;
+                    if (items[mid].tile0 <= t) lo = mid;
+                    else hi = mid;
                 }
-                if (local) {
-                    sl.mi0[threadIdx.x] = (uint32_t)e.t;
-                    sl.y0[threadIdx.x] = (uint32_t)e.y;
-                    sl.up[threadIdx.x] = (uint32_t)e.g.up;
-                    sl.dn[threadIdx.x] = (uint32_t)e.g.dn;
-                    sl.kp[threadIdx.x] = e.g.kp;
-                    sl.kn[threadIdx.x] = e.g.kn;
-                    items = (uint32_t)((bound + kItemSteps - 1) / kItemSteps);
-                }
+                s_item = lo;
             }
         }
-        // exclusive scan of item counts (skipped when the group has none):
-        // shuffle scan within each warp, then the warps' totals
-        if (!__syncthreads_or(items != 0)) continue;
-        const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-        uint32_t incl = items;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            const uint32_t v = __shfl_up_sync(0xffffffffu, incl, o);
-            if (lane >= (uint32_t)o) incl += v;
-        }
-        if (lane == 31) sl.warp_total[warp] = incl;
         __syncthreads();
-        uint32_t before = 0, total = 0;
-#pragma unroll
-        for (int k = 0; k < kLargeThreads / 32; k++) {
-            const uint32_t t = sl.warp_total[k];
-            before += k < (int)warp ? t : 0u;
-            total += t;
-        }
-        sl.start[threadIdx.x + 1] = before + incl;
-        if (threadIdx.x == 0) sl.start[0] = 0;
-        __syncthreads();
-        for (uint32_t it = threadIdx.x; it < total; it += kLargeThreads) {
-            uint32_t lo = 0, hi = kLargeThreads;
-            while (hi - lo > 1) {
-                uint32_t mid = (lo + hi) >> 1;
-                if (sl.start[mid] <= it) lo = mid;
-                else hi = mid;
+        const uint32_t t = s_tile;
+        if (t >= n_tiles) break;
+        const LargeItem &it = items[s_item];
+        if (it.job != loaded) {
+            // another job: its descriptor and masks (all threads passed the
+            // barrier above, so nobody still reads the old ones)
+            const LargeJob &lj = jobs[it.job];
+            if (threadIdx.x == 0) s_job = lj.job;
+            const uint32_t mwords = (uint32_t)((lj.job.walk.jmax + 31) / 32), ywords = (lj.job.walk.w + 31) / 32;
+            if (lj.masks_in_shared) {
+                for (uint32_t i = threadIdx.x; i < mwords; i += blockDim.x) s_masks[i] = lj.mmask[i];
+                for (uint32_t i = threadIdx.x; i < ywords; i += blockDim.x) s_masks[mwords + i] = lj.ymask[i];
+                if (threadIdx.x == 0) s_mm = s_masks, s_ym = s_masks + mwords;
+            } else if (threadIdx.x == 0) {
+                s_mm = lj.mmask, s_ym = lj.ymask;
             }
-            const uint32_t s = lo;
-            const uint64_t n0 = (uint64_t)(it - sl.start[s]) * kItemSteps;
-            const ThreeGap<uint32_t> g =
-                gap32(ThreeGap<T>{sl.kp[s], (T)sl.up[s], sl.kn[s], (T)sl.dn[s]}, (uint32_t)minc);
-            uint32_t y, mi;
-            rotation_at32(sl.mi0[s], sl.y0[s], g, (uint32_t)n0, (uint32_t)minc, y, mi);
-            rotation_walk32(mi, y, g, (uint32_t)w, (uint32_t)minc, kItemSteps, mark);
+            loaded = it.job;
+            __syncthreads();
         }
-        __syncthreads();
+        const Marker mark{s_job, s_mm, s_ym};
+        const uint32_t i = (t - it.tile0) * kLargeThreads + threadIdx.x;
+        const bool has = i < it.count;
+        const T *a = (const T *)it.a, *b = (const T *)it.b;
+        const T p = has ? (T)(it.base + it.off[i]) : (T)0;
+        large_group<T, true>(s_job, mark, sl, has, p, has ? a[i] : (T)0, has ? b[i] : (T)0, heavy,
+                             heavy_count, heavy_cap, it.job);
     }
 }
 
@@ -231,13 +311,44 @@ __global__ void __launch_bounds__(kLargeThreads)
     const uint32_t w = job.walk.w;
     for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
         const HeavyPrime hp = heavy[h];
-        const uint32_t jmax = (uint32_t)job.walk.jmax;
+        const uint32_t jmax = (uint32_t)job.walk.jmax, shift = job.item_shift;
         const ThreeGap<uint32_t> g = gap32(ThreeGap<uint64_t>{hp.kp, hp.up, hp.kn, hp.dn}, jmax);
-        const uint64_t items = (hp.steps + kItemSteps - 1) / kItemSteps;
+        const uint64_t items = (hp.steps + (1u << shift) - 1) >> shift;
         for (uint64_t it = threadIdx.x; it < items; it += blockDim.x) {
             uint32_t y, mi;
-            rotation_at32(hp.mi0, hp.y0, g, (uint32_t)(it * kItemSteps), jmax, y, mi);
-            rotation_walk32(mi, y, g, w, jmax, kItemSteps, mark);
+            rotation_at32(hp.mi0, hp.y0, g, (uint32_t)(it << shift), jmax, y, mi);
+            rotation_walk32(mi, y, g, w, jmax, 1u << shift, mark);
+        }
+    }
+}
+
+// Heavy primes of many jobs: each entry carries its job; the masks are read
+// from global memory (L2), since consecutive entries of one CTA belong to
+// different jobs.
+__global__ void __launch_bounds__(kLargeThreads)
+    heavy_multi_kernel(const LargeJob *__restrict__ jobs, const HeavyPrime *__restrict__ heavy,
+                       const unsigned long long *heavy_count, uint32_t heavy_cap) {
+    __shared__ JobDev s_job;
+    __shared__ uint32_t s_loaded;
+    if (threadIdx.x == 0) s_loaded = ~0u;
+    const uint64_t nh = min((uint64_t)*heavy_count, (uint64_t)heavy_cap);
+    for (uint64_t h = blockIdx.x; h < nh; h += gridDim.x) {
+        const HeavyPrime hp = heavy[h];
+        __syncthreads();
+        if (threadIdx.x == 0 && s_loaded != hp.job) {
+            s_job = jobs[hp.job].job;
+            s_loaded = hp.job;
+        }
+        __syncthreads();
+        const LargeJob &lj = jobs[hp.job];
+        const Marker mark{s_job, lj.mmask, lj.ymask};
+        const uint32_t jmax = (uint32_t)s_job.walk.jmax, w = s_job.walk.w, shift = s_job.item_shift;
+        const ThreeGap<uint32_t> g = gap32(ThreeGap<uint64_t>{hp.kp, hp.up, hp.kn, hp.dn}, jmax);
+        const uint64_t items = (hp.steps + (1u << shift) - 1) >> shift;
+        for (uint64_t it = threadIdx.x; it < items; it += blockDim.x) {
+            uint32_t y, mi;
+            rotation_at32(hp.mi0, hp.y0, g, (uint32_t)(it << shift), jmax, y, mi);
+            rotation_walk32(mi, y, g, w, jmax, 1u << shift, mark);
         }
     }
 }
@@ -293,6 +404,34 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
     if (per_sm < 1) per_sm = 1;
     heavy_kernel<<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(
         job, scratch.heavy, heavy_count, scratch.heavy_cap, d_mmask, d_ymask, in_shared);
+    return cudaGetLastError();
+}
+
+cudaError_t large_multi(const LargeJob *d_jobs, const LargeItem *d_items, uint32_t n_items, uint32_t n_tiles,
+                        size_t smem, bool wide, LargeScratch scratch, cudaStream_t stream) {
+    if (n_tiles == 0) return cudaSuccess;
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(scratch.counters, 0, 2 * sizeof(unsigned long long), stream))) return e;
+    unsigned long long *tile_ctr = scratch.counters, *heavy_count = scratch.counters + 1;
+    auto launch = [&](auto kernel) -> cudaError_t {
+        cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err) return err;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kLargeThreads, smem);
+        if (per_sm < 1) per_sm = 1;
+        const uint64_t blocks = std::min<uint64_t>((uint64_t)sms * per_sm, n_tiles);
+        kernel<<<(unsigned)blocks, kLargeThreads, smem, stream>>>(d_jobs, d_items, n_items, n_tiles, tile_ctr,
+                                                                  scratch.heavy, heavy_count, scratch.heavy_cap);
+        return cudaGetLastError();
+    };
+    e = wide ? launch(large_multi_kernel<uint64_t>) : launch(large_multi_kernel<uint32_t>);
+    if (e) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heavy_multi_kernel, kLargeThreads, 0))) return e;
+    if (per_sm < 1) per_sm = 1;
+    heavy_multi_kernel<<<(unsigned)(sms * per_sm), kLargeThreads, 0, stream>>>(d_jobs, scratch.heavy, heavy_count,
+                                                                               scratch.heavy_cap);
     return cudaGetLastError();
 }
 

@@ -14,6 +14,9 @@ from pathlib import Path
 
 PKG = Path(__file__).resolve().parent
 LIB_PATH = Path(os.environ.get("PGSIEVE_LIB", PKG / "_build" / "libpgsieve.so"))
+# tuned knobs per (device, job class), loaded into every context; empty
+# PGSIEVE_TUNING turns it off, another path replaces it
+TUNING_PATH = os.environ.get("PGSIEVE_TUNING", str(PKG / "tuning.tsv"))
 HEADER = PKG.parent / "include" / "pgsieve.h"
 
 PGS_OK = 0
@@ -132,6 +135,22 @@ class GapResult(ctypes.Structure):
     ]
 
 
+class Tuning(ctypes.Structure):
+    """pgs_tuning: launch knobs per job class (output never depends on them)."""
+
+    _fields_ = [
+        ("direct_steps", ctypes.c_uint32),
+        ("item_steps", ctypes.c_uint32),
+        ("heavy_steps", ctypes.c_uint32),
+        ("rows_per_cta", ctypes.c_uint32),
+        ("text_chunks", ctypes.c_uint32),
+        ("kmod_lsb_limbs", ctypes.c_uint32),
+    ]
+
+    def as_dict(self) -> dict:
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class GapStats(ctypes.Structure):
     _fields_ = [
         ("rounds", ctypes.c_uint64),
@@ -220,6 +239,14 @@ _SIGNATURES = {
                                        ctypes.POINTER(ctypes.c_double)]),
     "pgs_server_stats_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ServerStats)]),
     "pgs_server_stop": (ctypes.c_int, [ctypes.c_void_p]),
+    "pgs_tuning_default": (None, [ctypes.c_void_p]),
+    "pgs_tuning_class": (ctypes.c_int, [ctypes.POINTER(Job), ctypes.c_char_p, ctypes.c_size_t]),
+    "pgs_tuning_set": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_void_p]),
+    "pgs_tuning_get": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_void_p]),
+    "pgs_tuning_load": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "pgs_tuning_save": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_char_p]),
+    "pgs_tune": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.c_int, ctypes.c_void_p,
+                                ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib: ctypes.CDLL | None = None
@@ -267,6 +294,21 @@ def plan(job: JobSpec) -> dict:
     }
 
 
+def tuning_class(job: JobSpec) -> str:
+    """The job's tuning class, P<p>.SL<log2 SL>.minc<log2 minc>."""
+    buf = ctypes.create_string_buffer(64)
+    n = load().pgs_tuning_class(ctypes.byref(job.c()), buf, 64)
+    if n < 0:
+        raise PgsError(n, "pgs_tuning_class")
+    return buf.value.decode()
+
+
+def tuning_default() -> dict:
+    t = Tuning()
+    load().pgs_tuning_default(ctypes.byref(t))
+    return t.as_dict()
+
+
 def _arr(ctype, values):
     a = (ctype * max(1, len(values)))()
     for i, v in enumerate(values):
@@ -277,13 +319,49 @@ def _arr(ctype, values):
 class Sieve:
     """One library context on a CUDA device."""
 
-    def __init__(self, device: int = 0):
+    def __init__(self, device: int = 0, load_tuning: bool = True):
         self.lib = load()
         h = ctypes.c_void_p()
         rc = self.lib.pgs_create(device, ctypes.byref(h))
         if rc != PGS_OK:
             raise PgsError(rc, "pgs_create failed (no usable CUDA device?)")
         self.h = h
+        if load_tuning and TUNING_PATH and Path(TUNING_PATH).exists():
+            self.lib.pgs_tuning_load(self.h, str(TUNING_PATH).encode())
+
+    # -- tuning (pgs_tuning_*, pgs_tune) --------------------------------------
+
+    def tune(self, job: JobSpec, reps: int = 3) -> tuple[dict, float, float]:
+        """Tune the job's class on this device: (knobs, ms with the
+        defaults, ms with the knobs)."""
+        t = Tuning()
+        a, b = ctypes.c_double(), ctypes.c_double()
+        self._check(self.lib.pgs_tune(self.h, ctypes.byref(job.c()), reps, ctypes.byref(t), ctypes.byref(a),
+                                      ctypes.byref(b)))
+        return t.as_dict(), a.value, b.value
+
+    def tuning_get(self, job: JobSpec) -> tuple[dict, bool]:
+        t = Tuning()
+        rc = self.lib.pgs_tuning_get(self.h, ctypes.byref(job.c()), ctypes.byref(t))
+        if rc < 0:
+            self._check(rc)
+        return t.as_dict(), rc == 1
+
+    def tuning_set(self, job: JobSpec, knobs: dict) -> None:
+        t = Tuning(**{**tuning_default(), **knobs})
+        self._check(self.lib.pgs_tuning_set(self.h, ctypes.byref(job.c()), ctypes.byref(t)))
+
+    def tuning_load(self, path: str | os.PathLike) -> int:
+        rc = self.lib.pgs_tuning_load(self.h, str(path).encode())
+        if rc < 0:
+            self._check(rc)
+        return rc
+
+    def tuning_save(self, path: str | os.PathLike) -> int:
+        rc = self.lib.pgs_tuning_save(self.h, str(path).encode())
+        if rc < 0:
+            self._check(rc)
+        return rc
 
     def close(self) -> None:
         if self.h:

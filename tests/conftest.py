@@ -29,6 +29,7 @@ def built():
     pkg_build.build_lib()
     pkg_build.build_oracle()
     pkg_build.build_arith_host()
+    pkg_build.build_tune_host()
     return True
 
 
