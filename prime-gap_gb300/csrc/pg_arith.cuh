@@ -87,6 +87,103 @@ PG_HD uint32_t umulhi32(uint32_t a, uint32_t b) {
 #endif
 }
 
+// ---------------------------------------------------------------------------
+// two 32-bit quotients by one divisor
+//
+// Division by multiplication with an approximate reciprocal and a remainder
+// correction (Granlund & Montgomery, "Division by invariant integers using
+// multiplication", PLDI 1994).  r = floor(x), x = 2^32 (1 - 2^-19) / d in
+// single precision: a reciprocal of at most 1 ulp error (rcp.approx) of d
+// rounded toward zero, times 2^32 - 2^13 rounded toward zero.  Then
+//   2^32/d (1 - 2^-18) - 1 <= r < 2^32/d,
+// so q0 = floor(n r / 2^32) never exceeds q = floor(n / d), and while
+// q < 2^18 it is at most 2 below it (n/d - n r/2^32 < (n/d) 2^-18 + 1 < 2);
+// q0 < 2^17 implies q < 2^18.  Two remainder tests per quotient finish it;
+// a larger q0 (a continued-fraction quotient of 2^17 or more, rare) takes
+// the exact division.  One reciprocal (three conversion/transcendental-unit
+// operations) serves both quotients, where two hardware divisions each
+// need their own.
+
+// single-precision steps with explicit rounding; the host forms compute the
+// same roundings exactly (the reciprocal within the device's 1-ulp bound)
+PG_HD float u32_to_f32_rz(uint32_t v) {
+#if defined(__CUDA_ARCH__)
+    return __uint2float_rz(v);
+#else
+    float f = (float)v;
+    if ((double)f > (double)v) f = nextafterf(f, 0.0f);
+    return f;
+#endif
+}
+PG_HD float rcp_approx(float x) {
+#if defined(__CUDA_ARCH__)
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+#else
+    return 1.0f / x;
+#endif
+}
+PG_HD float mul_f32_rz(float a, float b) {
+#if defined(__CUDA_ARCH__)
+    return __fmul_rz(a, b);
+#else
+    const double e = (double)a * (double)b;  // exact: 24 + 24 bits
+    float f = (float)e;
+    if ((double)f > e) f = nextafterf(f, 0.0f);
+    return f;
+#endif
+}
+PG_HD uint32_t f32_to_u32_rz(float x) {
+#if defined(__CUDA_ARCH__)
+    return __float2uint_rz(x);
+#else
+    return (uint32_t)x;
+#endif
+}
+
+// r of the comment above for d >= 1.  `skew` (host tests only) moves the
+// reciprocal by that many ulps to cover the device's error bound.
+PG_HD uint32_t recip32(uint32_t d, int skew = 0) {
+    float rf = rcp_approx(u32_to_f32_rz(d));
+#if !defined(__CUDA_ARCH__)
+    for (; skew > 0; skew--) rf = nextafterf(rf, 2.0f);
+    for (; skew < 0; skew++) rf = nextafterf(rf, 0.0f);
+#else
+    (void)skew;
+#endif
+    return f32_to_u32_rz(mul_f32_rz(rf, 4294959104.0f));  // 2^32 - 2^13
+}
+
+PG_HD void udiv2_32(uint32_t n1, uint32_t n2, uint32_t d, uint32_t &q1, uint32_t &q2, int skew = 0) {
+    const uint32_t r = recip32(d, skew);
+    uint32_t a = umulhi32(n1, r), b = umulhi32(n2, r);
+    if ((a | b) >= (1u << 17)) {
+        q1 = n1 / d;
+        q2 = n2 / d;
+        return;
+    }
+    uint32_t ra = n1 - a * d, rb = n2 - b * d;
+    if (ra >= d) a++, ra -= d;
+    if (ra >= d) a++;
+    if (rb >= d) b++, rb -= d;
+    if (rb >= d) b++;
+    q1 = a;
+    q2 = b;
+}
+
+// 2^32 mod p for odd p >= 3 without a hardware division.  p >= 2^31: 2^32 - p.
+// 2^16 <= p < 2^31: q0 = recip32(p) is at most floor(2^32/p) and at most one
+// below it ((2^32/p) 2^-18 + 1 < 2), so 2^32 - q0 p lies in [0, 3p) and two
+// conditional subtractions finish it.  Smaller p: the remainder operator.
+PG_HD uint32_t pow32_mod(uint32_t p, int skew = 0) {
+    if (p >= 0x80000000u) return 0u - p;
+    if (p < (1u << 16)) return (0u - p) % p;
+    uint32_t r = 0u - recip32(p, skew) * p;
+    r = r >= p ? r - p : r;
+    return r >= p ? r - p : r;
+}
+
 PG_HD uint32_t redc32(uint64_t t, uint32_t p, uint32_t pinv) {
     const uint32_t lo = (uint32_t)t, hi = (uint32_t)(t >> 32);
     const uint32_t m = lo * pinv;
@@ -149,7 +246,7 @@ PG_HD void kmod32_multi(const uint32_t *limbs, int n, const uint32_t *p, uint32_
 #pragma unroll
     for (int k = 0; k < NP; k++) {
         pinv[k] = neg_inv32(p[k]);
-        const uint32_t r1 = (0u - p[k]) % p[k];
+        const uint32_t r1 = pow32_mod(p[k]);
         r2[k] = r2_from_r1(r1, p[k], pinv[k]);
         u[k] = 0;
         lazy = lazy && p[k] < 0x80000000u;
@@ -217,7 +314,7 @@ PG_HD void kmod32_lsb_multi(const uint32_t *limbs, int n, const uint32_t *p, uin
 #pragma unroll
     for (int k = 0; k < NP; k++) {
         pinv[k] = neg_inv32(p[k]);
-        r2[k] = r2_from_r1((0u - p[k]) % p[k], p[k], pinv[k]);
+        r2[k] = r2_from_r1(pow32_mod(p[k]), p[k], pinv[k]);
         W[k] = 0;
     }
     for (int i = 0; i < n; i++) {
@@ -564,91 +661,6 @@ PG_HD void walk_start(const WalkParams &wk, uint64_t p, uint64_t r, uint64_t pin
 
 
 // ---------------------------------------------------------------------------
-// two 32-bit quotients by one divisor
-//
-// Division by multiplication with an approximate reciprocal and a remainder
-// correction (Granlund & Montgomery, "Division by invariant integers using
-// multiplication", PLDI 1994).  r = floor(x), x = 2^32 (1 - 2^-19) / d in
-// single precision: a reciprocal of at most 1 ulp error (rcp.approx) of d
-// rounded toward zero, times 2^32 - 2^13 rounded toward zero.  Then
-//   2^32/d (1 - 2^-18) - 1 <= r < 2^32/d,
-// so q0 = floor(n r / 2^32) never exceeds q = floor(n / d), and while
-// q < 2^18 it is at most 2 below it (n/d - n r/2^32 < (n/d) 2^-18 + 1 < 2);
-// q0 < 2^17 implies q < 2^18.  Two remainder tests per quotient finish it;
-// a larger q0 (a continued-fraction quotient of 2^17 or more, rare) takes
-// the exact division.  One reciprocal (three conversion/transcendental-unit
-// operations) serves both quotients, where two hardware divisions each
-// need their own.
-
-// single-precision steps with explicit rounding; the host forms compute the
-// same roundings exactly (the reciprocal within the device's 1-ulp bound)
-PG_HD float u32_to_f32_rz(uint32_t v) {
-#if defined(__CUDA_ARCH__)
-    return __uint2float_rz(v);
-#else
-    float f = (float)v;
-    if ((double)f > (double)v) f = nextafterf(f, 0.0f);
-    return f;
-#endif
-}
-PG_HD float rcp_approx(float x) {
-#if defined(__CUDA_ARCH__)
-    float r;
-    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
-    return r;
-#else
-    return 1.0f / x;
-#endif
-}
-PG_HD float mul_f32_rz(float a, float b) {
-#if defined(__CUDA_ARCH__)
-    return __fmul_rz(a, b);
-#else
-    const double e = (double)a * (double)b;  // exact: 24 + 24 bits
-    float f = (float)e;
-    if ((double)f > e) f = nextafterf(f, 0.0f);
-    return f;
-#endif
-}
-PG_HD uint32_t f32_to_u32_rz(float x) {
-#if defined(__CUDA_ARCH__)
-    return __float2uint_rz(x);
-#else
-    return (uint32_t)x;
-#endif
-}
-
-// r of the comment above for d >= 1.  `skew` (host tests only) moves the
-// reciprocal by that many ulps to cover the device's error bound.
-PG_HD uint32_t recip32(uint32_t d, int skew = 0) {
-    float rf = rcp_approx(u32_to_f32_rz(d));
-#if !defined(__CUDA_ARCH__)
-    for (; skew > 0; skew--) rf = nextafterf(rf, 2.0f);
-    for (; skew < 0; skew++) rf = nextafterf(rf, 0.0f);
-#else
-    (void)skew;
-#endif
-    return f32_to_u32_rz(mul_f32_rz(rf, 4294959104.0f));  // 2^32 - 2^13
-}
-
-PG_HD void udiv2_32(uint32_t n1, uint32_t n2, uint32_t d, uint32_t &q1, uint32_t &q2, int skew = 0) {
-    const uint32_t r = recip32(d, skew);
-    uint32_t a = umulhi32(n1, r), b = umulhi32(n2, r);
-    if ((a | b) >= (1u << 17)) {
-        q1 = n1 / d;
-        q2 = n2 / d;
-        return;
-    }
-    uint32_t ra = n1 - a * d, rb = n2 - b * d;
-    if (ra >= d) a++, ra -= d;
-    if (ra >= d) a++;
-    if (rb >= d) b++, rb -= d;
-    if (rb >= d) b++;
-    q1 = a;
-    q2 = b;
-}
-
-// ---------------------------------------------------------------------------
 // first entry and three-gap data in one continued-fraction pass
 //
 // The subtractive continued fraction of three_gap is a Rauzy induction of the
@@ -685,9 +697,13 @@ PG_HD Entry<T> first_entry(T p, T a, T w, T y0, uint64_t t_lim = ~0ull) {
     T kp = 1, up = a, kn = 1, dn = p - a;
     T y = y0;
     uint64_t t = 0;
-    for (int pass = 0; pass < 256 && (up >= w || dn >= w); pass++) {
+    // Every level with q >= 1 lowers big by at least small >= 1 (small stays
+    // positive: for a modulus sharing a factor with a, up == dn stops the
+    // descent with q == 0 before either reaches 0), so the loop ends.
+    for (;;) {
         const bool A = up > dn;
         T big = A ? up : dn;
+        if (big < w) break;  // up, dn < w: the last level
         const T small = A ? dn : up;
         T kbig = A ? kp : kn;
         const T ksmall = A ? kn : kp;

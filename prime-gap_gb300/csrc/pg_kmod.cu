@@ -110,7 +110,7 @@ __global__ void __launch_bounds__(kKmodThreads)
         for (int k = 0; k < kPrimesPerThread; k++) {
             p[k] = idx0 + k < n ? (uint32_t)(base + off[idx0 + k]) : 3u;  // pad with a prime
             pinv[k] = neg_inv32(p[k]);
-            r2[k] = r2_from_r1((0u - p[k]) % p[k], p[k], pinv[k]);
+            r2[k] = r2_from_r1(pow32_mod(p[k]), p[k], pinv[k]);
             acc[k] = 0;
             lazy = lazy && p[k] < 0x80000000u;
         }

@@ -298,4 +298,7 @@ void ah_udiv2(uint32_t n1, uint32_t n2, uint32_t d, int skew, uint32_t *out2) {
     pg::udiv2_32(n1, n2, d, out2[0], out2[1], skew);
 }
 
+// 2^32 mod p through the approximate reciprocal (K mod p setup).
+uint32_t ah_pow32_mod(uint32_t p, int skew) { return pg::pow32_mod(p, skew); }
+
 }

@@ -39,6 +39,8 @@ def ah(built):
     lib.ah_hits_grid.restype = ctypes.c_size_t
     lib.ah_hits_grid.argtypes = [u64, ctypes.c_uint32, ctypes.c_uint32, u64, u64, u64, u64,
                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
+    lib.ah_pow32_mod.restype = ctypes.c_uint32
+    lib.ah_pow32_mod.argtypes = [ctypes.c_uint32, ctypes.c_int]
     lib.ah_udiv2.restype = None
     lib.ah_udiv2.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                              ctypes.POINTER(ctypes.c_uint32)]
@@ -442,3 +444,15 @@ def test_udiv2_shared_reciprocal_exact(ah):
         for skew in (-2, -1, 0, 1, 2):
             ah.ah_udiv2(n1, n2, d, skew, out)
             assert (out[0], out[1]) == (n1 // d, n2 // d), (n1, n2, d, skew)
+
+
+def test_pow32_mod_without_division(ah):
+    """2^32 mod p of the K mod p setup (reciprocal and two subtractions) for
+    odd p across the three ranges and their edges, reciprocal skewed up to
+    2 ulps either way."""
+    rng = random.Random(8)
+    ps = [3, 5, 65535, 65537, 65539, (1 << 31) - 1, (1 << 31) + 1, (1 << 32) - 5, (1 << 32) - 1]
+    ps += [rng.randrange(1, 1 << b) | 1 for b in (17, 20, 24, 28, 31, 32) for _ in range(3000)]
+    for p in ps:
+        for skew in (-2, 0, 2):
+            assert ah.ah_pow32_mod(p, skew) == (1 << 32) % p, (p, skew)
