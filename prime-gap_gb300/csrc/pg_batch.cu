@@ -715,6 +715,11 @@ int plan_batch(pgs_ctx *ctx, pgs_batch *b, cudaStream_t s) {
     }
     std::map<int, std::vector<size_t>> q_of_job;
     for (size_t i = 0; i < qjob.size(); i++) q_of_job[qjob[i].first].push_back(i);
+    for (int j = 0; j < n; j++) {  // the large primes each job sieves (its result's prime count)
+        uint64_t c = 0;
+        for (size_t i : q_of_job[j]) c += rg[nq_chain + i].second - rg[nq_chain + i].first;
+        b->jobs[j]->large_primes = c;
+    }
     for (pgs_batch::Chunk *ch : b->chunks) {
         std::vector<pg::LargeItem> it32, it64;
         for (int j : ch->jobs)
@@ -775,7 +780,7 @@ int job_setup(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s) {
     pr->launches++;
     if (pr->sp_bound) {
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), nl, 0, t.small.as<uint32_t>(), misc + 1, pr->sp_bound, nullptr,
-                           pr->sr.p, nullptr, false, s));
+                           pr->sr.p, nullptr, false, s, 0, h.klimbs.data()));
         pr->launches++;
     }
     if (!h.dq.empty()) {
@@ -830,7 +835,8 @@ int launch_batch(pgs_ctx *ctx, pgs_batch *b) {
         CK(pg::kmod_chain(b->chain_limbs.as<uint32_t>() + b->limb_base[c->chain],
                           b->chain_off.as<uint32_t>() + b->off_base[c->chain], (int)ch.P.size(), (int)ch.limbs.size(),
                           w.lo, w.off.as<uint32_t>() + c->begin, c->count, c->r.p,
-                          (char *)c->r.p + ch.P.size() * c->count * width, c->wide, s0));
+                          (char *)c->r.p + ch.P.size() * c->count * width, c->wide, s0, ch.limbs.data(),
+                          ch.seg_off.data()));
     }
     const pg::LargeScratch scr{b->counters.as<unsigned long long>(), b->heavy.as<pg::HeavyPrime>(),
                                pg::heavy_capacity()};

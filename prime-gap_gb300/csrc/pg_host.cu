@@ -355,6 +355,10 @@ int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out, c
     const size_t nr = job_ranges(pr);
     std::vector<uint64_t> misc(1 + 2 * nr);
     CK(cudaMemcpyAsync(misc.data(), pr->misc.p, misc.size() * 8, cudaMemcpyDeviceToHost, s));
+    // per-row unknown counts: their sum is the result's total
+    std::vector<uint32_t> counts(2 * h.valid_mi.size());
+    if (!counts.empty())
+        CK(cudaMemcpyAsync(counts.data(), pr->counts.p, counts.size() * 4, cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
     const uint64_t total = given ? given->total : misc[0];
     if (total > pr->text_cap) {
@@ -391,8 +395,16 @@ int fetch_job(pgs_ctx *ctx, pgs_prepared *pr, cudaStream_t s, pgs_result *out, c
     out->text_len = total;
     out->internal = new PinnedOwner{cap};
     out->rows = h.valid_mi.size();
+    // (low, high) per row; bitcompressed rows keep (unknowns, bytes)
+    uint64_t unknowns = 0;
+    const size_t step = h.job.compression == 2 ? 2 : 1;
+    for (size_t i = 0; i < counts.size(); i += step) unknowns += counts[i];
+    out->unknowns = unknowns;
     uint64_t primes = h.primes_to_P;
-    for (size_t i = 0; i < nr; i++) primes += misc[2 + 2 * i] - misc[1 + 2 * i];
+    if (pr->large_primes != ~0ull)
+        primes += misc[2] - misc[1] + pr->large_primes;  // small-prime range, then the host's count
+    else
+        for (size_t i = 0; i < nr; i++) primes += misc[2 + 2 * i] - misc[1 + 2 * i];
     out->primes = primes;
     out->prime_limit = h.prime_limit;
     out->launches = pr->launches;

@@ -222,6 +222,10 @@ struct pgs_prepared {
     bool table_mode = false;
     uint64_t tbl_a = 0, tbl_b = 0;
     std::vector<int> tbl_windows;
+    // primes above the small phase that the job sieves, when the host knows
+    // them (the batch finds every range at prepare time); ~0 when they are
+    // read from the job's range words on the device
+    uint64_t large_primes = ~0ull;
     size_t footprint = 0;  // device bytes held by this job
     uint64_t win_bound = 0;
     pgh::DevBuf klimbs, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0, mmask, ymask;

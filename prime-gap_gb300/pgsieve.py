@@ -690,6 +690,7 @@ def _result_stats(res: Result) -> dict:
         "text_len": res.text_len,
         "rows": res.rows,
         "primes": res.primes,
+        "unknowns": res.unknowns,
         "prime_limit": res.prime_limit,
         "ms_total": res.ms_total,
         "ms_stage": {STAGES[i]: res.ms_stage[i] for i in range(8)},

@@ -44,6 +44,26 @@ def test_batch_goldens(sieve, goldens):
             assert hashlib.md5(b.fetch(i)).hexdigest() == goldens[n]["md5"], n
 
 
+def test_batch_result_counts_match_plain(sieve):
+    """Each batched job reports the rows, sieving primes and unknowns of the
+    same job run alone (the bench's pairs come from these counts)."""
+    jobs = _small_mix(8, 21) + [pgsieve.JobSpec(503, 210, 1234567, 300, 5000, 4_400_000_000)]
+    want = []
+    for j in jobs:
+        st: dict = {}
+        with sieve.prepare(j) as prep:
+            prep.run(False)
+            prep.fetch(st)
+        want.append((st["rows"], st["primes"], st["unknowns"]))
+    with sieve.batch(jobs, lanes=4) as b:
+        b.run(graph=True)
+        for i in range(len(jobs)):
+            with b.fetch_view(i) as v:
+                assert (v.res.rows, v.res.primes, v.res.unknowns) == want[i], jobs[i]
+    for j, w in zip(jobs, want):
+        assert pgsieve.plan(j)["valid_ms"] == w[0]
+
+
 def test_batch_graph_replay_matches_plain(sieve):
     jobs = _small_mix(16, 11)
     want = [sieve.method2(j) for j in jobs]

@@ -117,6 +117,24 @@ def test_method2_text_pipeline_short_estimate(sieve, goldens, name, monkeypatch)
     assert len(data) == g["bytes"]
 
 
+@pytest.mark.parametrize("name", ["fn1", "fn1_rle", "fn1_bitcompressed", "small_d7_odd"])
+def test_result_unknowns_count(sieve, goldens, name):
+    """pgs_result.unknowns is the number of unknown offsets in the file: the
+    header counts of the plain text, whatever the compression."""
+    g = goldens[name]
+    st: dict = {}
+    with sieve.prepare(_spec(g)) as prep:
+        prep.run(False)
+        prep.fetch(st)
+    plain = pgo.method2(g["p"], g["d"], g["mstart"], g["minc"], g["sieve_length"], g["max_prime"], 0,
+                        threads=16).decode()
+    total = 0
+    for line in plain.splitlines():
+        head = line.split("|")[0].split(":")[1].split()
+        total += -int(head[0]) + int(head[1])
+    assert st["unknowns"] == total
+
+
 def test_prepare_run_fetch_repeatable(sieve, goldens):
     g = goldens["fn1"]
     with sieve.prepare(_spec(g)) as prep:
