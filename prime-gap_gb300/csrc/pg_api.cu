@@ -365,7 +365,7 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
         span(PGS_STAGE_PRIMES, a, b);
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), pr->sp_lo,
                            pr->sp.as<uint32_t>(), misc + 1, pr->sp_bound, nullptr, pr->sr.p,
-                           nullptr, false, s));
+                           nullptr, false, s, 0, h.klimbs.data()));
         CK(mark(a));
         span(PGS_STAGE_KMOD, b, a);
         pr->launches += 2;
@@ -385,7 +385,7 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
         CK(mark(e_b));
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
                            ctx->win_off.as<uint32_t>(), rng, win.bound, &h.walk, ctx->win_r.p,
-                           ctx->win_t0.p, win.wide, s, (int)pr->tune.kmod_lsb_limbs));
+                           ctx->win_t0.p, win.wide, s, (int)pr->tune.kmod_lsb_limbs, h.klimbs.data()));
         CK(mark(e_c));
         CK(pg::large_window(job, win.lo, ctx->win_off.as<uint32_t>(), rng, win.bound, ctx->win_r.p,
                             ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint2>(),

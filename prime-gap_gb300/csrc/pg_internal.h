@@ -61,18 +61,22 @@ cudaError_t set_pair(unsigned long long *d_out, uint64_t a, uint64_t b, cudaStre
 // (wide).  K limbs on the device.
 // lsb_min_limbs > 0: the least-significant-first chain from that many limbs
 // (32-bit primes; 64-bit primes from three quarters of it), else the built-in
-// thresholds.
+// thresholds.  h_klimbs: the same limbs on the host; up to 1024 of them go
+// in the launch's parameters instead of shared memory.
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
                         const unsigned long long *d_range, uint64_t max_count,
                         const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream,
-                        int lsb_min_limbs = 0);
+                        int lsb_min_limbs = 0, const uint32_t *h_klimbs = nullptr);
 
 // K'_g mod p for the G groups of a chain (K'_g = K'_(g-1) * S_g, segment g's
 // limbs at d_seg_limbs[d_seg_off[g] .. d_seg_off[g+1]), little-endian) for
 // the n primes base + d_off[i]: r_g at d_r[g * n + i], R^2 mod p at
 // d_r2[i], words of the primes' width.  nlimbs + G + 1 <= 12288.
+// h_seg_limbs / h_seg_off: the same words on the host, passed in the
+// launch's parameters when they fit (1024 words).
 cudaError_t kmod_chain(const uint32_t *d_seg_limbs, const uint32_t *d_seg_off, int G, int nlimbs, uint64_t base,
-                       const uint32_t *d_off, uint64_t n, void *d_r, void *d_r2, bool wide, cudaStream_t stream);
+                       const uint32_t *d_off, uint64_t n, void *d_r, void *d_r2, bool wide, cudaStream_t stream,
+                       const uint32_t *h_seg_limbs = nullptr, const uint32_t *h_seg_off = nullptr);
 
 // K mod q for an explicit list of 32-bit primes (d-primes, tests).
 cudaError_t kmod_list32(const uint32_t *d_klimbs, int nlimbs, const uint32_t *d_q, uint32_t n,

@@ -14,6 +14,7 @@
 // this K without a division; or, for one job, its walk step and start residue directly
 // ((base_r * M + SL) % prime, modulo_search.cpp:345; see WalkParams).
 #include <algorithm>
+#include <cstring>
 
 #include "pg_arith.cuh"
 #include "pg_internal.h"
@@ -28,17 +29,32 @@ constexpr int kPrimesPerThread = 4;     // 32-bit primes
 constexpr int kLsbMinLimbs = 32;        // 32-bit primes: LSB chain from 32 limbs
 constexpr int kLsbMinLimbsWide = 24;    // 64-bit primes: from 12 words
 
-template <bool kWide, bool kLsb>
+// K's limbs as a kernel parameter (constant bank, read as warp-uniform
+// loads): no shared-memory fill and no barrier at the start of every CTA.
+constexpr int kParamLimbs = 1024;
+template <int N>
+struct KLimbs {
+    uint32_t limb[N];
+};
+
+// kParam: K's limbs come in `kl` (nlimbs <= kParamLimbs); otherwise they are
+// copied from klimbs to shared memory (or read from global when too long).
+template <bool kWide, bool kLsb, bool kParam>
 __global__ void __launch_bounds__(kKmodThreads)
-    kmod_kernel(const uint32_t *__restrict__ klimbs, int nlimbs, uint64_t base,
-                const uint32_t *__restrict__ off, const unsigned long long *range,
+    kmod_kernel(const __grid_constant__ KLimbs<kParam ? kParamLimbs : 1> kl, const uint32_t *__restrict__ klimbs,
+                int nlimbs, uint64_t base, const uint32_t *__restrict__ off, const unsigned long long *range,
                 uint64_t max_count, WalkParams walk, int with_walk, void *a_out, void *b_out) {
     extern __shared__ uint32_t s_limbs[];
-    const bool in_shared = nlimbs <= kMaxSharedLimbs;
-    if (in_shared)
-        for (int i = threadIdx.x; i < nlimbs; i += blockDim.x) s_limbs[i] = klimbs[i];
-    __syncthreads();
-    const uint32_t *limbs = in_shared ? s_limbs : klimbs;
+    const uint32_t *limbs;
+    if constexpr (kParam) {
+        limbs = kl.limb;
+    } else {
+        const bool in_shared = nlimbs <= kMaxSharedLimbs;
+        if (in_shared)
+            for (int i = threadIdx.x; i < nlimbs; i += blockDim.x) s_limbs[i] = klimbs[i];
+        __syncthreads();
+        limbs = in_shared ? s_limbs : klimbs;
+    }
     // primes off[range[0] .. range[1]), never more than the list's capacity
     const uint64_t begin = range[0];
     const uint64_t n = min((uint64_t)(range[1] - begin), max_count);
@@ -90,15 +106,25 @@ __global__ void __launch_bounds__(kKmodThreads)
 // form, one REDC with R^2).  One pass over K'_G's limbs serves every group,
 // instead of one reduction of each K'_g.  Writes r_g at r_out[g * stride + i]
 // and R^2 mod p at r2_out[i] (R = 2^32 or 2^64, the primes' width).
-template <bool kWide>
+// The segments' limbs and then their G + 1 offsets arrive in the launch's
+// parameters (kl) when they fit, else from seg_limbs / seg_off through
+// shared memory.
+template <bool kWide, bool kParam>
 __global__ void __launch_bounds__(kKmodThreads)
-    kmod_chain_kernel(const uint32_t *__restrict__ seg_limbs, const uint32_t *__restrict__ seg_off, int G,
+    kmod_chain_kernel(const __grid_constant__ KLimbs<kParam ? kParamLimbs : 1> kl,
+                      const uint32_t *__restrict__ seg_limbs, const uint32_t *__restrict__ seg_off, int G,
                       int nlimbs, uint64_t base, const uint32_t *__restrict__ off, uint64_t n, void *r_out,
                       void *r2_out) {
-    extern __shared__ uint32_t s_limbs[];  // nlimbs limbs, then G + 1 segment offsets
-    for (int i = threadIdx.x; i < nlimbs; i += blockDim.x) s_limbs[i] = seg_limbs[i];
-    for (int i = threadIdx.x; i <= G; i += blockDim.x) s_limbs[nlimbs + i] = seg_off[i];
-    __syncthreads();
+    extern __shared__ uint32_t s_words[];  // nlimbs limbs, then G + 1 segment offsets
+    const uint32_t *s_limbs;
+    if constexpr (kParam) {
+        s_limbs = kl.limb;
+    } else {
+        for (int i = threadIdx.x; i < nlimbs; i += blockDim.x) s_words[i] = seg_limbs[i];
+        for (int i = threadIdx.x; i <= G; i += blockDim.x) s_words[nlimbs + i] = seg_off[i];
+        __syncthreads();
+        s_limbs = s_words;
+    }
     const uint32_t *so = s_limbs + nlimbs;
     if (!kWide) {
         uint32_t *ro = (uint32_t *)r_out;
@@ -190,7 +216,7 @@ __global__ void __launch_bounds__(kKmodThreads)
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
                         const unsigned long long *d_range, uint64_t max_count,
                         const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream,
-                        int lsb_min_limbs) {
+                        int lsb_min_limbs, const uint32_t *h_klimbs) {
     if (max_count == 0) return cudaSuccess;
     const WalkParams wp = walk ? *walk : WalkParams{};
     const int ww = walk != nullptr;
@@ -204,18 +230,28 @@ cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, con
     const int lsb_min = lsb_min_limbs > 0 ? (wide ? std::max(1, lsb_min_limbs * 3 / 4) : lsb_min_limbs)
                                           : (wide ? kLsbMinLimbsWide : kLsbMinLimbs);
     const bool lsb = nlimbs >= lsb_min;
-    if (wide && lsb)
-        kmod_kernel<true, true><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
-                                                                        d_range, max_count, wp, ww, d_a, d_b);
-    else if (wide)
-        kmod_kernel<true, false><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
-                                                                         d_range, max_count, wp, ww, d_a, d_b);
-    else if (lsb)
-        kmod_kernel<false, true><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
-                                                                         d_range, max_count, wp, ww, d_a, d_b);
-    else
-        kmod_kernel<false, false><<<blocks, kKmodThreads, smem, stream>>>(d_klimbs, nlimbs, base, d_off,
-                                                                          d_range, max_count, wp, ww, d_a, d_b);
+    if (h_klimbs && nlimbs <= kParamLimbs) {
+        KLimbs<kParamLimbs> kl;
+        memcpy(kl.limb, h_klimbs, (size_t)nlimbs * sizeof(uint32_t));
+        auto go = [&](auto kernel) {
+            kernel<<<blocks, kKmodThreads, 0, stream>>>(kl, d_klimbs, nlimbs, base, d_off, d_range, max_count, wp,
+                                                        ww, d_a, d_b);
+        };
+        if (wide && lsb) go(kmod_kernel<true, true, true>);
+        else if (wide) go(kmod_kernel<true, false, true>);
+        else if (lsb) go(kmod_kernel<false, true, true>);
+        else go(kmod_kernel<false, false, true>);
+        return cudaGetLastError();
+    }
+    const KLimbs<1> none{};
+    auto go = [&](auto kernel) {
+        kernel<<<blocks, kKmodThreads, smem, stream>>>(none, d_klimbs, nlimbs, base, d_off, d_range, max_count, wp,
+                                                       ww, d_a, d_b);
+    };
+    if (wide && lsb) go(kmod_kernel<true, true, false>);
+    else if (wide) go(kmod_kernel<true, false, false>);
+    else if (lsb) go(kmod_kernel<false, true, false>);
+    else go(kmod_kernel<false, false, false>);
     return cudaGetLastError();
 }
 
@@ -228,19 +264,33 @@ cudaError_t kmod_list32(const uint32_t *d_klimbs, int nlimbs, const uint32_t *d_
 }
 
 cudaError_t kmod_chain(const uint32_t *d_seg_limbs, const uint32_t *d_seg_off, int G, int nlimbs, uint64_t base,
-                       const uint32_t *d_off, uint64_t n, void *d_r, void *d_r2, bool wide, cudaStream_t stream) {
+                       const uint32_t *d_off, uint64_t n, void *d_r, void *d_r2, bool wide, cudaStream_t stream,
+                       const uint32_t *h_seg_limbs, const uint32_t *h_seg_off) {
     if (n == 0 || G == 0) return cudaSuccess;
     const uint64_t per_thread = wide ? 1 : kPrimesPerThread;
     const uint64_t threads = (n + per_thread - 1) / per_thread;
     const unsigned blocks = (unsigned)((threads + kKmodThreads - 1) / kKmodThreads);
-    const size_t smem = (size_t)(nlimbs + G + 1) * sizeof(uint32_t);
     if (nlimbs + G + 1 > kMaxSharedLimbs) return cudaErrorInvalidValue;
+    if (h_seg_limbs && h_seg_off && nlimbs + G + 1 <= kParamLimbs) {
+        KLimbs<kParamLimbs> kl;
+        memcpy(kl.limb, h_seg_limbs, (size_t)nlimbs * sizeof(uint32_t));
+        memcpy(kl.limb + nlimbs, h_seg_off, (size_t)(G + 1) * sizeof(uint32_t));
+        if (wide)
+            kmod_chain_kernel<true, true><<<blocks, kKmodThreads, 0, stream>>>(kl, d_seg_limbs, d_seg_off, G, nlimbs,
+                                                                               base, d_off, n, d_r, d_r2);
+        else
+            kmod_chain_kernel<false, true><<<blocks, kKmodThreads, 0, stream>>>(kl, d_seg_limbs, d_seg_off, G, nlimbs,
+                                                                                base, d_off, n, d_r, d_r2);
+        return cudaGetLastError();
+    }
+    const size_t smem = (size_t)(nlimbs + G + 1) * sizeof(uint32_t);
+    const KLimbs<1> none{};
     if (wide)
-        kmod_chain_kernel<true><<<blocks, kKmodThreads, smem, stream>>>(d_seg_limbs, d_seg_off, G, nlimbs, base,
-                                                                        d_off, n, d_r, d_r2);
+        kmod_chain_kernel<true, false><<<blocks, kKmodThreads, smem, stream>>>(none, d_seg_limbs, d_seg_off, G, nlimbs,
+                                                                               base, d_off, n, d_r, d_r2);
     else
-        kmod_chain_kernel<false><<<blocks, kKmodThreads, smem, stream>>>(d_seg_limbs, d_seg_off, G, nlimbs, base,
-                                                                         d_off, n, d_r, d_r2);
+        kmod_chain_kernel<false, false><<<blocks, kKmodThreads, smem, stream>>>(none, d_seg_limbs, d_seg_off, G,
+                                                                                nlimbs, base, d_off, n, d_r, d_r2);
     return cudaGetLastError();
 }
 
