@@ -357,6 +357,10 @@ typedef struct {
                                 (default 4) */
     uint32_t kmod_lsb_limbs; /* K mod p least significant limb first from this many limbs
                                 (default 32) */
+    uint32_t large_form;     /* large-prime kernel of a one-job run: 0 = CTAs pool their
+                                primes' walks as 64-step items (default), 1 = warps run
+                                alone and hand longer walks to a list walked one warp per
+                                walk (faster for short walks, i.e. small jobs) */
 } pgs_tuning;
 
 void pgs_tuning_default(pgs_tuning *out);
@@ -364,7 +368,8 @@ void pgs_tuning_default(pgs_tuning *out);
  * returns the length (without the NUL), or PGS_EINVAL if cap is too small. */
 int pgs_tuning_class(const pgs_job *job, char *buf, size_t cap);
 /* Knobs for the job's class on this context (PGS_EINVAL for values outside
- * the ranges above).  Jobs prepared afterwards use them. */
+ * the ranges above).  One-job runs prepared afterwards (pgs_prepare,
+ * pgs_method2) use them; batched and served jobs keep the defaults. */
 int pgs_tuning_set(pgs_ctx *ctx, const pgs_job *job, const pgs_tuning *t);
 /* The knobs jobs of this class get: returns 1 when the class is tuned, 0
  * when it gets the defaults. */

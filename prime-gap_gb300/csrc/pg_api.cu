@@ -56,6 +56,7 @@ void pgs_destroy(pgs_ctx *ctx) {
     ctx->win_t0.release();
     ctx->large_ctr.release();
     ctx->heavy.release();
+    ctx->walks.release();
     batch_state_destroy(ctx);
     ctx->dpool.trim();
     if (ctx->copy) cudaStreamDestroy(ctx->copy);
@@ -175,7 +176,7 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     CK(ctx->win_off.ensure(pr->win_bound * 4 + 4));
     CK(ctx->win_r.ensure(pr->win_bound * 8 + 8));
     CK(ctx->win_t0.ensure(pr->win_bound * 8 + 8));
-    CK(ctx->large_ctr.ensure(2 * sizeof(unsigned long long)));
+    CK(ctx->large_ctr.ensure(pg::kLargeCounters * sizeof(unsigned long long)));
     CK(ctx->heavy.ensure((size_t)pg::heavy_capacity() * pg::kHeavyPrimeBytes));
     CK(cudaStreamSynchronize(s));
     float ms = 0;
@@ -375,6 +376,8 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
                            (uint32_t)h.dq.size(), pr->dr.as<uint32_t>(), s));
         pr->launches += 1;
     }
+    // the warp-alone form's walk list, on first use
+    if (pr->tune.large_form == 1) CK(ctx->walks.ensure((size_t)pg::walk_capacity() * pg::kWalkEntryBytes));
     // large primes, window by window
     for (size_t w = 0; w < pr->windows.size(); w++) {
         const Window &win = pr->windows[w];
@@ -391,7 +394,9 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
                             ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint2>(),
                             pr->ymask.as<uint2>(),
                             pg::LargeScratch{ctx->large_ctr.as<unsigned long long>(),
-                                             ctx->heavy.as<pg::HeavyPrime>(), pg::heavy_capacity()},
+                                             ctx->heavy.as<pg::HeavyPrime>(), pg::heavy_capacity(),
+                                             ctx->walks.as<pg::WalkEntry>(),
+                                             ctx->walks.p ? pg::walk_capacity() : 0u},
                             s));
         CK(mark(e_d));
         span(PGS_STAGE_PRIMES, e_a, e_b);

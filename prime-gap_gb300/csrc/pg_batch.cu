@@ -133,7 +133,7 @@ int lane_buffers(pgs_ctx *ctx, Lane *l) {
     const uint64_t need = ctx->table ? ctx->table->max_count : 0;
     CK(l->r.ensure(need * 8 + 8));
     CK(l->t0.ensure(need * 8 + 8));
-    CK(l->ctr.ensure(2 * sizeof(unsigned long long)));
+    CK(l->ctr.ensure(pg::kLargeCounters * sizeof(unsigned long long)));
     CK(l->heavy.ensure((size_t)pg::heavy_capacity() * pg::kHeavyPrimeBytes));
     return PGS_OK;
 }
@@ -187,7 +187,9 @@ int prepare_table_job(pgs_ctx *ctx, const pgs_job &job, cudaStream_t s, pgs_prep
         }
     }
     HostJob &h = pr->hj;
-    pr->tune = tuning_for(ctx, job);
+    // the tuner measures one-job runs; batched and served jobs keep the
+    // defaults (per-class picks applied to the batch measured 1 % slower)
+    pr->tune = pgt::tuning_default();
     PrimeTable &t = *ctx->table;
     const uint64_t rows = h.valid_mi.size();
     const uint64_t shi = std::min<uint64_t>(h.s1, h.prime_limit);

@@ -269,6 +269,7 @@ pg::JobDev job_dev(pgs_prepared *pr) {
     j.direct_steps = pr->tune.direct_steps;
     j.item_shift = (uint32_t)pgt::ilog2(pr->tune.item_steps);
     j.heavy_steps = pr->tune.heavy_steps;
+    j.large_form = pr->tune.large_form;
     return j;
 }
 

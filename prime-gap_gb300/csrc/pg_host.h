@@ -199,7 +199,7 @@ struct pgs_ctx {
     std::mutex mu;
     std::string err;
     pg::BasePrimes base;
-    pgh::DevBuf win_off, win_r, win_t0, large_ctr, heavy;
+    pgh::DevBuf win_off, win_r, win_t0, large_ctr, heavy, walks;
     pgh::DevicePool dpool;
     // batched / served paths (pg_batch.cu)
     PrimeTable *table = nullptr;
@@ -213,7 +213,7 @@ struct pgs_ctx {
 struct pgs_prepared {
     pgs_ctx *ctx = nullptr;
     pgh::HostJob hj;
-    pgs_tuning tune{24, 64, 4096, 16, 4, 32};  // the job's class tuning (defaults)
+    pgs_tuning tune{24, 64, 4096, 16, 4, 32, 0};  // the job's class tuning (defaults)
     std::vector<pgh::Window> windows;
     uint64_t sp_lo = 0, sp_hi = 0, sp_bound = 0;
     uint64_t text_cap = 0;

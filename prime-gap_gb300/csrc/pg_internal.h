@@ -101,18 +101,25 @@ struct JobDev {
     // fraction's thread, of more than heavy_steps in a CTA of their own, the
     // rest in items of 2^item_shift steps over the CTA
     uint32_t direct_steps, item_shift, heavy_steps;
+    uint32_t large_form;  // one-job kernel form: 0 CTA-pooled items, 1 warps alone with a walk list
 };
 
 struct HeavyPrime;
 // Device scratch of the large-prime phase: two counters (group claims, heavy
 // primes) and the heavy-prime list.
+struct WalkEntry;
 struct LargeScratch {
-    unsigned long long *counters;
+    unsigned long long *counters;  // kLargeCounters words
     HeavyPrime *heavy;
     uint32_t heavy_cap;
+    WalkEntry *walks = nullptr;    // walk list of the warp-alone one-job form
+    uint32_t walk_cap = 0;
 };
+constexpr int kLargeCounters = 4;
 uint32_t heavy_capacity();
+uint32_t walk_capacity();
 constexpr size_t kHeavyPrimeBytes = 48;
+constexpr size_t kWalkEntryBytes = 32;
 
 // d_mmask: valid-m bitmask over walk indices j (walk.jmax bits), d_ymask:
 // live-offset bitmask over walk residues y (walk.w bits), each as {bits, set

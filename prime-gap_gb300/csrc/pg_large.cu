@@ -73,6 +73,14 @@ struct HeavyPrime {
 };
 static_assert(sizeof(HeavyPrime) == kHeavyPrimeBytes, "heavy list stride");
 
+// A walk of more than direct_steps and at most heavy_steps steps, handed from
+// the warp-alone continued-fraction kernel to walk_kernel: first hit
+// (mi0, y0) and the rotation, step costs clamped to the walk's end (gap32).
+struct WalkEntry {
+    uint32_t mi0, y0, up, dn, kp, kn, steps, pad;
+};
+static_assert(sizeof(WalkEntry) == kWalkEntryBytes, "walk list stride");
+
 namespace {
 
 template <typename T>
@@ -297,6 +305,101 @@ __global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
     }
 }
 
+// The warp-alone form of one job (tuning knob large_form = 1): no CTA
+// barrier after the masks.  Each warp claims 32 primes at a time, runs their
+// continued fractions, walks the short rotations (at most direct_steps
+// steps) in place and hands the others to two lists -- up to heavy_steps
+// steps to walk_kernel (one warp per walk), more to heavy_kernel (one CTA per
+// prime).  A full list falls back to the next one, and finally to walking the
+// rotation in this thread.  Faster than the pooled form when walks are short
+// (small jobs: config 1's large stage 0.43 -> 0.35 ms), slower when many walks
+// of 25-100 steps leave each lane of walk_kernel only a few steps after its
+// closed-form start (config 2: 5.85 -> 8.64 ms); the tuner picks per class.
+template <typename T, bool kStartIn>
+__global__ void __launch_bounds__(kLargeThreads)
+    large_cf_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
+                    const unsigned long long *range, uint64_t max_count, const T *__restrict__ a_in,
+                    const void *__restrict__ b_in, const unsigned long long *rrange,
+                    const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask, int masks_in_shared,
+                    unsigned long long *ctr, HeavyPrime *heavy, uint32_t heavy_cap, WalkEntry *walks,
+                    uint32_t walk_cap) {
+    extern __shared__ uint2 s_masks[];
+    const uint2 *mmask, *ymask;
+    load_masks(job, g_mmask, g_ymask, masks_in_shared, s_masks, mmask, ymask);
+    const Marker mark{job, mmask, ymask};
+    const uint64_t n = min((uint64_t)(range[1] - range[0]), max_count);
+    off += range[0];
+    a_in += range[0] - rrange[0];
+    const T *b = (const T *)b_in + (range[0] - rrange[0]);
+    const T w = (T)job.walk.w;
+    const uint64_t minc = job.walk.jmax;
+    const uint32_t lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long g = 0;
+        if (lane == 0) g = atomicAdd(ctr, 1ull);
+        g = __shfl_sync(0xffffffffu, g, 0);
+        if (g * 32 >= n) break;
+        const uint64_t i = g * 32 + lane;
+        if (i >= n) continue;
+        const T p = (T)(base + off[i]);
+        T step, t0;
+        if constexpr (!kStartIn)
+            step = a_in[i], t0 = b[i];
+        else if constexpr (sizeof(T) == 4)
+            walk_start(job.walk, p, a_in[i], b[i], step, t0, job.kmul);
+        else
+            walk_start(job.walk, p, a_in[i], neg_inv64(p), b[i], step, t0, job.kmul);
+        const Entry<T> e = first_entry<T>(p, step, w, t0, minc);
+        if (e.t >= minc || e.y >= w) continue;
+        const uint64_t bound = rotation_steps_bound<T>(e.t, minc, e.g, p);
+        const ThreeGap<uint32_t> g32 = gap32(e.g, (uint32_t)minc);
+        if (bound > job.direct_steps) {
+            if (bound <= job.heavy_steps) {
+                const unsigned long long k = atomicAdd(ctr + 2, 1ull);
+                if (k < walk_cap) {
+                    walks[k] = WalkEntry{(uint32_t)e.t, (uint32_t)e.y, g32.up, g32.dn, g32.kp, g32.kn,
+                                         (uint32_t)bound, 0u};
+                    continue;
+                }
+            }
+            const unsigned long long h = atomicAdd(ctr + 1, 1ull);
+            if (h < heavy_cap) {
+                heavy[h] = HeavyPrime{(uint32_t)e.t, (uint32_t)e.y, (uint32_t)e.g.up, (uint32_t)e.g.dn,
+                                      (uint64_t)e.g.kp, (uint64_t)e.g.kn, bound, 0u, 0u};
+                continue;
+            }
+        }
+        rotation_walk32((uint32_t)e.t, (uint32_t)e.y, g32, (uint32_t)w, (uint32_t)minc, (uint32_t)bound, mark);
+    }
+}
+
+// The walk list of the warp-alone form: each warp claims one walk and splits
+// its steps evenly over its lanes (each lane starts from the closed form).
+__global__ void __launch_bounds__(kLargeThreads)
+    walk_kernel(JobDev job, const WalkEntry *__restrict__ walks, const unsigned long long *ctr, uint32_t walk_cap,
+                const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask, int masks_in_shared,
+                unsigned long long *claim) {
+    extern __shared__ uint2 s_masks[];
+    const uint2 *mmask, *ymask;
+    load_masks(job, g_mmask, g_ymask, masks_in_shared, s_masks, mmask, ymask);
+    const Marker mark{job, mmask, ymask};
+    const uint64_t nw = min((uint64_t)ctr[2], (uint64_t)walk_cap);
+    const uint32_t jmax = (uint32_t)job.walk.jmax, w = job.walk.w, lane = threadIdx.x & 31;
+    for (;;) {
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(claim, 1ull);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (k >= nw) break;
+        const WalkEntry we = walks[k];
+        const ThreeGap<uint32_t> g{we.kp, we.up, we.kn, we.dn};
+        const uint32_t per = (we.steps + 31) / 32, n0 = lane * per;
+        if (n0 >= we.steps) continue;
+        uint32_t y, mi;
+        rotation_at32(we.mi0, we.y0, g, n0, jmax, y, mi);
+        rotation_walk32(mi, y, g, w, jmax, per, mark);
+    }
+}
+
 // One CTA per heavy prime: its rotation steps split over the CTA's threads.
 __global__ void __launch_bounds__(kLargeThreads)
     heavy_kernel(JobDev job, const HeavyPrime *__restrict__ heavy,
@@ -356,6 +459,7 @@ __global__ void __launch_bounds__(kLargeThreads)
 }  // namespace
 
 uint32_t heavy_capacity() { return 1u << 20; }
+uint32_t walk_capacity() { return 1u << 24; }
 
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_range, uint64_t max_count, const void *d_a,
@@ -370,7 +474,7 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     cudaError_t e;
-    if ((e = cudaMemsetAsync(scratch.counters, 0, 2 * sizeof(unsigned long long), stream))) return e;
+    if ((e = cudaMemsetAsync(scratch.counters, 0, kLargeCounters * sizeof(unsigned long long), stream))) return e;
     unsigned long long *group_ctr = scratch.counters, *heavy_count = scratch.counters + 1;
     auto prep = [&](auto kernel) -> cudaError_t {
         // static + dynamic shared memory above 48 KiB needs the opt-in, and
@@ -392,7 +496,26 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
             group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
         return cudaSuccess;
     };
-    if (wide)
+    // the warp-alone form: as many warps as fit, each claiming 32 primes
+    auto launch_cf = [&](auto kernel, const auto *a) -> cudaError_t {
+        cudaError_t err = prep(kernel);
+        if (err) return err;
+        if (per_sm < 1) per_sm = 1;
+        const uint64_t ctas = ((max_count + 31) / 32 + kLargeThreads / 32 - 1) / (kLargeThreads / 32);
+        const uint64_t blocks = std::min<uint64_t>((uint64_t)sms * per_sm, ctas);
+        kernel<<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
+            job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask, in_shared, scratch.counters,
+            scratch.heavy, scratch.heavy_cap, scratch.walks, scratch.walk_cap);
+        return cudaSuccess;
+    };
+    const bool alone = job.large_form == 1 && scratch.walks != nullptr;
+    if (alone && wide)
+        e = start_in_kernel ? launch_cf(large_cf_kernel<uint64_t, true>, (const uint64_t *)d_a)
+                            : launch_cf(large_cf_kernel<uint64_t, false>, (const uint64_t *)d_a);
+    else if (alone)
+        e = start_in_kernel ? launch_cf(large_cf_kernel<uint32_t, true>, (const uint32_t *)d_a)
+                            : launch_cf(large_cf_kernel<uint32_t, false>, (const uint32_t *)d_a);
+    else if (wide)
         e = start_in_kernel ? launch(large_kernel<uint64_t, true>, (const uint64_t *)d_a)
                             : launch(large_kernel<uint64_t, false>, (const uint64_t *)d_a);
     else
@@ -400,6 +523,13 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
                             : launch(large_kernel<uint32_t, false>, (const uint32_t *)d_a);
     if (e) return e;
     if ((e = cudaGetLastError())) return e;
+    if (alone) {
+        if ((e = prep(walk_kernel))) return e;
+        if (per_sm < 1) per_sm = 1;
+        walk_kernel<<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(
+            job, scratch.walks, scratch.counters, scratch.walk_cap, d_mmask, d_ymask, in_shared, scratch.counters + 3);
+        if ((e = cudaGetLastError())) return e;
+    }
     if ((e = prep(heavy_kernel))) return e;
     if (per_sm < 1) per_sm = 1;
     heavy_kernel<<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(

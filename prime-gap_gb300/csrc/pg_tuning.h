@@ -6,7 +6,7 @@
 // depth and the walks' lengths (P's K, the window 2*SL+1, the walk length
 // minc) -- more than on the exact values.  The cache file has one line per
 // (device, class):
-//   device <TAB> class <TAB> direct item_steps heavy rows chunks lsb <TAB> ms_default ms_tuned
+//   device <TAB> class <TAB> direct item_steps heavy rows chunks lsb form <TAB> ms_default ms_tuned
 // Lines starting with '#' are comments.  Saving merges with the file's other
 // devices' lines.
 #pragma once
@@ -43,6 +43,7 @@ inline pgs_tuning tuning_default() {
     t.rows_per_cta = 16;
     t.text_chunks = 4;
     t.kmod_lsb_limbs = 32;
+    t.large_form = 0;
     return t;
 }
 
@@ -51,7 +52,8 @@ inline bool tuning_valid(const pgs_tuning &t) {
     return t.direct_steps >= 1 && t.direct_steps <= 1024 &&
            (t.item_steps == 32 || t.item_steps == 64 || t.item_steps == 128) && t.heavy_steps >= 256 &&
            t.heavy_steps <= (1u << 24) && t.heavy_steps >= t.direct_steps && t.rows_per_cta >= 1 &&
-           t.rows_per_cta <= 32 && t.text_chunks >= 1 && t.text_chunks <= 4 && t.kmod_lsb_limbs >= 1;
+           t.rows_per_cta <= 32 && t.text_chunks >= 1 && t.text_chunks <= 4 && t.kmod_lsb_limbs >= 1 &&
+           t.large_form <= 1;
 }
 
 struct Entry {
@@ -62,8 +64,8 @@ struct Entry {
 inline std::string format_line(const std::string &device, const std::string &cls, const Entry &e) {
     std::ostringstream o;
     o << device << '\t' << cls << '\t' << e.t.direct_steps << ' ' << e.t.item_steps << ' ' << e.t.heavy_steps << ' '
-      << e.t.rows_per_cta << ' ' << e.t.text_chunks << ' ' << e.t.kmod_lsb_limbs << '\t' << e.ms_default << ' '
-      << e.ms_tuned;
+      << e.t.rows_per_cta << ' ' << e.t.text_chunks << ' ' << e.t.kmod_lsb_limbs << ' ' << e.t.large_form << '\t'
+      << e.ms_default << ' ' << e.ms_tuned;
     return o.str();
 }
 
@@ -84,7 +86,7 @@ inline bool parse_line(const std::string &line, std::string &device, std::string
     if (f.size() < 3 || f[0].empty() || f[1].empty()) return false;
     std::istringstream v(f[2]);
     if (!(v >> e.t.direct_steps >> e.t.item_steps >> e.t.heavy_steps >> e.t.rows_per_cta >> e.t.text_chunks >>
-          e.t.kmod_lsb_limbs))
+          e.t.kmod_lsb_limbs >> e.t.large_form))
         return false;
     if (!tuning_valid(e.t)) return false;
     e.ms_default = e.ms_tuned = 0;
@@ -124,7 +126,7 @@ inline int save(const std::string &path, const std::string &device, const std::m
     std::ofstream out(path, std::ios::trunc);
     if (!out) return -1;
     out << "# libpgsieve tuning: device, class (P.SL<log2>.minc<log2>), direct item_steps heavy rows chunks "
-           "kmod_lsb, ms default and tuned\n";
+           "kmod_lsb large_form, ms default and tuned\n";
     for (const auto &l : keep) out << l << '\n';
     for (const auto &kv : m) out << format_line(device, kv.first, kv.second) << '\n';
     return out ? (int)m.size() : -1;

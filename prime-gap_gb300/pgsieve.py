@@ -145,6 +145,7 @@ class Tuning(ctypes.Structure):
         ("rows_per_cta", ctypes.c_uint32),
         ("text_chunks", ctypes.c_uint32),
         ("kmod_lsb_limbs", ctypes.c_uint32),
+        ("large_form", ctypes.c_uint32),
     ]
 
     def as_dict(self) -> dict:

@@ -1,6 +1,7 @@
-"""Tuned knobs change the time, never the bytes: plain, one-call and batched
-outputs with extreme knob settings against the reference's golden md5s, and
-pgs_tune's result stored for the job's class."""
+"""Tuned knobs change the time, never the bytes: plain and one-call outputs
+with extreme knob settings against the reference's golden md5s (batched jobs
+keep the default knobs and must match too), and pgs_tune's result stored for
+the job's class."""
 from __future__ import annotations
 
 import hashlib
@@ -13,11 +14,11 @@ pytestmark = pytest.mark.gpu
 
 EXTREMES = [
     {"direct_steps": 8, "item_steps": 32, "heavy_steps": 1024, "rows_per_cta": 4, "text_chunks": 1,
-     "kmod_lsb_limbs": 8},
+     "kmod_lsb_limbs": 8, "large_form": 1},
     {"direct_steps": 48, "item_steps": 128, "heavy_steps": 16384, "rows_per_cta": 32, "text_chunks": 2,
-     "kmod_lsb_limbs": 1 << 20},
+     "kmod_lsb_limbs": 1 << 20, "large_form": 0},
     {"direct_steps": 1, "item_steps": 64, "heavy_steps": 256, "rows_per_cta": 1, "text_chunks": 3,
-     "kmod_lsb_limbs": 1},
+     "kmod_lsb_limbs": 1, "large_form": 1},
 ]
 NAMES = ["fn1", "fn1_bitcompressed", "small_d7_odd", "small_d30030", "config1", "edge_maxprime_1M"]
 
@@ -56,3 +57,18 @@ def test_tune_stores_class_result(goldens, tmp_path):
         assert s2.tuning_get(job)[1] is False
         assert s2.tuning_load(f) == 1
         assert s2.tuning_get(job) == (knobs, True)
+
+
+@pytest.mark.parametrize("name", ["config2", "w64_503_210"])
+def test_warp_alone_form_full_size(goldens, name):
+    """The warp-alone large-prime form (walk list) on config 2 and on a job
+    past 2^32, against the reference's md5."""
+    import json
+    from pathlib import Path
+
+    g = goldens.get(name) or json.loads(
+        (Path(__file__).resolve().parent / "golden" / "mix_goldens.json").read_text())[name]
+    with pgsieve.Sieve(0, load_tuning=False) as s:
+        job = _spec(g)
+        s.tuning_set(job, {"large_form": 1})
+        assert hashlib.md5(s.method2(job)).hexdigest() == g["md5"]

@@ -49,7 +49,8 @@ def test_class_keys(th, built):
 
 def test_defaults_are_the_built_in_constants(built):
     assert pgsieve.tuning_default() == {"direct_steps": 24, "item_steps": 64, "heavy_steps": 4096,
-                                        "rows_per_cta": 16, "text_chunks": 4, "kmod_lsb_limbs": 32}
+                                        "rows_per_cta": 16, "text_chunks": 4, "kmod_lsb_limbs": 32,
+                                        "large_form": 0}
 
 
 def test_cache_file_round_trip_and_device_merge(th, tmp_path):
@@ -71,16 +72,18 @@ def test_cache_file_round_trip_and_device_merge(th, tmp_path):
 
 
 @pytest.mark.parametrize("line,ok", [
-    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 16 4 32\t10 9", True),
-    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 16 4 32", True),
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 16 4 32 0\t10 9", True),
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 16 4 32 1", True),
     ("# comment", False),
     ("", False),
-    ("NVIDIA GB300\tP1511.SL14.minc16\t24 48 4096 16 4 32", False),   # item_steps not a power 32..128
-    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 33 4 32", False),   # rows_per_cta > 32
-    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 16 5 32", False),   # text_chunks > 4
-    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 16 16 4 32", False),     # heavy below direct / 256
-    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096", False),           # short
-    ("NVIDIA GB300 P1511.SL14.minc16 24 64 4096 16 4 32", False),     # no tabs
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 48 4096 16 4 32 0", False),   # item_steps not a power 32..128
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 33 4 32 0", False),   # rows_per_cta > 32
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 16 5 32 0", False),   # text_chunks > 4
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 16 16 4 32 0", False),     # heavy below direct / 256
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 16 4 32 2", False),   # no third kernel form
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096 16 4 32", False),     # a line of the six-knob format
+    ("NVIDIA GB300\tP1511.SL14.minc16\t24 64 4096", False),             # short
+    ("NVIDIA GB300 P1511.SL14.minc16 24 64 4096 16 4 32 0", False),       # no tabs
 ])
 def test_cache_line_validation(th, line, ok):
     out = _T()
