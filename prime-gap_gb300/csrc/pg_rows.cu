@@ -93,11 +93,14 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
         uint32_t mr = (uint32_t)(((m % p) * r) % p);
         uint32_t x0 = (sl % p + p - mr) % p;
         // row by row (the same row across the warp): step the residue over
-        // the m values since the previous row, then strike this row
+        // the m values since the previous row, then strike this row; with d
+        // even every valid m is odd, so the step is 2r mod p per two m
+        const uint32_t stride = job.walk.stride;
+        const uint32_t rs = stride == 2 ? (r >= p - r ? r - (p - r) : r + r) : r;
         uint32_t mi_at = mi_first;
         for (uint32_t j = 0; j < nrows; j++) {
             const uint32_t mi = s_mi[j];
-            for (; mi_at < mi; mi_at++) x0 = x0 >= r ? x0 - r : x0 + (p - r);
+            for (; mi_at < mi; mi_at += stride) x0 = x0 >= rs ? x0 - rs : x0 + (p - rs);
             const uint32_t xs = x0 + (((x0 ^ x_par) & 1) ? p : 0);
             for (uint32_t h = (xs - x_par) >> 1; h < rd.nb; h += p)
                 atomicOr(&sh[j * nbw + (h >> 5)], 1u << (h & 31));
