@@ -115,6 +115,15 @@ PG_HD float u32_to_f32_rz(uint32_t v) {
     return f;
 #endif
 }
+PG_HD float u64_to_f32_rz(uint64_t v) {
+#if defined(__CUDA_ARCH__)
+    return __ull2float_rz(v);
+#else
+    if (v < (1ull << 24)) return (float)v;
+    const int sh = 64 - __builtin_clzll(v) - 24;  // keep the top 24 bits
+    return ldexpf((float)(v >> sh), sh);
+#endif
+}
 PG_HD float rcp_approx(float x) {
 #if defined(__CUDA_ARCH__)
     float r;
@@ -138,7 +147,7 @@ PG_HD uint32_t f32_to_u32_rz(float x) {
 #if defined(__CUDA_ARCH__)
     return __float2uint_rz(x);
 #else
-    return (uint32_t)x;
+    return x >= 4294967296.0f ? 0xFFFFFFFFu : (uint32_t)x;  // saturates as the device does
 #endif
 }
 
@@ -170,6 +179,34 @@ PG_HD void udiv2_32(uint32_t n1, uint32_t n2, uint32_t d, uint32_t &q1, uint32_t
     if (rb >= d) b++;
     q1 = a;
     q2 = b;
+}
+
+// Two 64-bit quotients by one divisor, the same way in single precision:
+// x = (n_f * rs) with n_f = n rounded toward zero to 24 bits, rs = rcp(d_f)
+// (1 - 2^-19) rounded toward zero, d_f = d rounded toward zero.  With the
+// reciprocal within 3 ulps, (n/d)(1 - 2^-18) < x < n/d, so q0 = floor(x)
+// never exceeds q = floor(n/d) and, while q0 < 2^17 (hence n/d < 2^18), is
+// at least q - 1: one remainder test finishes it.  A larger q0 takes the
+// exact division.
+PG_HD void udiv2_64(uint64_t n1, uint64_t n2, uint64_t d, uint64_t &q1, uint64_t &q2, int skew = 0) {
+    float rf = rcp_approx(u64_to_f32_rz(d));
+#if !defined(__CUDA_ARCH__)
+    for (; skew > 0; skew--) rf = nextafterf(rf, 2.0f);
+    for (; skew < 0; skew++) rf = nextafterf(rf, 0.0f);
+#else
+    (void)skew;
+#endif
+    const float rs = mul_f32_rz(rf, 0.999998092651367188f);  // 1 - 2^-19, exact in single precision
+    const uint32_t a = f32_to_u32_rz(mul_f32_rz(u64_to_f32_rz(n1), rs));
+    const uint32_t b = f32_to_u32_rz(mul_f32_rz(u64_to_f32_rz(n2), rs));
+    if ((a | b) >= (1u << 17)) {
+        q1 = n1 / d;
+        q2 = n2 / d;
+        return;
+    }
+    const uint64_t ra = n1 - (uint64_t)a * d, rb = n2 - (uint64_t)b * d;
+    q1 = a + (ra >= d ? 1u : 0u);
+    q2 = b + (rb >= d ? 1u : 0u);
 }
 
 // 2^32 mod p for odd p >= 3 without a hardware division.  p >= 2^31: 2^32 - p.
@@ -680,61 +717,92 @@ struct Entry {
     ThreeGap<T> g;
 };
 
-// One code path for both orientations (no divergence inside a warp): the
-// level with the larger gap `big` (up if up > dn, else dn) loses q copies of
-// the smaller gap `small`, and its m-step gains q copies of the other's.
-// The entry point moves as follows, with f = ceil((big - y) / small) for
-// y < big (else 0):
-//   up > dn: level i of the batch enters [0, up - i*dn): y -= dn whenever
+// Levels alternate: a level with up > dn leaves up' <= max(w - 1, dn), so
+// either up' <= dn (the next level has dn > up') or both gaps are below w and
+// the descent ends (for a prime modulus up' == dn cannot happen above 1).  The
+// loop therefore runs the two kinds of level in turn, each with its roles
+// fixed in the code: no per-level selects, and every lane of a warp runs the
+// same kind of level at the same time.  The first level must have up > dn:
+// for a < p - a the search runs on the mirror image z = (w - 1 - y) mod p,
+// which maps [0, w) onto itself and turns the rotation by a into the rotation
+// by p - a; the answer maps back by y = w - 1 - z and the three-gap data by
+// swapping (kp, up) with (kn, dn).
+//
+// One level with big > small (up > dn, or dn > up in the other kind): big
+// loses q copies of small, with q the least count leaving big <= max(w - 1,
+// small), i.e. q = floor(min(C - w, big - 1) / small) with C = up + dn, and
+// its m-step gains q copies of the other's.  The entry point y in [0, C)
+// moves as follows, with f = floor((C - 1 - y) / small) (ceil((big - y) /
+// small) for y < big, 0 otherwise):
+//   up > dn: sub-level i of the batch enters [0, up - i*dn): y -= dn whenever
 //            y >= up - i*dn, which, once true, stays true: q - f subtractions;
-//   up <= dn: level i enters [0, dn - i*up) with one wrap y -= dn - i*up at
-//            the first level where y >= dn - i*up, i = f (after it y < up).
-// t only grows, and the first hit comes no earlier than the first entry into
-// the current circle, so once t >= t_lim the search stops (no hit below
-// t_lim): the caller sees t >= t_lim.
+//   dn > up: sub-level i enters [0, dn - i*up) with one wrap y -= dn - i*up
+//            at the first i where y >= dn - i*up, i = f (after it y < up).
+// Both quotients share the divisor and one approximate reciprocal.
+//
+// Time: t only grows, and the first hit comes no earlier than the first
+// entry into the current circle, so once t >= t_lim the search stops (no hit
+// below t_lim): the caller sees t >= t_lim.  The loop keeps the budget
+// rem = lim - t in the modulus' width: each increment dt is at most p (it is
+// at most the level's new kp or kn, and kp*dn + kn*up = p), and for 32-bit
+// moduli the true first entry is below p < 2^32 - 1, so a limit above 2^32 - 1
+// never triggers and clamping it there changes nothing.
+template <typename T>
+PG_HD void quot2(T n1, T n2, T d, T &q1, T &q2) {
+    if constexpr (sizeof(T) == 4) {
+        udiv2_32(n1, n2, d, q1, q2);
+    } else {
+        udiv2_64(n1, n2, d, q1, q2);
+    }
+}
+
 template <typename T>
 PG_HD Entry<T> first_entry(T p, T a, T w, T y0, uint64_t t_lim = ~0ull) {
-    T kp = 1, up = a, kn = 1, dn = p - a;
-    T y = y0;
-    uint64_t t = 0;
-    // Every level with q >= 1 lowers big by at least small >= 1 (small stays
-    // positive: for a modulus sharing a factor with a, up == dn stops the
-    // descent with q == 0 before either reaches 0), so the loop ends.
+    const bool mir = a < p - a;
+    T up = mir ? p - a : a, dn = p - up, kp = 1, kn = 1;
+    T y = !mir ? y0 : (y0 < w ? w - 1 - y0 : p - (y0 - (w - 1)));
+    const T lim = t_lim < (uint64_t)(T)~(T)0 ? (T)t_lim : (T)~(T)0;
+    T rem = lim;
+    // Every level with q >= 1 lowers its big gap by at least small >= 1, so
+    // the loop ends; q == 0 only for a tie up == dn (not for a prime modulus).
     for (;;) {
-        const bool A = up > dn;
-        T big = A ? up : dn;
-        if (big < w) break;  // up, dn < w: the last level
-        const T small = A ? dn : up;
-        T kbig = A ? kp : kn;
-        const T ksmall = A ? kn : kp;
-        const T lim = (w - 1) > small ? (w - 1) : small;
-        T q, f;
-        if constexpr (sizeof(T) == 4) {
-            // both quotients from one reciprocal of `small`
-            udiv2_32(big - lim + small - 1, y >= big ? 0u : big - y + small - 1, small, q, f);
-        } else {
-            q = (big - lim + small - 1) / small;
-            f = y >= big ? (T)0 : (big - y + small - 1) / small;
+        if (up < w) break;  // up > dn: both below w
+        {
+            const T C = up + dn, n1 = (C - w) < (up - 1) ? (C - w) : (up - 1);
+            T q, f;
+            quot2<T>(n1, C - 1 - y, dn, q, f);
+            if (q == 0) break;
+            if (f < q) {
+                const T m = q - f, dt = m * kn;
+                if (dt >= rem) return {(uint64_t)(lim - rem) + dt, y, {kp, up, kn, dn}};
+                y -= m * dn;
+                rem -= dt;
+            }
+            up -= q * dn;
+            kp += q * kn;
         }
-        if (q == 0) break;
-        if (f < q) {
-            const T dy = A ? (q - f) * small : big - f * small;
-            const uint64_t dt = A ? (uint64_t)(q - f) * ksmall : (uint64_t)kbig + (uint64_t)f * ksmall;
-            y -= dy;
-            t += dt;
+        if (dn < w) break;  // dn > up: both below w
+        {
+            const T C = up + dn, n1 = (C - w) < (dn - 1) ? (C - w) : (dn - 1);
+            T q, f;
+            quot2<T>(n1, C - 1 - y, up, q, f);
+            if (q == 0) break;
+            if (f < q) {
+                const T dt = kn + f * kp;
+                if (dt >= rem) return {(uint64_t)(lim - rem) + dt, y, {kp, up, kn, dn}};
+                y -= dn - f * up;
+                rem -= dt;
+            }
+            dn -= q * up;
+            kn += q * kp;
         }
-        big -= q * small;
-        kbig += q * ksmall;
-        up = A ? big : small;
-        dn = A ? small : big;
-        kp = A ? kbig : ksmall;
-        kn = A ? ksmall : kbig;
-        if (t >= t_lim) return {t, y, {kp, up, kn, dn}};
     }
+    uint64_t t = lim - rem;
     if (y >= w) {  // last level: [0, up + dn) -> [0, w) by one wrap
         y -= dn;
         t += kn;
     }
+    if (mir) return {t, w - 1 - y, {kn, dn, kp, up}};
     return {t, y, {kp, up, kn, dn}};
 }
 

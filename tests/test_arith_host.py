@@ -41,6 +41,8 @@ def ah(built):
                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
     lib.ah_pow32_mod.restype = ctypes.c_uint32
     lib.ah_pow32_mod.argtypes = [ctypes.c_uint32, ctypes.c_int]
+    lib.ah_udiv2_64.restype = None
+    lib.ah_udiv2_64.argtypes = [u64, u64, u64, ctypes.c_int, ctypes.POINTER(u64)]
     lib.ah_udiv2.restype = None
     lib.ah_udiv2.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                              ctypes.POINTER(ctypes.c_uint32)]
@@ -443,6 +445,34 @@ def test_udiv2_shared_reciprocal_exact(ah):
     for n1, n2, d in cases:
         for skew in (-2, -1, 0, 1, 2):
             ah.ah_udiv2(n1, n2, d, skew, out)
+            assert (out[0], out[1]) == (n1 // d, n2 // d), (n1, n2, d, skew)
+
+
+def test_udiv2_64_shared_reciprocal_exact(ah):
+    """The 64-bit continued fraction's two quotients by one single-precision
+    reciprocal equal the exact quotients: divisors up to 2^64, quotients on
+    both sides of the fast-path edge (2^17), the reciprocal moved up to 2 ulps
+    either way."""
+    rng = random.Random(5)
+    out = (ctypes.c_uint64 * 2)()
+    cases = []
+    for _ in range(30000):
+        d = rng.choice([1, 2, 3, rng.randrange(1, 1 << 16), rng.randrange(1, 1 << 33), rng.randrange(1, 1 << 46),
+                        rng.randrange(1, 1 << 64), (1 << 46) - 1, (1 << 24) + 1, (1 << 40) + 1, (1 << 64) - 1])
+        qmax = rng.choice([3, 1 << 10, 1 << 17, 1 << 18, 1 << 40, 1 << 64])
+        def num():
+            v = rng.randrange(0, qmax) * d + rng.randrange(0, d)
+            return v if v < (1 << 64) else rng.randrange(0, 1 << 64)
+        cases.append((num(), num(), d))
+    for d in (1, 3, 1000003, (1 << 33) + 17, (1 << 45) + 59):
+        for q in ((1 << 17) - 1, 1 << 17, (1 << 17) + 1, (1 << 18) - 1, (1 << 18) + 1):
+            for dr in (0, d - 1):
+                n = q * d + dr
+                if n < (1 << 64):
+                    cases.append((n, n, d))
+    for n1, n2, d in cases:
+        for skew in (-2, -1, 0, 1, 2):
+            ah.ah_udiv2_64(n1, n2, d, skew, out)
             assert (out[0], out[1]) == (n1 // d, n2 // d), (n1, n2, d, skew)
 
 
