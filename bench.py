@@ -942,7 +942,7 @@ def run_tune(args, rank, world, local):
             table.append({"job": name, "class": pgsieve.tuning_class(spec), "knobs": knobs,
                           "ms_default": ms_def, "ms_tuned": ms_tuned})
         jobs = workloads.mixed_jobs(64, seed=4)
-        seen = set()
+        seen = {r["class"] for r in table}  # a mix job of a config's class keeps the config's knobs
         for j in jobs:
             c = pgsieve.tuning_class(j)
             if c in seen:

@@ -357,14 +357,18 @@ typedef struct {
                                 (default 4) */
     uint32_t kmod_lsb_limbs; /* K mod p least significant limb first from this many limbs
                                 (default 32) */
-    uint32_t large_form;     /* large-prime kernel of a one-job run: 0 = CTAs pool their
-                                primes' walks as 64-step items (default), 1 = warps run
-                                alone and hand longer walks to a list walked one warp per
-                                walk (faster for short walks, i.e. small jobs) */
+    uint32_t large_form;     /* large-prime kernel of a one-job run, two bits.  Bit 0: 0 =
+                                CTAs pool their primes' walks as 64-step items (default),
+                                1 = warps run alone and hand longer walks to a list walked
+                                one warp per walk (faster for short walks, i.e. small
+                                jobs).  Bits 1 and 2: K mod p of the large primes below
+                                and above 2^32 is computed inside that kernel (K of at
+                                most 1024 limbs) instead of in a launch of its own */
 } pgs_tuning;
 
 void pgs_tuning_default(pgs_tuning *out);
-/* The job's tuning class, "P<p>.SL<floor(log2 SL)>.minc<floor(log2 minc)>";
+/* The job's tuning class,
+ * "P<p>.SL<floor(log2 SL)>.minc<floor(log2 minc)>.mp<floor(log2 max_prime)>";
  * returns the length (without the NUL), or PGS_EINVAL if cap is too small. */
 int pgs_tuning_class(const pgs_job *job, char *buf, size_t cap);
 /* Knobs for the job's class on this context (PGS_EINVAL for values outside

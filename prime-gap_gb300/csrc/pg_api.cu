@@ -377,7 +377,10 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
         pr->launches += 1;
     }
     // the warp-alone form's walk list, on first use
-    if (pr->tune.large_form == 1) CK(ctx->walks.ensure((size_t)pg::walk_capacity() * pg::kWalkEntryBytes));
+    if (pr->tune.large_form & 1u) CK(ctx->walks.ensure((size_t)pg::walk_capacity() * pg::kWalkEntryBytes));
+    // K mod p of a window's primes inside the large-prime kernel: bit 1 of
+    // the form for windows of 32-bit primes, bit 2 for 64-bit primes
+    const bool limbs_fit = h.klimbs.size() <= (size_t)pg::kParamLimbs;
     // large primes, window by window
     for (size_t w = 0; w < pr->windows.size(); w++) {
         const Window &win = pr->windows[w];
@@ -385,10 +388,12 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
         int e_a, e_b, e_c, e_d;
         CK(mark(e_a));
         CK(pg::sieve_window(ctx->base, win.lo, win.hi, ctx->win_off.as<uint32_t>(), win.bound, cnt, s));
+        const bool fuse = limbs_fit && (pr->tune.large_form & (win.wide ? 4u : 2u));
         CK(mark(e_b));
-        CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
-                           ctx->win_off.as<uint32_t>(), rng, win.bound, &h.walk, ctx->win_r.p,
-                           ctx->win_t0.p, win.wide, s, (int)pr->tune.kmod_lsb_limbs, h.klimbs.data()));
+        if (!fuse)
+            CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
+                               ctx->win_off.as<uint32_t>(), rng, win.bound, &h.walk, ctx->win_r.p,
+                               ctx->win_t0.p, win.wide, s, (int)pr->tune.kmod_lsb_limbs, h.klimbs.data()));
         CK(mark(e_c));
         CK(pg::large_window(job, win.lo, ctx->win_off.as<uint32_t>(), rng, win.bound, ctx->win_r.p,
                             ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint2>(),
@@ -397,12 +402,13 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
                                              ctx->heavy.as<pg::HeavyPrime>(), pg::heavy_capacity(),
                                              ctx->walks.as<pg::WalkEntry>(),
                                              ctx->walks.p ? pg::walk_capacity() : 0u},
-                            s));
+                            s, fuse ? h.klimbs.data() : nullptr, (int)h.klimbs.size(),
+                            pg::kmod_lsb((int)h.klimbs.size(), win.wide, (int)pr->tune.kmod_lsb_limbs)));
         CK(mark(e_d));
         span(PGS_STAGE_PRIMES, e_a, e_b);
         span(PGS_STAGE_KMOD, e_b, e_c);
         span(PGS_STAGE_LARGE, e_c, e_d);
-        pr->launches += 4;
+        pr->launches += fuse ? 3 : 4;
     }
     // rows, text
     CK(mark(a));

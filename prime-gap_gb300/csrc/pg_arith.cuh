@@ -354,6 +354,7 @@ PG_HD void kmod32_lsb_multi(const uint32_t *limbs, int n, const uint32_t *p, uin
         r2[k] = r2_from_r1(pow32_mod(p[k]), p[k], pinv[k]);
         W[k] = 0;
     }
+#pragma unroll 4
     for (int i = 0; i < n; i++) {
         const uint32_t l = limbs[i];
 #pragma unroll

@@ -68,6 +68,18 @@ cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, con
                         const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream,
                         int lsb_min_limbs = 0, const uint32_t *h_klimbs = nullptr);
 
+// Whether K mod p of nlimbs limbs runs least significant limb first, under
+// the lsb_min_limbs rule of kmod_window.
+bool kmod_lsb(int nlimbs, bool wide, int lsb_min_limbs);
+
+// K's limbs as a kernel parameter (constant bank, read as warp-uniform
+// loads): no shared-memory fill and no barrier at the start of every CTA.
+constexpr int kParamLimbs = 1024;
+template <int N>
+struct KLimbs {
+    uint32_t limb[N];
+};
+
 // K'_g mod p for the G groups of a chain (K'_g = K'_(g-1) * S_g, segment g's
 // limbs at d_seg_limbs[d_seg_off[g] .. d_seg_off[g+1]), little-endian) for
 // the n primes base + d_off[i]: r_g at d_r[g * n + i], R^2 mod p at
@@ -101,7 +113,10 @@ struct JobDev {
     // fraction's thread, of more than heavy_steps in a CTA of their own, the
     // rest in items of 2^item_shift steps over the CTA
     uint32_t direct_steps, item_shift, heavy_steps;
-    uint32_t large_form;  // one-job kernel form: 0 CTA-pooled items, 1 warps alone with a walk list
+    // one-job kernel form: bit 0 clear = CTA-pooled items, set = warps alone
+    // with a walk list; bits 1 and 2 = K mod p inside the large-prime kernel
+    // for windows of 32-bit and of 64-bit primes
+    uint32_t large_form;
 };
 
 struct HeavyPrime;
@@ -127,12 +142,15 @@ constexpr size_t kWalkEntryBytes = 32;
 // d_a/d_b as written by kmod_window over the index range d_rrange, which
 // contains d_range: with start_in_kernel, K mod p and 2^64 mod p (jobs that
 // share K share them; each starts its walk here), else the job's walk step
-// and start residue.
+// and start residue.  With h_klimbs (nlimbs <= kParamLimbs, K's limbs on the
+// host), the kernel computes K mod p itself, least significant limb first
+// when lsb, and d_a, d_b, d_rrange are not read.
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_range, uint64_t max_count, const void *d_a,
                          const void *d_b, const unsigned long long *d_rrange, bool wide,
                          bool start_in_kernel, const uint2 *d_mmask, const uint2 *d_ymask,
-                         LargeScratch scratch, cudaStream_t stream);
+                         LargeScratch scratch, cudaStream_t stream, const uint32_t *h_klimbs = nullptr,
+                         int nlimbs = 0, bool lsb = true);
 
 // Many jobs in one launch (the batch).  A job: its descriptor (kmul set:
 // walks start from K' mod p) and masks; masks_in_shared when they fit the

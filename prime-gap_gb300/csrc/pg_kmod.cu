@@ -29,14 +29,6 @@ constexpr int kPrimesPerThread = 4;     // 32-bit primes
 constexpr int kLsbMinLimbs = 32;        // 32-bit primes: LSB chain from 32 limbs
 constexpr int kLsbMinLimbsWide = 24;    // 64-bit primes: from 12 words
 
-// K's limbs as a kernel parameter (constant bank, read as warp-uniform
-// loads): no shared-memory fill and no barrier at the start of every CTA.
-constexpr int kParamLimbs = 1024;
-template <int N>
-struct KLimbs {
-    uint32_t limb[N];
-};
-
 // kParam: K's limbs come in `kl` (nlimbs <= kParamLimbs); otherwise they are
 // copied from klimbs to shared memory (or read from global when too long).
 template <bool kWide, bool kLsb, bool kParam>
@@ -213,6 +205,15 @@ __global__ void __launch_bounds__(kKmodThreads)
 
 }  // namespace
 
+// Least significant limb first once the cheaper step (an add, a multiply and
+// a multiply-add, against a multiply-add, a multiply and a multiply-add)
+// outweighs the R^(n+1) power.
+bool kmod_lsb(int nlimbs, bool wide, int lsb_min_limbs) {
+    const int lsb_min = lsb_min_limbs > 0 ? (wide ? std::max(1, lsb_min_limbs * 3 / 4) : lsb_min_limbs)
+                                          : (wide ? kLsbMinLimbsWide : kLsbMinLimbs);
+    return nlimbs >= lsb_min;
+}
+
 cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, const uint32_t *d_off,
                         const unsigned long long *d_range, uint64_t max_count,
                         const WalkParams *walk, void *d_a, void *d_b, bool wide, cudaStream_t stream,
@@ -224,12 +225,7 @@ cudaError_t kmod_window(const uint32_t *d_klimbs, int nlimbs, uint64_t base, con
     const uint64_t threads = (max_count + per_thread - 1) / per_thread;
     const unsigned blocks = (unsigned)((threads + kKmodThreads - 1) / kKmodThreads);
     const size_t smem = nlimbs <= kMaxSharedLimbs ? (size_t)nlimbs * sizeof(uint32_t) : 0;
-    // least significant limb first once the cheaper step (an add, a multiply
-    // and a multiply-add, against a multiply-add, a multiply and a
-    // multiply-add) outweighs the R^(n+1) power
-    const int lsb_min = lsb_min_limbs > 0 ? (wide ? std::max(1, lsb_min_limbs * 3 / 4) : lsb_min_limbs)
-                                          : (wide ? kLsbMinLimbsWide : kLsbMinLimbs);
-    const bool lsb = nlimbs >= lsb_min;
+    const bool lsb = kmod_lsb(nlimbs, wide, lsb_min_limbs);
     if (h_klimbs && nlimbs <= kParamLimbs) {
         KLimbs<kParamLimbs> kl;
         memcpy(kl.limb, h_klimbs, (size_t)nlimbs * sizeof(uint32_t));

@@ -28,6 +28,7 @@
 // ranks in those masks (rank counts beside them, no table reads) and set one
 // bit of the L2-resident composite bitset with a global atomicOr.
 #include <algorithm>
+#include <cstring>
 
 #include "pg_arith.cuh"
 #include "pg_internal.h"
@@ -117,29 +118,57 @@ __device__ __forceinline__ void load_masks(const JobDev &job, const uint2 *g_mma
     __syncthreads();
 }
 
+// Where a kernel's walk inputs come from.
+constexpr int kInWalk = 0;      // a = the job's walk step, b = its start residue (kmod_window)
+constexpr int kInKprime = 1;    // a = K' mod p, b = R^2 mod p: the walk of K = K' * kmul starts here
+constexpr int kInLimbsLsb = 2;  // K mod p computed here from K's limbs, least significant first
+constexpr int kInLimbsMsb = 3;  // the same, most significant limb first
+
+// Walk step and start residue of prime p, the i-th of the window's inputs
+// a_in, b_in (kInWalk, kInKprime), or of K's limbs (kInLimbs*: one thread
+// per prime does K mod p here, so the large-prime phase's continued
+// fractions, mostly integer-ALU work, share the SM with the K mod p chains,
+// mostly wide multiplies, instead of following them in another launch).
+template <typename T, int kIn>
+__device__ __forceinline__ void walk_inputs(const JobDev &job, const uint32_t *limbs, int nlimbs, T p,
+                                            const T *a_in, const T *b_in, uint64_t i, T &step, T &t0) {
+    if constexpr (kIn == kInWalk) {
+        step = a_in[i];
+        t0 = b_in[i];
+    } else if constexpr (kIn == kInKprime) {
+        if constexpr (sizeof(T) == 4)
+            walk_start(job.walk, p, a_in[i], b_in[i], step, t0, job.kmul);
+        else
+            walk_start(job.walk, p, a_in[i], neg_inv64(p), b_in[i], step, t0, job.kmul);
+    } else if constexpr (sizeof(T) == 4) {
+        uint32_t pp[1] = {p}, r[1], pinv[1], r2[1];
+        if constexpr (kIn == kInLimbsLsb)
+            kmod32_lsb_multi<1>(limbs, nlimbs, pp, r, pinv, r2);
+        else
+            kmod32_multi<1>(limbs, nlimbs, pp, r, pinv, r2);
+        walk_start(job.walk, p, r[0], r2[0], step, t0, 1, pinv[0]);
+    } else {
+        uint64_t pinv, r2;
+        const uint64_t r = kIn == kInLimbsLsb ? kmod64_lsb(limbs, nlimbs, p, &pinv, &r2)
+                                              : kmod64(limbs, nlimbs, p, &pinv, &r2);
+        walk_start(job.walk, p, r, pinv, r2, step, t0);
+    }
+}
+
 // One group of up to kLargeThreads primes of one job; the whole CTA calls it.
-// has: this thread holds a prime p with walk inputs a, b (the walk step and
-// start residue, or with kStartIn K' mod p and R^2 mod p, from which the
-// walk of K = K' * job.kmul starts here).  Phase 1 runs each prime's
-// continued fraction; few steps are walked at once, very many go to the
-// heavy list (tagged with job_tag), the rest are spread over the CTA as
-// items of 2^job.item_shift steps (phase 2).
-template <typename T, bool kStartIn>
+// has: this thread holds a prime p with its walk step and start residue t0.
+// Phase 1 runs each prime's continued fraction; few steps are walked at
+// once, very many go to the heavy list (tagged with job_tag), the rest are
+// spread over the CTA as items of 2^job.item_shift steps (phase 2).
+template <typename T>
 __device__ __forceinline__ void large_group(const JobDev &job, const Marker &mark, Slots<T> &sl, bool has,
-                                            T p, T a, T b, HeavyPrime *heavy,
+                                            T p, T step, T t0, HeavyPrime *heavy,
                                             unsigned long long *heavy_count, uint32_t heavy_cap,
                                             uint32_t job_tag) {
     const T w = (T)job.walk.w;
     const uint64_t minc = job.walk.jmax;  // the walk runs over j, not mi
     uint32_t items = 0;
     if (has) {
-        T step, t0;
-        if constexpr (!kStartIn)
-            step = a, t0 = b;
-        else if constexpr (sizeof(T) == 4)
-            walk_start(job.walk, p, a, b, step, t0, job.kmul);
-        else
-            walk_start(job.walk, p, a, neg_inv64(p), b, step, t0, job.kmul);
         const Entry<T> e = first_entry<T>(p, step, w, t0, minc);
         if (e.t < minc && e.y < w) {
             const uint64_t bound = rotation_steps_bound<T>(e.t, minc, e.g, p);
@@ -211,9 +240,10 @@ __device__ __forceinline__ void large_group(const JobDev &job, const Marker &mar
     __syncthreads();
 }
 
-template <typename T, bool kStartIn>
+template <typename T, int kIn>
 __global__ void __launch_bounds__(kLargeThreads)
-    large_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
+    large_kernel(const __grid_constant__ KLimbs<kIn >= kInLimbsLsb ? kParamLimbs : 1> kl, int nlimbs,
+                 JobDev job, uint64_t base, const uint32_t *__restrict__ off,
                  const unsigned long long *range, uint64_t max_count, const T *__restrict__ a_in,
                  const void *__restrict__ b_in, const unsigned long long *rrange,
                  const uint2 *__restrict__ g_mmask,
@@ -228,8 +258,11 @@ __global__ void __launch_bounds__(kLargeThreads)
     const Marker mark{job, mmask, ymask};
     const uint64_t n = min((uint64_t)(range[1] - range[0]), max_count);
     off += range[0];
-    a_in += range[0] - rrange[0];
-    const T *b = (const T *)b_in + (range[0] - rrange[0]);  // R^2 mod p, or the start residue
+    const T *b = (const T *)b_in;  // R^2 mod p, or the start residue
+    if constexpr (kIn < kInLimbsLsb) {
+        a_in += range[0] - rrange[0];
+        b += range[0] - rrange[0];
+    }
 
     for (;;) {
         if (threadIdx.x == 0) s_group = atomicAdd(group_ctr, 1ull);
@@ -239,8 +272,9 @@ __global__ void __launch_bounds__(kLargeThreads)
         const uint64_t i = group * kLargeThreads + threadIdx.x;
         const bool has = i < n;
         const T p = has ? (T)(base + off[i]) : (T)0;
-        large_group<T, kStartIn>(job, mark, sl, has, p, has ? a_in[i] : (T)0, has ? b[i] : (T)0, heavy,
-                                 heavy_count, heavy_cap, 0u);
+        T step = 0, t0 = 0;
+        if (has) walk_inputs<T, kIn>(job, kl.limb, nlimbs, p, a_in, b, i, step, t0);
+        large_group<T>(job, mark, sl, has, p, step, t0, heavy, heavy_count, heavy_cap, 0u);
     }
 }
 
@@ -300,12 +334,13 @@ __global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
         const bool has = i < it.count;
         const T *a = (const T *)it.a, *b = (const T *)it.b;
         const T p = has ? (T)(it.base + it.off[i]) : (T)0;
-        large_group<T, true>(s_job, mark, sl, has, p, has ? a[i] : (T)0, has ? b[i] : (T)0, heavy,
-                             heavy_count, heavy_cap, it.job);
+        T step = 0, t0 = 0;
+        if (has) walk_inputs<T, kInKprime>(s_job, nullptr, 0, p, a, b, i, step, t0);
+        large_group<T>(s_job, mark, sl, has, p, step, t0, heavy, heavy_count, heavy_cap, it.job);
     }
 }
 
-// The warp-alone form of one job (tuning knob large_form = 1): no CTA
+// The warp-alone form of one job (tuning knob large_form, bit 0): no CTA
 // barrier after the masks.  Each warp claims 32 primes at a time, runs their
 // continued fractions, walks the short rotations (at most direct_steps
 // steps) in place and hands the others to two lists -- up to heavy_steps
@@ -315,9 +350,10 @@ __global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
 // (small jobs: config 1's large stage 0.43 -> 0.35 ms), slower when many walks
 // of 25-100 steps leave each lane of walk_kernel only a few steps after its
 // closed-form start (config 2: 5.85 -> 8.64 ms); the tuner picks per class.
-template <typename T, bool kStartIn>
+template <typename T, int kIn>
 __global__ void __launch_bounds__(kLargeThreads)
-    large_cf_kernel(JobDev job, uint64_t base, const uint32_t *__restrict__ off,
+    large_cf_kernel(const __grid_constant__ KLimbs<kIn >= kInLimbsLsb ? kParamLimbs : 1> kl, int nlimbs,
+                    JobDev job, uint64_t base, const uint32_t *__restrict__ off,
                     const unsigned long long *range, uint64_t max_count, const T *__restrict__ a_in,
                     const void *__restrict__ b_in, const unsigned long long *rrange,
                     const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask, int masks_in_shared,
@@ -329,8 +365,11 @@ __global__ void __launch_bounds__(kLargeThreads)
     const Marker mark{job, mmask, ymask};
     const uint64_t n = min((uint64_t)(range[1] - range[0]), max_count);
     off += range[0];
-    a_in += range[0] - rrange[0];
-    const T *b = (const T *)b_in + (range[0] - rrange[0]);
+    const T *b = (const T *)b_in;
+    if constexpr (kIn < kInLimbsLsb) {
+        a_in += range[0] - rrange[0];
+        b += range[0] - rrange[0];
+    }
     const T w = (T)job.walk.w;
     const uint64_t minc = job.walk.jmax;
     const uint32_t lane = threadIdx.x & 31;
@@ -343,12 +382,7 @@ __global__ void __launch_bounds__(kLargeThreads)
         if (i >= n) continue;
         const T p = (T)(base + off[i]);
         T step, t0;
-        if constexpr (!kStartIn)
-            step = a_in[i], t0 = b[i];
-        else if constexpr (sizeof(T) == 4)
-            walk_start(job.walk, p, a_in[i], b[i], step, t0, job.kmul);
-        else
-            walk_start(job.walk, p, a_in[i], neg_inv64(p), b[i], step, t0, job.kmul);
+        walk_inputs<T, kIn>(job, kl.limb, nlimbs, p, a_in, b, i, step, t0);
         const Entry<T> e = first_entry<T>(p, step, w, t0, minc);
         if (e.t >= minc || e.y >= w) continue;
         const uint64_t bound = rotation_steps_bound<T>(e.t, minc, e.g, p);
@@ -465,7 +499,8 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
                          const unsigned long long *d_range, uint64_t max_count, const void *d_a,
                          const void *d_b, const unsigned long long *d_rrange, bool wide,
                          bool start_in_kernel, const uint2 *d_mmask, const uint2 *d_ymask,
-                         LargeScratch scratch, cudaStream_t stream) {
+                         LargeScratch scratch, cudaStream_t stream, const uint32_t *h_klimbs, int nlimbs,
+                         bool lsb) {
     if (max_count == 0) return cudaSuccess;
     const size_t mask_bytes = 8ull * (mask_words_m(job) + mask_words_y(job));
     const int in_shared = mask_bytes <= 96 * 1024;
@@ -476,6 +511,12 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
     cudaError_t e;
     if ((e = cudaMemsetAsync(scratch.counters, 0, kLargeCounters * sizeof(unsigned long long), stream))) return e;
     unsigned long long *group_ctr = scratch.counters, *heavy_count = scratch.counters + 1;
+    // K's limbs in the launch's parameters when the kernel reduces K itself
+    const bool fused = h_klimbs != nullptr && nlimbs >= 1 && nlimbs <= kParamLimbs;
+    KLimbs<kParamLimbs> klp;
+    const KLimbs<1> kl1{};
+    if (fused) memcpy(klp.limb, h_klimbs, (size_t)nlimbs * sizeof(uint32_t));
+    if (!fused && d_rrange == nullptr) return cudaErrorInvalidValue;
     auto prep = [&](auto kernel) -> cudaError_t {
         // static + dynamic shared memory above 48 KiB needs the opt-in, and
         // the kernels' static part is several KiB: always state the size
@@ -484,7 +525,7 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kLargeThreads, smem);
         return cudaSuccess;
     };
-    auto launch = [&](auto kernel, const auto *a) -> cudaError_t {
+    auto launch = [&](auto kernel, const auto &kl, const auto *a) -> cudaError_t {
         cudaError_t err = prep(kernel);
         if (err) return err;
         if (per_sm < 1) per_sm = 1;
@@ -492,35 +533,39 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
         uint64_t blocks = (uint64_t)sms * per_sm;
         if (blocks > groups) blocks = groups;
         kernel<<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask, in_shared,
+            kl, nlimbs, job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask, in_shared,
             group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
         return cudaSuccess;
     };
     // the warp-alone form: as many warps as fit, each claiming 32 primes
-    auto launch_cf = [&](auto kernel, const auto *a) -> cudaError_t {
+    auto launch_cf = [&](auto kernel, const auto &kl, const auto *a) -> cudaError_t {
         cudaError_t err = prep(kernel);
         if (err) return err;
         if (per_sm < 1) per_sm = 1;
         const uint64_t ctas = ((max_count + 31) / 32 + kLargeThreads / 32 - 1) / (kLargeThreads / 32);
         const uint64_t blocks = std::min<uint64_t>((uint64_t)sms * per_sm, ctas);
         kernel<<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask, in_shared, scratch.counters,
-            scratch.heavy, scratch.heavy_cap, scratch.walks, scratch.walk_cap);
+            kl, nlimbs, job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask, in_shared,
+            scratch.counters, scratch.heavy, scratch.heavy_cap, scratch.walks, scratch.walk_cap);
         return cudaSuccess;
     };
-    const bool alone = job.large_form == 1 && scratch.walks != nullptr;
-    if (alone && wide)
-        e = start_in_kernel ? launch_cf(large_cf_kernel<uint64_t, true>, (const uint64_t *)d_a)
-                            : launch_cf(large_cf_kernel<uint64_t, false>, (const uint64_t *)d_a);
-    else if (alone)
-        e = start_in_kernel ? launch_cf(large_cf_kernel<uint32_t, true>, (const uint32_t *)d_a)
-                            : launch_cf(large_cf_kernel<uint32_t, false>, (const uint32_t *)d_a);
-    else if (wide)
-        e = start_in_kernel ? launch(large_kernel<uint64_t, true>, (const uint64_t *)d_a)
-                            : launch(large_kernel<uint64_t, false>, (const uint64_t *)d_a);
-    else
-        e = start_in_kernel ? launch(large_kernel<uint32_t, true>, (const uint32_t *)d_a)
-                            : launch(large_kernel<uint32_t, false>, (const uint32_t *)d_a);
+    const bool alone = (job.large_form & 1u) && scratch.walks != nullptr;
+    // kernel form x prime width x where the walk inputs come from
+    auto pick = [&](auto t) -> cudaError_t {
+        using T = decltype(t);
+        const T *a = (const T *)d_a;
+        if (fused) {
+            if (alone)
+                return lsb ? launch_cf(large_cf_kernel<T, kInLimbsLsb>, klp, a)
+                           : launch_cf(large_cf_kernel<T, kInLimbsMsb>, klp, a);
+            return lsb ? launch(large_kernel<T, kInLimbsLsb>, klp, a) : launch(large_kernel<T, kInLimbsMsb>, klp, a);
+        }
+        if (alone)
+            return start_in_kernel ? launch_cf(large_cf_kernel<T, kInKprime>, kl1, a)
+                                   : launch_cf(large_cf_kernel<T, kInWalk>, kl1, a);
+        return start_in_kernel ? launch(large_kernel<T, kInKprime>, kl1, a) : launch(large_kernel<T, kInWalk>, kl1, a);
+    };
+    e = wide ? pick(uint64_t{}) : pick(uint32_t{});
     if (e) return e;
     if ((e = cudaGetLastError())) return e;
     if (alone) {

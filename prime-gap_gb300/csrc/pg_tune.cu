@@ -137,7 +137,7 @@ int pgs_tune(pgs_ctx *ctx, const pgs_job *job, int reps, pgs_tuning *out, double
         std::vector<uint32_t> values;
     };
     const std::vector<Knob> knobs = {
-        {&pgs_tuning::large_form, {0, 1}},
+        {&pgs_tuning::large_form, {0, 1, 2, 3, 4, 5, 6, 7}},
         {&pgs_tuning::heavy_steps, {1024, 2048, 4096, 8192, 16384}},
         {&pgs_tuning::item_steps, {32, 64, 128}},
         {&pgs_tuning::direct_steps, {8, 16, 24, 32, 48}},

@@ -1,10 +1,11 @@
 // Tuning classes and the tuning cache file (host C++ only; also compiled into
 // the CPU tests).
 //
-// A job's class is (P, floor(log2 SL), floor(log2 minc)): the knobs that the
-// tuner picks depend on the prime phase's shape -- the continued fractions'
-// depth and the walks' lengths (P's K, the window 2*SL+1, the walk length
-// minc) -- more than on the exact values.  The cache file has one line per
+// A job's class is (P, floor(log2 SL), floor(log2 minc), floor(log2
+// max_prime)): the knobs that the tuner picks depend on the prime phase's
+// shape -- the continued fractions' depth and the walks' lengths (P's K, the
+// window 2*SL+1, the walk length minc) and the primes' count and width
+// (max_prime) -- more than on the exact values.  The cache file has one line per
 // (device, class):
 //   device <TAB> class <TAB> direct item_steps heavy rows chunks lsb form <TAB> ms_default ms_tuned
 // Lines starting with '#' are comments.  Saving merges with the file's other
@@ -31,7 +32,7 @@ inline int ilog2(uint64_t v) {
 
 inline std::string tuning_class(const pgs_job &j) {
     std::ostringstream o;
-    o << "P" << j.p << ".SL" << ilog2(j.sieve_length) << ".minc" << ilog2(j.minc);
+    o << "P" << j.p << ".SL" << ilog2(j.sieve_length) << ".minc" << ilog2(j.minc) << ".mp" << ilog2(j.max_prime);
     return o.str();
 }
 
@@ -53,7 +54,7 @@ inline bool tuning_valid(const pgs_tuning &t) {
            (t.item_steps == 32 || t.item_steps == 64 || t.item_steps == 128) && t.heavy_steps >= 256 &&
            t.heavy_steps <= (1u << 24) && t.heavy_steps >= t.direct_steps && t.rows_per_cta >= 1 &&
            t.rows_per_cta <= 32 && t.text_chunks >= 1 && t.text_chunks <= 4 && t.kmod_lsb_limbs >= 1 &&
-           t.large_form <= 1;
+           t.large_form <= 7;
 }
 
 struct Entry {
@@ -125,7 +126,7 @@ inline int save(const std::string &path, const std::string &device, const std::m
     }
     std::ofstream out(path, std::ios::trunc);
     if (!out) return -1;
-    out << "# libpgsieve tuning: device, class (P.SL<log2>.minc<log2>), direct item_steps heavy rows chunks "
+    out << "# libpgsieve tuning: device, class (P.SL<log2>.minc<log2>.mp<log2>), direct item_steps heavy rows chunks "
            "kmod_lsb large_form, ms default and tuned\n";
     for (const auto &l : keep) out << l << '\n';
     for (const auto &kv : m) out << format_line(device, kv.first, kv.second) << '\n';

@@ -296,7 +296,7 @@ def plan(job: JobSpec) -> dict:
 
 
 def tuning_class(job: JobSpec) -> str:
-    """The job's tuning class, P<p>.SL<log2 SL>.minc<log2 minc>."""
+    """The job's tuning class, P<p>.SL<log2 SL>.minc<log2 minc>.mp<log2 max_prime>."""
     buf = ctypes.create_string_buffer(64)
     n = load().pgs_tuning_class(ctypes.byref(job.c()), buf, 64)
     if n < 0:

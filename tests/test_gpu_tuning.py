@@ -19,6 +19,12 @@ EXTREMES = [
      "kmod_lsb_limbs": 1 << 20, "large_form": 0},
     {"direct_steps": 1, "item_steps": 64, "heavy_steps": 256, "rows_per_cta": 1, "text_chunks": 3,
      "kmod_lsb_limbs": 1, "large_form": 1},
+    # K mod p inside the large-prime kernel: most significant limb first, pooled
+    {"direct_steps": 24, "item_steps": 32, "heavy_steps": 2048, "rows_per_cta": 8, "text_chunks": 4,
+     "kmod_lsb_limbs": 1 << 20, "large_form": 6},
+    # least significant limb first, warps alone
+    {"direct_steps": 16, "item_steps": 64, "heavy_steps": 4096, "rows_per_cta": 16, "text_chunks": 1,
+     "kmod_lsb_limbs": 1, "large_form": 7},
 ]
 NAMES = ["fn1", "fn1_bitcompressed", "small_d7_odd", "small_d30030", "config1", "edge_maxprime_1M"]
 
@@ -59,10 +65,13 @@ def test_tune_stores_class_result(goldens, tmp_path):
         assert s2.tuning_get(job) == (knobs, True)
 
 
+@pytest.mark.parametrize("form", [1, 2, 5, 6, 7])
 @pytest.mark.parametrize("name", ["config2", "w64_503_210"])
-def test_warp_alone_form_full_size(goldens, name):
-    """The warp-alone large-prime form (walk list) on config 2 and on a job
-    past 2^32, against the reference's md5."""
+def test_large_forms_full_size(goldens, name, form):
+    """The other large-prime forms -- warps alone with a walk list (bit 0), K
+    mod p inside the large-prime kernel for 32-bit (bit 1) and 64-bit primes
+    (bit 2) -- on config 2 and on a job past 2^32, against the reference's
+    md5."""
     import json
     from pathlib import Path
 
@@ -70,5 +79,14 @@ def test_warp_alone_form_full_size(goldens, name):
         (Path(__file__).resolve().parent / "golden" / "mix_goldens.json").read_text())[name]
     with pgsieve.Sieve(0, load_tuning=False) as s:
         job = _spec(g)
-        s.tuning_set(job, {"large_form": 1})
+        s.tuning_set(job, {"large_form": form})
         assert hashlib.md5(s.method2(job)).hexdigest() == g["md5"]
+
+
+def test_fused_kmod_config3(goldens):
+    """K mod p of 64-bit primes inside the large-prime kernel, config 3 at
+    full size (2.5e8 primes above 2^32), against the reference's md5."""
+    with pgsieve.Sieve(0, load_tuning=False) as s:
+        job = _spec(goldens["config3"])
+        s.tuning_set(job, {"large_form": 6})
+        assert hashlib.md5(s.method2(job)).hexdigest() == goldens["config3"]["md5"]
