@@ -181,6 +181,29 @@ PG_HD void udiv2_32(uint32_t n1, uint32_t n2, uint32_t d, uint32_t &q1, uint32_t
     q2 = b;
 }
 
+// Two 32-bit quotients by one divisor with the quotients themselves taken in
+// single precision (the bound of udiv2_64 below): one remainder test each
+// instead of two, for two more conversions.
+PG_HD void udiv2f_32(uint32_t n1, uint32_t n2, uint32_t d, uint32_t &q1, uint32_t &q2, int skew = 0) {
+    float rf = rcp_approx(u32_to_f32_rz(d));
+#if !defined(__CUDA_ARCH__)
+    for (; skew > 0; skew--) rf = nextafterf(rf, 2.0f);
+    for (; skew < 0; skew++) rf = nextafterf(rf, 0.0f);
+#else
+    (void)skew;
+#endif
+    const float rs = mul_f32_rz(rf, 0.999998092651367188f);  // 1 - 2^-19
+    const uint32_t a = f32_to_u32_rz(mul_f32_rz(u32_to_f32_rz(n1), rs));
+    const uint32_t b = f32_to_u32_rz(mul_f32_rz(u32_to_f32_rz(n2), rs));
+    if ((a | b) >= (1u << 17)) {
+        q1 = n1 / d;
+        q2 = n2 / d;
+        return;
+    }
+    q1 = a + (n1 - a * d >= d ? 1u : 0u);
+    q2 = b + (n2 - b * d >= d ? 1u : 0u);
+}
+
 // Two 64-bit quotients by one divisor, the same way in single precision:
 // x = (n_f * rs) with n_f = n rounded toward zero to 24 bits, rs = rcp(d_f)
 // (1 - 2^-19) rounded toward zero, d_f = d rounded toward zero.  With the
@@ -751,7 +774,7 @@ struct Entry {
 template <typename T>
 PG_HD void quot2(T n1, T n2, T d, T &q1, T &q2) {
     if constexpr (sizeof(T) == 4) {
-        udiv2_32(n1, n2, d, q1, q2);
+        udiv2f_32(n1, n2, d, q1, q2);
     } else {
         udiv2_64(n1, n2, d, q1, q2);
     }

@@ -298,6 +298,10 @@ void ah_udiv2(uint32_t n1, uint32_t n2, uint32_t d, int skew, uint32_t *out2) {
     pg::udiv2_32(n1, n2, d, out2[0], out2[1], skew);
 }
 
+void ah_udiv2f(uint32_t n1, uint32_t n2, uint32_t d, int skew, uint32_t *out2) {
+    pg::udiv2f_32(n1, n2, d, out2[0], out2[1], skew);
+}
+
 void ah_udiv2_64(uint64_t n1, uint64_t n2, uint64_t d, int skew, uint64_t *out2) {
     pg::udiv2_64(n1, n2, d, out2[0], out2[1], skew);
 }

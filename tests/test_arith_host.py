@@ -41,6 +41,9 @@ def ah(built):
                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
     lib.ah_pow32_mod.restype = ctypes.c_uint32
     lib.ah_pow32_mod.argtypes = [ctypes.c_uint32, ctypes.c_int]
+    lib.ah_udiv2f.restype = None
+    lib.ah_udiv2f.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
+                              ctypes.POINTER(ctypes.c_uint32)]
     lib.ah_udiv2_64.restype = None
     lib.ah_udiv2_64.argtypes = [u64, u64, u64, ctypes.c_int, ctypes.POINTER(u64)]
     lib.ah_udiv2.restype = None
@@ -446,6 +449,8 @@ def test_udiv2_shared_reciprocal_exact(ah):
         for skew in (-2, -1, 0, 1, 2):
             ah.ah_udiv2(n1, n2, d, skew, out)
             assert (out[0], out[1]) == (n1 // d, n2 // d), (n1, n2, d, skew)
+            ah.ah_udiv2f(n1, n2, d, skew, out)
+            assert (out[0], out[1]) == (n1 // d, n2 // d), ("f", n1, n2, d, skew)
 
 
 def test_udiv2_64_shared_reciprocal_exact(ah):
