@@ -389,8 +389,11 @@ PG_HD void kmod32_lsb_multi(const uint32_t *limbs, int n, const uint32_t *p, uin
     uint32_t X[NP];
 #pragma unroll
     for (int k = 0; k < NP; k++) X[k] = r2[k];
-    int top = 31;
-    while (top > 0 && !(((uint32_t)n >> top) & 1u)) top--;
+#if defined(__CUDA_ARCH__)
+    const int top = 31 - __clz(n);  // n >= 1: the leading bit
+#else
+    const int top = 31 - __builtin_clz((unsigned)n);
+#endif
     for (int b = top - 1; b >= 0; b--) {
         const bool one = ((uint32_t)n >> b) & 1u;
 #pragma unroll
@@ -835,17 +838,20 @@ PG_HD Entry<T> first_entry(T p, T a, T w, T y0, uint64_t t_lim = ~0ull) {
 // mi = mi0 + (n - W)*kp + W*kn with W = floor(Y / C); it is a hit iff the
 // residue is below w.  Returns an upper bound on the steps n with mi < mi_hi
 // (mi_n - mi0 >= n*p/C - kp - kn since kp*dn + kn*up = p).
+// Also: every step advances mi by at least min(kp, kn), so there are at most
+// (mi_hi - mi0) / min(kp, kn) + 1 steps.  Single precision with a relative
+// margin (each term within 2^-21, the margin 1.0001) and 2 added: the bound
+// only sizes work, but must not fall below the true count.  Walk indices are
+// below 2^31, so the span converts from 32 bits; a 32-bit prime's gaps and
+// step costs too, with no 64-bit conversion or division.
 template <typename T>
 PG_HD uint64_t rotation_steps_bound(uint64_t mi0, uint64_t mi_hi, const ThreeGap<T> &g, T p) {
     if (mi0 >= mi_hi) return 0;
+    const float span = (float)(uint32_t)(mi_hi - mi0);
     const float C = (float)g.up + (float)g.dn;
-    // single precision with a relative margin: the result only sizes work
-    float n = ((float)(mi_hi - mi0) + (float)g.kp + (float)g.kn) * C / (float)p;
-    uint64_t b = (uint64_t)(n * 1.0001f) + 2;
-    // every step advances mi by at least min(kp, kn)
-    const uint64_t kmin = g.kp < g.kn ? (uint64_t)g.kp : (uint64_t)g.kn;
-    const uint64_t cap = (mi_hi - mi0) / kmin + 1;
-    return b < cap ? b : cap;
+    const float n = (span + (float)g.kp + (float)g.kn) * C * rcp_approx((float)p);
+    const float c = span * rcp_approx((float)(g.kp < g.kn ? g.kp : g.kn));
+    return f32_to_u32_rz((n < c ? n : c) * 1.0001f + 2.0f);
 }
 
 // The rotation's walk in 32-bit arithmetic, for walk indices below
@@ -863,12 +869,9 @@ PG_HD void rotation_at32(uint32_t mi0, uint32_t y0, const ThreeGap<uint32_t> &g,
     uint64_t W;
     if (n0 < (1u << 19)) {
         // W = floor(Y / C) <= n0 + 1 < 2^19 + 1 (y0 < C, up < C): a
-        // single-precision quotient is within 2^-21 relative, so within one
-#if defined(__CUDA_ARCH__)
-        W = (uint64_t)((float)Y * __fdividef(1.0f, (float)C));
-#else
-        W = (uint64_t)((float)Y * (1.0f / (float)C));
-#endif
+        // single-precision quotient (from 32-bit operands, Y = y0 + n0 up)
+        // is within 2^-20 relative, so within one
+        W = f32_to_u32_rz(((float)n0 * (float)g.up + (float)y0) * rcp_approx((float)C));
         const int64_t rem = (int64_t)(Y - W * C);
         if (rem < 0) W--;
         else if (rem >= (int64_t)C) W++;

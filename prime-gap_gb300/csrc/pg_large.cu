@@ -29,6 +29,7 @@
 // bit of the L2-resident composite bitset with a global atomicOr.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 
 #include "pg_arith.cuh"
 #include "pg_internal.h"
@@ -102,18 +103,21 @@ __host__ __device__ inline uint32_t mask_words_m(const JobDev &job) { return (ui
 __host__ __device__ inline uint32_t mask_words_y(const JobDev &job) { return (job.walk.w + 31) / 32; }
 
 // Copies the masks ({bits, rank} pairs) to shared memory when they fit
-// (in_shared); returns where the kernel reads them.
+// (kShared, a template parameter so that every mask read of a walk step
+// compiles to a shared-memory load rather than a generic one); returns where
+// the kernel reads them.
+template <bool kShared>
 __device__ __forceinline__ void load_masks(const JobDev &job, const uint2 *g_mmask, const uint2 *g_ymask,
-                                           int in_shared, uint2 *s_masks, const uint2 *&mmask,
-                                           const uint2 *&ymask) {
-    const uint32_t mwords = mask_words_m(job), ywords = mask_words_y(job);
-    mmask = g_mmask;
-    ymask = g_ymask;
-    if (in_shared) {
+                                           uint2 *s_masks, const uint2 *&mmask, const uint2 *&ymask) {
+    if constexpr (kShared) {
+        const uint32_t mwords = mask_words_m(job), ywords = mask_words_y(job);
         for (uint32_t i = threadIdx.x; i < mwords; i += blockDim.x) s_masks[i] = g_mmask[i];
         for (uint32_t i = threadIdx.x; i < ywords; i += blockDim.x) s_masks[mwords + i] = g_ymask[i];
         mmask = s_masks;
         ymask = s_masks + mwords;
+    } else {
+        mmask = g_mmask;
+        ymask = g_ymask;
     }
     __syncthreads();
 }
@@ -240,21 +244,21 @@ __device__ __forceinline__ void large_group(const JobDev &job, const Marker &mar
     __syncthreads();
 }
 
-template <typename T, int kIn>
+template <typename T, int kIn, bool kShared>
 __global__ void __launch_bounds__(kLargeThreads)
     large_kernel(const __grid_constant__ KLimbs<kIn >= kInLimbsLsb ? kParamLimbs : 1> kl, int nlimbs,
                  JobDev job, uint64_t base, const uint32_t *__restrict__ off,
                  const unsigned long long *range, uint64_t max_count, const T *__restrict__ a_in,
                  const void *__restrict__ b_in, const unsigned long long *rrange,
                  const uint2 *__restrict__ g_mmask,
-                 const uint2 *__restrict__ g_ymask, int masks_in_shared,
+                 const uint2 *__restrict__ g_ymask,
                  unsigned long long *group_ctr, HeavyPrime *heavy, unsigned long long *heavy_count,
                  uint32_t heavy_cap) {
     extern __shared__ uint2 s_masks[];
     __shared__ Slots<T> sl;
     __shared__ unsigned long long s_group;
     const uint2 *mmask, *ymask;
-    load_masks(job, g_mmask, g_ymask, masks_in_shared, s_masks, mmask, ymask);
+    load_masks<kShared>(job, g_mmask, g_ymask, s_masks, mmask, ymask);
     const Marker mark{job, mmask, ymask};
     const uint64_t n = min((uint64_t)(range[1] - range[0]), max_count);
     off += range[0];
@@ -350,18 +354,18 @@ __global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
 // (small jobs: config 1's large stage 0.43 -> 0.35 ms), slower when many walks
 // of 25-100 steps leave each lane of walk_kernel only a few steps after its
 // closed-form start (config 2: 5.85 -> 8.64 ms); the tuner picks per class.
-template <typename T, int kIn>
+template <typename T, int kIn, bool kShared>
 __global__ void __launch_bounds__(kLargeThreads)
     large_cf_kernel(const __grid_constant__ KLimbs<kIn >= kInLimbsLsb ? kParamLimbs : 1> kl, int nlimbs,
                     JobDev job, uint64_t base, const uint32_t *__restrict__ off,
                     const unsigned long long *range, uint64_t max_count, const T *__restrict__ a_in,
                     const void *__restrict__ b_in, const unsigned long long *rrange,
-                    const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask, int masks_in_shared,
+                    const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask,
                     unsigned long long *ctr, HeavyPrime *heavy, uint32_t heavy_cap, WalkEntry *walks,
                     uint32_t walk_cap) {
     extern __shared__ uint2 s_masks[];
     const uint2 *mmask, *ymask;
-    load_masks(job, g_mmask, g_ymask, masks_in_shared, s_masks, mmask, ymask);
+    load_masks<kShared>(job, g_mmask, g_ymask, s_masks, mmask, ymask);
     const Marker mark{job, mmask, ymask};
     const uint64_t n = min((uint64_t)(range[1] - range[0]), max_count);
     off += range[0];
@@ -409,13 +413,13 @@ __global__ void __launch_bounds__(kLargeThreads)
 
 // The walk list of the warp-alone form: each warp claims one walk and splits
 // its steps evenly over its lanes (each lane starts from the closed form).
+template <bool kShared>
 __global__ void __launch_bounds__(kLargeThreads)
     walk_kernel(JobDev job, const WalkEntry *__restrict__ walks, const unsigned long long *ctr, uint32_t walk_cap,
-                const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask, int masks_in_shared,
-                unsigned long long *claim) {
+                const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask, unsigned long long *claim) {
     extern __shared__ uint2 s_masks[];
     const uint2 *mmask, *ymask;
-    load_masks(job, g_mmask, g_ymask, masks_in_shared, s_masks, mmask, ymask);
+    load_masks<kShared>(job, g_mmask, g_ymask, s_masks, mmask, ymask);
     const Marker mark{job, mmask, ymask};
     const uint64_t nw = min((uint64_t)ctr[2], (uint64_t)walk_cap);
     const uint32_t jmax = (uint32_t)job.walk.jmax, w = job.walk.w, lane = threadIdx.x & 31;
@@ -435,14 +439,14 @@ __global__ void __launch_bounds__(kLargeThreads)
 }
 
 // One CTA per heavy prime: its rotation steps split over the CTA's threads.
+template <bool kShared>
 __global__ void __launch_bounds__(kLargeThreads)
     heavy_kernel(JobDev job, const HeavyPrime *__restrict__ heavy,
                  const unsigned long long *heavy_count, uint32_t heavy_cap,
-                 const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask,
-                 int masks_in_shared) {
+                 const uint2 *__restrict__ g_mmask, const uint2 *__restrict__ g_ymask) {
     extern __shared__ uint2 s_masks[];
     const uint2 *mmask, *ymask;
-    load_masks(job, g_mmask, g_ymask, masks_in_shared, s_masks, mmask, ymask);
+    load_masks<kShared>(job, g_mmask, g_ymask, s_masks, mmask, ymask);
     const Marker mark{job, mmask, ymask};
     const uint64_t nh = min((uint64_t)*heavy_count, (uint64_t)heavy_cap);
     const uint32_t w = job.walk.w;
@@ -533,7 +537,7 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
         uint64_t blocks = (uint64_t)sms * per_sm;
         if (blocks > groups) blocks = groups;
         kernel<<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            kl, nlimbs, job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask, in_shared,
+            kl, nlimbs, job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask,
             group_ctr, scratch.heavy, heavy_count, scratch.heavy_cap);
         return cudaSuccess;
     };
@@ -545,41 +549,54 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
         const uint64_t ctas = ((max_count + 31) / 32 + kLargeThreads / 32 - 1) / (kLargeThreads / 32);
         const uint64_t blocks = std::min<uint64_t>((uint64_t)sms * per_sm, ctas);
         kernel<<<(unsigned)blocks, kLargeThreads, smem, stream>>>(
-            kl, nlimbs, job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask, in_shared,
+            kl, nlimbs, job, base, d_off, d_range, max_count, a, d_b, d_rrange, d_mmask, d_ymask,
             scratch.counters, scratch.heavy, scratch.heavy_cap, scratch.walks, scratch.walk_cap);
         return cudaSuccess;
     };
     const bool alone = (job.large_form & 1u) && scratch.walks != nullptr;
-    // kernel form x prime width x where the walk inputs come from
-    auto pick = [&](auto t) -> cudaError_t {
+    // kernel form x prime width x where the walk inputs come from x where the masks live
+    auto pick = [&](auto t, auto sh) -> cudaError_t {
         using T = decltype(t);
+        constexpr bool S = decltype(sh)::value;
         const T *a = (const T *)d_a;
         if (fused) {
             if (alone)
-                return lsb ? launch_cf(large_cf_kernel<T, kInLimbsLsb>, klp, a)
-                           : launch_cf(large_cf_kernel<T, kInLimbsMsb>, klp, a);
-            return lsb ? launch(large_kernel<T, kInLimbsLsb>, klp, a) : launch(large_kernel<T, kInLimbsMsb>, klp, a);
+                return lsb ? launch_cf(large_cf_kernel<T, kInLimbsLsb, S>, klp, a)
+                           : launch_cf(large_cf_kernel<T, kInLimbsMsb, S>, klp, a);
+            return lsb ? launch(large_kernel<T, kInLimbsLsb, S>, klp, a)
+                       : launch(large_kernel<T, kInLimbsMsb, S>, klp, a);
         }
         if (alone)
-            return start_in_kernel ? launch_cf(large_cf_kernel<T, kInKprime>, kl1, a)
-                                   : launch_cf(large_cf_kernel<T, kInWalk>, kl1, a);
-        return start_in_kernel ? launch(large_kernel<T, kInKprime>, kl1, a) : launch(large_kernel<T, kInWalk>, kl1, a);
+            return start_in_kernel ? launch_cf(large_cf_kernel<T, kInKprime, S>, kl1, a)
+                                   : launch_cf(large_cf_kernel<T, kInWalk, S>, kl1, a);
+        return start_in_kernel ? launch(large_kernel<T, kInKprime, S>, kl1, a)
+                               : launch(large_kernel<T, kInWalk, S>, kl1, a);
     };
-    e = wide ? pick(uint64_t{}) : pick(uint32_t{});
+    auto walks_heavy = [&](auto sh) -> cudaError_t {
+        constexpr bool S = decltype(sh)::value;
+        cudaError_t err;
+        if (alone) {
+            if ((err = prep(walk_kernel<S>))) return err;
+            if (per_sm < 1) per_sm = 1;
+            walk_kernel<S><<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(
+                job, scratch.walks, scratch.counters, scratch.walk_cap, d_mmask, d_ymask, scratch.counters + 3);
+            if ((err = cudaGetLastError())) return err;
+        }
+        if ((err = prep(heavy_kernel<S>))) return err;
+        if (per_sm < 1) per_sm = 1;
+        heavy_kernel<S><<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(
+            job, scratch.heavy, heavy_count, scratch.heavy_cap, d_mmask, d_ymask);
+        return cudaGetLastError();
+    };
+    using Shared = std::true_type;
+    using Global = std::false_type;
+    if (in_shared)
+        e = wide ? pick(uint64_t{}, Shared{}) : pick(uint32_t{}, Shared{});
+    else
+        e = wide ? pick(uint64_t{}, Global{}) : pick(uint32_t{}, Global{});
     if (e) return e;
     if ((e = cudaGetLastError())) return e;
-    if (alone) {
-        if ((e = prep(walk_kernel))) return e;
-        if (per_sm < 1) per_sm = 1;
-        walk_kernel<<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(
-            job, scratch.walks, scratch.counters, scratch.walk_cap, d_mmask, d_ymask, in_shared, scratch.counters + 3);
-        if ((e = cudaGetLastError())) return e;
-    }
-    if ((e = prep(heavy_kernel))) return e;
-    if (per_sm < 1) per_sm = 1;
-    heavy_kernel<<<(unsigned)(sms * per_sm), kLargeThreads, smem, stream>>>(
-        job, scratch.heavy, heavy_count, scratch.heavy_cap, d_mmask, d_ymask, in_shared);
-    return cudaGetLastError();
+    return in_shared ? walks_heavy(Shared{}) : walks_heavy(Global{});
 }
 
 cudaError_t large_multi(const LargeJob *d_jobs, const LargeItem *d_items, uint32_t n_items, uint32_t n_tiles,
