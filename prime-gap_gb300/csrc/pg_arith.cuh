@@ -909,6 +909,36 @@ PG_HD void rotation_walk32(uint32_t mi, uint32_t y, const ThreeGap<uint32_t> &g,
     }
 }
 
+// return_walk32: the same walk (the circle steps [0, steps) from (mi, y),
+// while mi < mi_hi), visiting only its hits: from a hit y < w the next one
+// is y + up (one step, kp) if that is below w, else y - dn (one step, kn) if
+// y >= dn, else y + up - dn (two steps, the first off the window, kp + kn):
+// the three-gap first-return map (p > 2w).  A start off the window (y >= w
+// > dn) wraps into it in one step.  emit(mi, y, true) at every hit; about a
+// third of a rotation's steps are misses, whose mask reads this saves.
+// Step costs are clamped to mi_hi, so mi stays below 2 mi_hi < 2^32.
+template <typename Emit>
+PG_HD void return_walk32(uint32_t mi, uint32_t y, const ThreeGap<uint32_t> &g, uint32_t w, uint32_t mi_hi,
+                         uint32_t steps, Emit &emit) {
+    const uint32_t up = g.up, dn = g.dn;
+    const uint32_t kp = g.kp < mi_hi ? g.kp : mi_hi, kn = g.kn < mi_hi ? g.kn : mi_hi;
+    const uint32_t kpn = kp + kn < mi_hi ? kp + kn : mi_hi;
+    uint32_t k = 0;
+    if (y >= w && steps) {
+        y -= dn;
+        mi += kn;
+        k = 1;
+    }
+    while (k < steps && mi < mi_hi) {
+        emit(mi, y, true);
+        const uint32_t a = y + up;
+        const bool near = a < w, wrap = y >= dn;
+        y = near ? a : (wrap ? y - dn : a - dn);
+        mi += near ? kp : (wrap ? kn : kpn);
+        k += (near | wrap) ? 1u : 2u;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // hit enumeration
 

@@ -179,7 +179,7 @@ __device__ __forceinline__ void large_group(const JobDev &job, const Marker &mar
             bool local = true;
             if (bound <= job.direct_steps) {
                 // few steps: walk the rotation here
-                rotation_walk32((uint32_t)e.t, (uint32_t)e.y, gap32(e.g, (uint32_t)minc), (uint32_t)w,
+                return_walk32((uint32_t)e.t, (uint32_t)e.y, gap32(e.g, (uint32_t)minc), (uint32_t)w,
                                 (uint32_t)minc, (uint32_t)bound, mark);
                 local = false;
             } else if (bound > job.heavy_steps) {
@@ -239,7 +239,7 @@ __device__ __forceinline__ void large_group(const JobDev &job, const Marker &mar
             gap32(ThreeGap<T>{sl.kp[s], (T)sl.up[s], sl.kn[s], (T)sl.dn[s]}, (uint32_t)minc);
         uint32_t y, mi;
         rotation_at32(sl.mi0[s], sl.y0[s], g, (uint32_t)n0, (uint32_t)minc, y, mi);
-        rotation_walk32(mi, y, g, (uint32_t)w, (uint32_t)minc, 1u << shift, mark);
+        return_walk32(mi, y, g, (uint32_t)w, (uint32_t)minc, 1u << shift, mark);
     }
     __syncthreads();
 }
@@ -407,7 +407,7 @@ __global__ void __launch_bounds__(kLargeThreads)
                 continue;
             }
         }
-        rotation_walk32((uint32_t)e.t, (uint32_t)e.y, g32, (uint32_t)w, (uint32_t)minc, (uint32_t)bound, mark);
+        return_walk32((uint32_t)e.t, (uint32_t)e.y, g32, (uint32_t)w, (uint32_t)minc, (uint32_t)bound, mark);
     }
 }
 
@@ -434,7 +434,7 @@ __global__ void __launch_bounds__(kLargeThreads)
         if (n0 >= we.steps) continue;
         uint32_t y, mi;
         rotation_at32(we.mi0, we.y0, g, n0, jmax, y, mi);
-        rotation_walk32(mi, y, g, w, jmax, per, mark);
+        return_walk32(mi, y, g, w, jmax, per, mark);
     }
 }
 
@@ -458,7 +458,7 @@ __global__ void __launch_bounds__(kLargeThreads)
         for (uint64_t it = threadIdx.x; it < items; it += blockDim.x) {
             uint32_t y, mi;
             rotation_at32(hp.mi0, hp.y0, g, (uint32_t)(it << shift), jmax, y, mi);
-            rotation_walk32(mi, y, g, w, jmax, 1u << shift, mark);
+            return_walk32(mi, y, g, w, jmax, 1u << shift, mark);
         }
     }
 }
@@ -489,7 +489,7 @@ __global__ void __launch_bounds__(kLargeThreads)
         for (uint64_t it = threadIdx.x; it < items; it += blockDim.x) {
             uint32_t y, mi;
             rotation_at32(hp.mi0, hp.y0, g, (uint32_t)(it << shift), jmax, y, mi);
-            rotation_walk32(mi, y, g, w, jmax, 1u << shift, mark);
+            return_walk32(mi, y, g, w, jmax, 1u << shift, mark);
         }
     }
 }

@@ -298,6 +298,31 @@ void ah_udiv2(uint32_t n1, uint32_t n2, uint32_t d, int skew, uint32_t *out2) {
     pg::udiv2_32(n1, n2, d, out2[0], out2[1], skew);
 }
 
+// The walk from (mi, y) over `steps` circle steps below mi_hi, both ways:
+// circle steps (rotation_walk32) and hit to hit (return_walk32).  Writes the
+// hits of each as (mi, y) pairs; returns 1 when the two lists agree.
+struct HitList {
+    uint32_t *out;
+    size_t cap, n;
+    void operator()(uint64_t mi, uint32_t y, bool hit) {
+        if (!hit) return;
+        if (n + 2 <= cap) out[n] = (uint32_t)mi, out[n + 1] = y;
+        n += 2;
+    }
+};
+int ah_return_walk_agrees(uint32_t mi, uint32_t y, uint32_t kp, uint32_t up, uint32_t kn, uint32_t dn,
+                          uint32_t w, uint32_t mi_hi, uint32_t steps, uint32_t *buf, size_t cap, size_t *nhits) {
+    const pg::ThreeGap<uint32_t> g{kp, up, kn, dn};
+    HitList a{buf, cap / 2, 0}, b{buf + cap / 2, cap / 2, 0};
+    pg::rotation_walk32(mi, y, g, w, mi_hi, steps, a);
+    pg::return_walk32(mi, y, g, w, mi_hi, steps, b);
+    *nhits = a.n / 2;
+    if (a.n != b.n) return 0;
+    for (size_t i = 0; i < a.n && i < cap / 2; i++)
+        if (a.out[i] != b.out[i]) return 0;
+    return 1;
+}
+
 void ah_udiv2f(uint32_t n1, uint32_t n2, uint32_t d, int skew, uint32_t *out2) {
     pg::udiv2f_32(n1, n2, d, out2[0], out2[1], skew);
 }

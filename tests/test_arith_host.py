@@ -41,6 +41,9 @@ def ah(built):
                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(u64), ctypes.c_size_t]
     lib.ah_pow32_mod.restype = ctypes.c_uint32
     lib.ah_pow32_mod.argtypes = [ctypes.c_uint32, ctypes.c_int]
+    lib.ah_return_walk_agrees.restype = ctypes.c_int
+    lib.ah_return_walk_agrees.argtypes = [ctypes.c_uint32] * 9 + [ctypes.POINTER(ctypes.c_uint32), ctypes.c_size_t,
+                                                                 ctypes.POINTER(ctypes.c_size_t)]
     lib.ah_udiv2f.restype = None
     lib.ah_udiv2f.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int,
                               ctypes.POINTER(ctypes.c_uint32)]
@@ -420,6 +423,38 @@ def test_hits_grid_split_vs_oracle(ah, threads, cta, cap):
         k = min(n, cap)
         assert n == len(want), (M, max_mi, SL, q, r)
         assert list(zip(mi[:k], md[:k])) == [tuple(h) for h in want[:k]], (M, max_mi, SL, q, r)
+
+
+def test_return_walk_equals_circle_walk(ah):
+    """The hit-to-hit walk (three-gap first-return map) emits exactly the
+    circle walk's hits, in order, for any start on the circle (a hit or a
+    miss), any step budget (items of the rotation, budgets ending on the
+    middle of a two-step return) and any mi bound."""
+    rng = random.Random(23)
+    cap = 1 << 16
+    buf = (ctypes.c_uint32 * cap)()
+    n = ctypes.c_size_t()
+    total = 0
+    for _ in range(3000):
+        bits = rng.choice([13, 21, 29, 32])
+        p = _rand_prime(rng, 2 ** (bits - 1), 2 ** bits)
+        w = rng.randrange(3, max(4, min(p // 2 - 1, 1 << 16)))
+        if 2 * w >= p:
+            continue
+        a = rng.randrange(1, p)
+        out = (ctypes.c_uint64 * 6)()
+        ah.ah_first_entry(p, a, w, rng.randrange(0, p), out)
+        _, _, kp, up, kn, dn = list(out)
+        C = up + dn
+        mi_hi = rng.choice([1, 7, 1000, 50000, 1 << 30])
+        steps = rng.choice([1, 2, 3, 24, 64, 1000])
+        kp32, kn32 = min(kp, mi_hi), min(kn, mi_hi)
+        y = rng.randrange(0, C)
+        mi = rng.randrange(0, mi_hi)
+        ok = ah.ah_return_walk_agrees(mi, y, kp32, up, kn32, dn, w, mi_hi, steps, buf, cap, ctypes.byref(n))
+        assert ok == 1, (p, a, w, mi, y, mi_hi, steps)
+        total += n.value
+    assert total > 10000
 
 
 def test_udiv2_shared_reciprocal_exact(ah):
