@@ -64,10 +64,14 @@ PG_HD uint32_t neg_inv32(uint32_t p) {
     return 0u - x;
 }
 
-// -p^{-1} mod 2^64 for odd p.
+// -p^{-1} mod 2^64 for odd p: the 32-bit inverse (three 32-bit steps from
+// 5 bits), then one 64-bit Newton step doubles it to 64 bits.
 PG_HD uint64_t neg_inv64(uint64_t p) {
-    uint64_t x = p;
-    for (int i = 0; i < 5; i++) x *= 2ull - p * x;
+    const uint32_t p32 = (uint32_t)p;
+    uint32_t x32 = (3u * p32) ^ 2u;
+    for (int i = 0; i < 3; i++) x32 *= 2u - p32 * x32;
+    uint64_t x = x32;
+    x *= 2ull - p * x;
     return 0ull - x;
 }
 
@@ -115,15 +119,33 @@ PG_HD float u32_to_f32_rz(uint32_t v) {
     return f;
 #endif
 }
-PG_HD float u64_to_f32_rz(uint64_t v) {
+// v rounded toward zero to 24 bits (exact top-24-bit truncation).
+PG_HD float u64_trunc24(uint64_t v) {
 #if defined(__CUDA_ARCH__)
-    return __ull2float_rz(v);
+    const int sh = v < (1ull << 24) ? 0 : 64 - __clzll((long long)v) - 24;
 #else
-    if (v < (1ull << 24)) return (float)v;
-    const int sh = 64 - __builtin_clzll(v) - 24;  // keep the top 24 bits
+    const int sh = v < (1ull << 24) ? 0 : 64 - __builtin_clzll(v) - 24;
+#endif
     return ldexpf((float)(v >> sh), sh);
+}
+// A 64-bit value in single precision rounded toward zero through its two
+// 32-bit halves: rz(rz(hi) 2^32 + rz(lo)), at most 2^-22 below v and never
+// above it.  (A direct 64-bit conversion runs on the double-precision pipe,
+// which is narrow on this part.)
+PG_HD float u64_to_f32_rz(uint64_t v) {
+    const uint32_t hi = (uint32_t)(v >> 32), lo = (uint32_t)v;
+#if defined(__CUDA_ARCH__)
+    if (hi == 0) return __uint2float_rz(lo);
+    return __fadd_rz(__fmul_rz(__uint2float_rz(hi), 4294967296.0f), __uint2float_rz(lo));
+#else
+    if (hi == 0) return u32_to_f32_rz(lo);
+    // the exact sum of the two rounded halves, then rounded toward zero
+    const uint64_t s = ((uint64_t)u32_to_f32_rz(hi) << 32) + (uint64_t)u32_to_f32_rz(lo);
+    return u64_trunc24(s);
 #endif
 }
+PG_HD float as_f32(uint32_t v) { return (float)v; }
+PG_HD float as_f32(uint64_t v) { return u64_to_f32_rz(v); }
 PG_HD float rcp_approx(float x) {
 #if defined(__CUDA_ARCH__)
     float r;
@@ -205,9 +227,10 @@ PG_HD void udiv2f_32(uint32_t n1, uint32_t n2, uint32_t d, uint32_t &q1, uint32_
 }
 
 // Two 64-bit quotients by one divisor, the same way in single precision:
-// x = (n_f * rs) with n_f = n rounded toward zero to 24 bits, rs = rcp(d_f)
-// (1 - 2^-19) rounded toward zero, d_f = d rounded toward zero.  With the
-// reciprocal within 3 ulps, (n/d)(1 - 2^-18) < x < n/d, so q0 = floor(x)
+// x = (n_f * rs) with n_f = n rounded toward zero (u64_to_f32_rz: within
+// 2^-22), rs = rcp(d_f) (1 - 2^-19) rounded toward zero, d_f = d rounded
+// toward zero.  With the reciprocal within 3 ulps, (n/d)(1 - 2^-18) < x <
+// n/d, so q0 = floor(x)
 // never exceeds q = floor(n/d) and, while q0 < 2^17 (hence n/d < 2^18), is
 // at least q - 1: one remainder test finishes it.  A larger q0 takes the
 // exact division.
@@ -230,6 +253,31 @@ PG_HD void udiv2_64(uint64_t n1, uint64_t n2, uint64_t d, uint64_t &q1, uint64_t
     const uint64_t ra = n1 - (uint64_t)a * d, rb = n2 - (uint64_t)b * d;
     q1 = a + (ra >= d ? 1u : 0u);
     q2 = b + (rb >= d ? 1u : 0u);
+}
+
+// 2^64 mod p and 2^128 mod p for odd 3 <= p < 2^46 with neither a division
+// nor double precision: x <- x 2^16 mod p eight times from x = 1.  Each
+// step's quotient is below 2^16 (x < p), so one single-precision reciprocal
+// gives it or one less (the bound of udiv2_64) and one remainder test ends it.
+PG_HD void pow64_128_mod(uint64_t p, uint64_t &r1, uint64_t &r2, int skew = 0) {
+    float rf = rcp_approx(u64_to_f32_rz(p));
+#if !defined(__CUDA_ARCH__)
+    for (; skew > 0; skew--) rf = nextafterf(rf, 2.0f);
+    for (; skew < 0; skew++) rf = nextafterf(rf, 0.0f);
+#else
+    (void)skew;
+#endif
+    const float rs = mul_f32_rz(rf, 0.999998092651367188f);  // 1 - 2^-19
+    uint64_t x = 1;
+#pragma unroll
+    for (int i = 0; i < 8; i++) {
+        const uint64_t n = x << 16;  // < 2^62
+        const uint32_t q = f32_to_u32_rz(mul_f32_rz(u64_to_f32_rz(n), rs));
+        uint64_t t = n - (uint64_t)q * p;
+        x = t >= p ? t - p : t;
+        if (i == 3) r1 = x;
+    }
+    r2 = x;
 }
 
 // 2^32 mod p for odd p >= 3 without a hardware division.  p >= 2^31: 2^32 - p.
@@ -411,8 +459,8 @@ PG_HD void kmod32_lsb_multi(const uint32_t *limbs, int n, const uint32_t *p, uin
 PG_HD uint64_t kmod64(const uint32_t *limbs, int n, uint64_t p, uint64_t *pinv_out = nullptr,
                       uint64_t *r2_out = nullptr) {
     const uint64_t pinv = neg_inv64(p);
-    const uint64_t r1 = (0ull - p) % p;                             // 2^64 mod p
-    const uint64_t r2 = mulmod_u64(r1, r1, p, 1.0 / (double)p);  // 2^128 mod p
+    uint64_t r1, r2;  // 2^64 and 2^128 mod p
+    pow64_128_mod(p, r1, r2);
     if (pinv_out) *pinv_out = pinv, *r2_out = r2;
     uint64_t u = 0;
     const int nw = (n + 1) / 2;
@@ -447,8 +495,8 @@ PG_HD uint64_t montmul64(uint64_t a, uint64_t b, uint64_t p, uint64_t pinv) {
 PG_HD uint64_t kmod64_lsb(const uint32_t *limbs, int n, uint64_t p, uint64_t *pinv_out = nullptr,
                           uint64_t *r2_out = nullptr) {
     const uint64_t pinv = neg_inv64(p);
-    const uint64_t r1 = (0ull - p) % p;                          // 2^64 mod p
-    const uint64_t r2 = mulmod_u64(r1, r1, p, 1.0 / (double)p);  // 2^128 mod p
+    uint64_t r1, r2;  // 2^64 and 2^128 mod p
+    pow64_128_mod(p, r1, r2);
     if (pinv_out) *pinv_out = pinv, *r2_out = r2;
     const int nw = (n + 1) / 2;
     uint64_t W = 0;
@@ -848,9 +896,9 @@ template <typename T>
 PG_HD uint64_t rotation_steps_bound(uint64_t mi0, uint64_t mi_hi, const ThreeGap<T> &g, T p) {
     if (mi0 >= mi_hi) return 0;
     const float span = (float)(uint32_t)(mi_hi - mi0);
-    const float C = (float)g.up + (float)g.dn;
-    const float n = (span + (float)g.kp + (float)g.kn) * C * rcp_approx((float)p);
-    const float c = span * rcp_approx((float)(g.kp < g.kn ? g.kp : g.kn));
+    const float C = as_f32(g.up) + as_f32(g.dn);
+    const float n = (span + as_f32(g.kp) + as_f32(g.kn)) * C * rcp_approx(as_f32(p));
+    const float c = span * rcp_approx(as_f32(g.kp < g.kn ? g.kp : g.kn));
     return f32_to_u32_rz((n < c ? n : c) * 1.0001f + 2.0f);
 }
 

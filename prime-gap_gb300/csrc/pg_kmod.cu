@@ -172,8 +172,8 @@ __global__ void __launch_bounds__(kKmodThreads)
         if (idx >= n) return;
         const uint64_t p = base + off[idx];
         const uint64_t pinv = neg_inv64(p);
-        const uint64_t r1 = (0ull - p) % p;                          // 2^64 mod p
-        const uint64_t r2 = mulmod_u64(r1, r1, p, 1.0 / (double)p);  // 2^128 mod p
+        uint64_t r1, r2;  // 2^64 and 2^128 mod p
+        pow64_128_mod(p, r1, r2);
         uint64_t acc = 0;
         for (int g = 0; g < G; g++) {
             const int lo = (int)so[g], nl = (int)so[g + 1] - lo;

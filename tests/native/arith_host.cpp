@@ -323,6 +323,10 @@ int ah_return_walk_agrees(uint32_t mi, uint32_t y, uint32_t kp, uint32_t up, uin
     return 1;
 }
 
+void ah_pow64_128(uint64_t p, int skew, uint64_t *out2) { pg::pow64_128_mod(p, out2[0], out2[1], skew); }
+
+uint64_t ah_neg_inv64(uint64_t p) { return pg::neg_inv64(p); }
+
 void ah_udiv2f(uint32_t n1, uint32_t n2, uint32_t d, int skew, uint32_t *out2) {
     pg::udiv2f_32(n1, n2, d, out2[0], out2[1], skew);
 }

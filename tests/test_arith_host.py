@@ -516,6 +516,25 @@ def test_udiv2_64_shared_reciprocal_exact(ah):
             assert (out[0], out[1]) == (n1 // d, n2 // d), (n1, n2, d, skew)
 
 
+def test_pow64_128_and_inverse_without_division(ah):
+    """2^64 and 2^128 mod p (eight single-precision reduction steps, the
+    reciprocal skewed up to 2 ulps) and -p^-1 mod 2^64 for odd p up to 2^46,
+    the 64-bit primes' K mod p set-up."""
+    ah.ah_pow64_128.restype = None
+    ah.ah_pow64_128.argtypes = [ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ctypes.c_uint64)]
+    ah.ah_neg_inv64.restype = ctypes.c_uint64
+    ah.ah_neg_inv64.argtypes = [ctypes.c_uint64]
+    rng = random.Random(31)
+    ps = [3, 5, 65537, (1 << 31) - 1, (1 << 32) + 15, (1 << 46) - 1, (1 << 45) + 1]
+    ps += [rng.randrange(3, 1 << b) | 1 for b in (8, 17, 24, 32, 33, 40, 46) for _ in range(500)]
+    out = (ctypes.c_uint64 * 2)()
+    for p in ps:
+        for skew in (-2, 0, 2):
+            ah.ah_pow64_128(p, skew, out)
+            assert (out[0], out[1]) == (pow(2, 64, p), pow(2, 128, p)), (p, skew)
+        assert (ah.ah_neg_inv64(p) * p) % (1 << 64) == (1 << 64) - 1, p
+
+
 def test_pow32_mod_without_division(ah):
     """2^32 mod p of the K mod p setup (reciprocal and two subtractions) for
     odd p across the three ranges and their edges, reciprocal skewed up to
