@@ -584,6 +584,7 @@ struct pgs_batch {
     std::vector<Chunk *> chunks;
     DevBuf d_jobs, counters, heavy;
     size_t smem = 0;
+    bool all_shared = false;  // every job's masks fit shared memory
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaEvent_t t0 = nullptr, t1 = nullptr, fork = nullptr, setup_done = nullptr;
@@ -684,6 +685,7 @@ int plan_batch(pgs_ctx *ctx, pgs_batch *b, cudaStream_t s) {
     // jobs and items
     std::vector<pg::LargeJob> lj(n);
     size_t smem = 0;
+    bool all_shared = true;
     for (int j = 0; j < n; j++) {
         pgs_prepared *pr = b->jobs[j];
         lj[j].job = job_dev(pr);
@@ -693,8 +695,10 @@ int plan_batch(pgs_ctx *ctx, pgs_batch *b, cudaStream_t s) {
         const size_t mb = 8ull * ((lj[j].job.walk.jmax + 31) / 32 + (lj[j].job.walk.w + 31) / 32);
         lj[j].masks_in_shared = mb <= 96 * 1024;
         if (lj[j].masks_in_shared) smem = std::max(smem, mb);
+        all_shared = all_shared && lj[j].masks_in_shared;
     }
     b->smem = smem;
+    b->all_shared = all_shared;
     // chunks: jobs by rows work, longest first, cut where the cumulative
     // large-prime work (primes to the limit) passes each quarter
     std::vector<int> order(n);
@@ -844,10 +848,10 @@ int launch_batch(pgs_ctx *ctx, pgs_batch *b) {
                                pg::heavy_capacity()};
     for (pgs_batch::Chunk *ch : b->chunks) {
         CK(pg::large_multi(b->d_jobs.as<pg::LargeJob>(), ch->items32.as<pg::LargeItem>(), ch->n32, ch->tiles32,
-                           b->smem, false, scr, s0));
+                           b->smem, false, scr, s0, b->all_shared));
         if (ch->tiles64)
             CK(pg::large_multi(b->d_jobs.as<pg::LargeJob>(), ch->items64.as<pg::LargeItem>(), ch->n64, ch->tiles64,
-                               b->smem, true, scr, s0));
+                               b->smem, true, scr, s0, b->all_shared));
         CK(cudaEventRecord(ch->done, s0));
         for (int j : ch->jobs) {
             const cudaStream_t s = ctx->lanes[b->lane_of[j]]->stream;

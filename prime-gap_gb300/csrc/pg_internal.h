@@ -173,8 +173,9 @@ struct LargeItem {
 constexpr uint32_t kLargeTile = 256;
 // Both kernels (tiles, then the heavy primes of every job) on one stream;
 // smem = the largest job's mask bytes among those with masks_in_shared.
+// all_shared: every job's masks fit the launch's shared memory.
 cudaError_t large_multi(const LargeJob *d_jobs, const LargeItem *d_items, uint32_t n_items, uint32_t n_tiles,
-                        size_t smem, bool wide, LargeScratch scratch, cudaStream_t stream);
+                        size_t smem, bool wide, LargeScratch scratch, cudaStream_t stream, bool all_shared);
 
 // ---- rows: small primes, merge, extract, format (pg_rows.cu) -----------------
 

@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(kLargeThreads)
 // into shared memory when the tile's job differs from their last one, and
 // run the group as the single-job kernel does, with the job's walk started
 // from K' mod p.  Every item has the same prime width (T).
-template <typename T>
+template <typename T, bool kAllShared>
 __global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
     large_multi_kernel(const LargeJob *__restrict__ jobs, const LargeItem *__restrict__ items, uint32_t n_items,
                        uint32_t n_tiles, unsigned long long *tile_ctr, HeavyPrime *heavy,
@@ -323,7 +323,7 @@ __global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
             const LargeJob &lj = jobs[it.job];
             if (threadIdx.x == 0) s_job = lj.job;
             const uint32_t mwords = (uint32_t)((lj.job.walk.jmax + 31) / 32), ywords = (lj.job.walk.w + 31) / 32;
-            if (lj.masks_in_shared) {
+            if (kAllShared || lj.masks_in_shared) {
                 for (uint32_t i = threadIdx.x; i < mwords; i += blockDim.x) s_masks[i] = lj.mmask[i];
                 for (uint32_t i = threadIdx.x; i < ywords; i += blockDim.x) s_masks[mwords + i] = lj.ymask[i];
                 if (threadIdx.x == 0) s_mm = s_masks, s_ym = s_masks + mwords;
@@ -333,14 +333,20 @@ __global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
             loaded = it.job;
             __syncthreads();
         }
-        const Marker mark{s_job, s_mm, s_ym};
         const uint32_t i = (t - it.tile0) * kLargeThreads + threadIdx.x;
         const bool has = i < it.count;
         const T *a = (const T *)it.a, *b = (const T *)it.b;
         const T p = has ? (T)(it.base + it.off[i]) : (T)0;
         T step = 0, t0 = 0;
         if (has) walk_inputs<T, kInKprime>(s_job, nullptr, 0, p, a, b, i, step, t0);
-        large_group<T>(s_job, mark, sl, has, p, step, t0, heavy, heavy_count, heavy_cap, it.job);
+        if constexpr (kAllShared) {
+            // every job's masks in shared memory: shared loads (see load_masks)
+            const Marker mark{s_job, s_masks, s_masks + (uint32_t)((s_job.walk.jmax + 31) / 32)};
+            large_group<T>(s_job, mark, sl, has, p, step, t0, heavy, heavy_count, heavy_cap, it.job);
+        } else {
+            const Marker mark{s_job, s_mm, s_ym};
+            large_group<T>(s_job, mark, sl, has, p, step, t0, heavy, heavy_count, heavy_cap, it.job);
+        }
     }
 }
 
@@ -600,7 +606,7 @@ cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off
 }
 
 cudaError_t large_multi(const LargeJob *d_jobs, const LargeItem *d_items, uint32_t n_items, uint32_t n_tiles,
-                        size_t smem, bool wide, LargeScratch scratch, cudaStream_t stream) {
+                        size_t smem, bool wide, LargeScratch scratch, cudaStream_t stream, bool all_shared) {
     if (n_tiles == 0) return cudaSuccess;
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
@@ -618,7 +624,10 @@ cudaError_t large_multi(const LargeJob *d_jobs, const LargeItem *d_items, uint32
                                                                   scratch.heavy, heavy_count, scratch.heavy_cap);
         return cudaGetLastError();
     };
-    e = wide ? launch(large_multi_kernel<uint64_t>) : launch(large_multi_kernel<uint32_t>);
+    if (all_shared)
+        e = wide ? launch(large_multi_kernel<uint64_t, true>) : launch(large_multi_kernel<uint32_t, true>);
+    else
+        e = wide ? launch(large_multi_kernel<uint64_t, false>) : launch(large_multi_kernel<uint32_t, false>);
     if (e) return e;
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, heavy_multi_kernel, kLargeThreads, 0))) return e;
     if (per_sm < 1) per_sm = 1;
