@@ -245,7 +245,7 @@ __device__ __forceinline__ void large_group(const JobDev &job, const Marker &mar
 }
 
 template <typename T, int kIn, bool kShared>
-__global__ void __launch_bounds__(kLargeThreads)
+__global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
     large_kernel(const __grid_constant__ KLimbs<kIn >= kInLimbsLsb ? kParamLimbs : 1> kl, int nlimbs,
                  JobDev job, uint64_t base, const uint32_t *__restrict__ off,
                  const unsigned long long *range, uint64_t max_count, const T *__restrict__ a_in,
