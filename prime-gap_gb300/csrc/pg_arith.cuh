@@ -941,9 +941,10 @@ PG_HD ThreeGap<uint32_t> gap32(const ThreeGap<T> &g, uint32_t mi_hi) {
 }
 
 // rotation_walk32: up to `steps` rotation steps from (mi, y) while
-// mi < mi_hi, calling emit(mi, y, y < w) at every step (the emitter acts on
-// hits; calling it unconditionally keeps a warp's lanes on one path).  A step
-// wraps when y + up >= C, i.e. y >= dn.
+// mi < mi_hi, calling emit(mi, y, y < w) at every step.  A step wraps when
+// y + up >= C, i.e. y >= dn.  The definition of a walk's steps; the kernels
+// run return_walk32 below, which visits the same hits and skips the misses
+// (the host tests check the two against each other).
 template <typename Emit>
 PG_HD void rotation_walk32(uint32_t mi, uint32_t y, const ThreeGap<uint32_t> &g, uint32_t w,
                            uint32_t mi_hi, uint32_t steps, Emit &emit) {

@@ -105,14 +105,14 @@ size_t ah_hits_items(uint64_t M, uint32_t max_mi, uint32_t SL, uint64_t p, uint6
         // the kernel's 32-bit walk forms, step costs clamped to max_mi
         const pg::ThreeGap<uint32_t> g = pg::gap32(e.g, max_mi);
         if (bound <= direct) {
-            pg::rotation_walk32((uint32_t)e.t, (uint32_t)e.y, g, (uint32_t)w, max_mi, (uint32_t)bound, c);
+            pg::return_walk32((uint32_t)e.t, (uint32_t)e.y, g, (uint32_t)w, max_mi, (uint32_t)bound, c);
             return;
         }
         uint64_t items = (bound + item_steps - 1) / item_steps;
         for (uint64_t it = 0; it < items; it++) {
             uint32_t y, mi;
             pg::rotation_at32((uint32_t)e.t, (uint32_t)e.y, g, (uint32_t)(it * item_steps), max_mi, y, mi);
-            pg::rotation_walk32(mi, y, g, (uint32_t)w, max_mi, item_steps, c);
+            pg::return_walk32(mi, y, g, (uint32_t)w, max_mi, item_steps, c);
         }
     };
     if (p < 0xFFFFFFFFull) {
