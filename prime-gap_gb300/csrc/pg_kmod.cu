@@ -2,7 +2,7 @@
 // K = P#/d against 32-bit and 64-bit primes by Montgomery multiplication.
 //
 // Replaces mpz_fdiv_ui(K, prime) at combined_sieve.cpp:1497 and 1856 (and the
-// mpz_mod_ui of 1674).  One thread per prime (four interleaved chains per
+// mpz_mod_ui of 1674).  One thread per prime (eight interleaved chains per
 // thread for 32-bit primes) reduces K's limbs: most significant first,
 // u <- REDC(u * R^2 + limb), for short K; least significant first,
 // W <- REDC(W + limb) and one multiply by R^(n+1) mod p at the end, for long
@@ -25,7 +25,8 @@ namespace {
 
 constexpr int kKmodThreads = 256;
 constexpr int kMaxSharedLimbs = 12288;  // 48 KiB
-constexpr int kPrimesPerThread = 4;     // 32-bit primes
+constexpr int kPrimesPerThread = 8;     // 32-bit primes
+constexpr int kChainPrimesPerThread = 4;  // 32-bit primes of the chained K' mod p (batch)
 constexpr int kLsbMinLimbs = 32;        // 32-bit primes: LSB chain from 32 limbs
 constexpr int kLsbMinLimbsWide = 24;    // 64-bit primes: from 12 words
 
@@ -120,12 +121,13 @@ __global__ void __launch_bounds__(kKmodThreads)
     const uint32_t *so = s_limbs + nlimbs;
     if (!kWide) {
         uint32_t *ro = (uint32_t *)r_out;
-        const uint64_t idx0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kPrimesPerThread;
+        const uint64_t idx0 = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) * kChainPrimesPerThread;
         if (idx0 >= n) return;
-        uint32_t p[kPrimesPerThread], pinv[kPrimesPerThread], r2[kPrimesPerThread], acc[kPrimesPerThread];
+        uint32_t p[kChainPrimesPerThread], pinv[kChainPrimesPerThread], r2[kChainPrimesPerThread],
+            acc[kChainPrimesPerThread];
         bool lazy = true;
 #pragma unroll
-        for (int k = 0; k < kPrimesPerThread; k++) {
+        for (int k = 0; k < kChainPrimesPerThread; k++) {
             p[k] = idx0 + k < n ? (uint32_t)(base + off[idx0 + k]) : 3u;  // pad with a prime
             pinv[k] = neg_inv32(p[k]);
             r2[k] = r2_from_r1(pow32_mod(p[k]), p[k], pinv[k]);
@@ -133,30 +135,30 @@ __global__ void __launch_bounds__(kKmodThreads)
             lazy = lazy && p[k] < 0x80000000u;
         }
         for (int g = 0; g < G; g++) {
-            uint32_t u[kPrimesPerThread];
+            uint32_t u[kChainPrimesPerThread];
 #pragma unroll
-            for (int k = 0; k < kPrimesPerThread; k++) u[k] = 0;
+            for (int k = 0; k < kChainPrimesPerThread; k++) u[k] = 0;
             const int lo = (int)so[g], hi = (int)so[g + 1];
             if (lazy) {
                 for (int i = hi - 1; i >= lo; i--) {
                     const uint32_t l = s_limbs[i];
 #pragma unroll
-                    for (int k = 0; k < kPrimesPerThread; k++)
+                    for (int k = 0; k < kChainPrimesPerThread; k++)
                         u[k] = redc32_lazy((uint64_t)u[k] * r2[k] + l, p[k], pinv[k]);
                 }
 #pragma unroll
-                for (int k = 0; k < kPrimesPerThread; k++)
+                for (int k = 0; k < kChainPrimesPerThread; k++)
                     if (u[k] >= p[k]) u[k] -= p[k];
             } else {
                 for (int i = hi - 1; i >= lo; i--) {
                     const uint32_t l = s_limbs[i];
 #pragma unroll
-                    for (int k = 0; k < kPrimesPerThread; k++)
+                    for (int k = 0; k < kChainPrimesPerThread; k++)
                         u[k] = redc32((uint64_t)u[k] * r2[k] + l, p[k], pinv[k]);
                 }
             }
 #pragma unroll
-            for (int k = 0; k < kPrimesPerThread; k++) {
+            for (int k = 0; k < kChainPrimesPerThread; k++) {
                 const uint32_t sg = redc32((uint64_t)u[k] * r2[k], p[k], pinv[k]);       // S_g mod p
                 const uint32_t r = g ? redc32((uint64_t)acc[k] * sg, p[k], pinv[k]) : sg;  // K'_g mod p
                 if (idx0 + k < n) ro[(uint64_t)g * n + idx0 + k] = r;
@@ -164,7 +166,7 @@ __global__ void __launch_bounds__(kKmodThreads)
             }
         }
 #pragma unroll
-        for (int k = 0; k < kPrimesPerThread; k++)
+        for (int k = 0; k < kChainPrimesPerThread; k++)
             if (idx0 + k < n) ((uint32_t *)r2_out)[idx0 + k] = r2[k];
     } else {
         uint64_t *ro = (uint64_t *)r_out;
@@ -263,7 +265,7 @@ cudaError_t kmod_chain(const uint32_t *d_seg_limbs, const uint32_t *d_seg_off, i
                        const uint32_t *d_off, uint64_t n, void *d_r, void *d_r2, bool wide, cudaStream_t stream,
                        const uint32_t *h_seg_limbs, const uint32_t *h_seg_off) {
     if (n == 0 || G == 0) return cudaSuccess;
-    const uint64_t per_thread = wide ? 1 : kPrimesPerThread;
+    const uint64_t per_thread = wide ? 1 : kChainPrimesPerThread;
     const uint64_t threads = (n + per_thread - 1) / per_thread;
     const unsigned blocks = (unsigned)((threads + kKmodThreads - 1) / kKmodThreads);
     if (nlimbs + G + 1 > kMaxSharedLimbs) return cudaErrorInvalidValue;
