@@ -92,6 +92,17 @@ void *pgs_get_stream(pgs_ctx *ctx);
  * parameters.  Free with pgs_result_free.
  */
 int pgs_method2(pgs_ctx *ctx, const pgs_job *job, pgs_result *out);
+
+/*
+ * The same job by the per-m path (replaces combined_sieve --method1:
+ * prime_gap_search and save_unknowns_method1, combined_sieve.cpp:383-751).
+ * The reference files every large prime under the next m it divides and
+ * sieves m by m; here the large-prime phase runs twice, counting and then
+ * filing each surviving (m, X) under its m, and each m's marks come from its
+ * own bucket.  The bytes equal pgs_method2's (the reference checks its two
+ * methods against each other, misc/tests.sh:62-67); slower, a cross-check.
+ */
+int pgs_method1(pgs_ctx *ctx, const pgs_job *job, pgs_result *out);
 void pgs_result_free(pgs_result *r);
 
 /*

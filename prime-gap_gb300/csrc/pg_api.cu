@@ -325,7 +325,7 @@ int text_pipeline(pgs_ctx *ctx, pgs_prepared *pr, const pg::RowsDev &rd, uint32_
 
 // One run of a prepared job (context locked).  With `sink`, the rows and
 // text are pipelined with their copy to the host (text_pipeline).
-int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
+int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, bool per_m = false) {
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     HostJob &h = pr->hj;
@@ -381,34 +381,75 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink) {
     // K mod p of a window's primes inside the large-prime kernel: bit 1 of
     // the form for windows of 32-bit primes, bit 2 for 64-bit primes
     const bool limbs_fit = h.klimbs.size() <= (size_t)pg::kParamLimbs;
-    // large primes, window by window
-    for (size_t w = 0; w < pr->windows.size(); w++) {
-        const Window &win = pr->windows[w];
-        unsigned long long *rng = misc + 3 + 2 * w, *cnt = rng + 1;
-        int e_a, e_b, e_c, e_d;
-        CK(mark(e_a));
-        CK(pg::sieve_window(ctx->base, win.lo, win.hi, ctx->win_off.as<uint32_t>(), win.bound, cnt, s));
-        const bool fuse = limbs_fit && (pr->tune.large_form & (win.wide ? 4u : 2u));
-        CK(mark(e_b));
-        if (!fuse)
-            CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
-                               ctx->win_off.as<uint32_t>(), rng, win.bound, &h.walk, ctx->win_r.p,
-                               ctx->win_t0.p, win.wide, s, (int)pr->tune.kmod_lsb_limbs, h.klimbs.data()));
-        CK(mark(e_c));
-        CK(pg::large_window(job, win.lo, ctx->win_off.as<uint32_t>(), rng, win.bound, ctx->win_r.p,
-                            ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint2>(),
-                            pr->ymask.as<uint2>(),
-                            pg::LargeScratch{ctx->large_ctr.as<unsigned long long>(),
-                                             ctx->heavy.as<pg::HeavyPrime>(), pg::heavy_capacity(),
-                                             ctx->walks.as<pg::WalkEntry>(),
-                                             ctx->walks.p ? pg::walk_capacity() : 0u},
-                            s, fuse ? h.klimbs.data() : nullptr, (int)h.klimbs.size(),
-                            pg::kmod_lsb((int)h.klimbs.size(), win.wide, (int)pr->tune.kmod_lsb_limbs)));
-        CK(mark(e_d));
-        span(PGS_STAGE_PRIMES, e_a, e_b);
-        span(PGS_STAGE_KMOD, e_b, e_c);
-        span(PGS_STAGE_LARGE, e_c, e_d);
-        pr->launches += fuse ? 3 : 4;
+    // large primes, window by window, marking through the job descriptor jd
+    auto large_phase = [&](const pg::JobDev &jd) -> cudaError_t {
+        for (size_t w = 0; w < pr->windows.size(); w++) {
+            const Window &win = pr->windows[w];
+            unsigned long long *rng = misc + 3 + 2 * w, *cnt = rng + 1;
+            int e_a, e_b, e_c, e_d;
+            cudaError_t e;
+            if ((e = mark(e_a))) return e;
+            if ((e = pg::sieve_window(ctx->base, win.lo, win.hi, ctx->win_off.as<uint32_t>(), win.bound, cnt, s)))
+                return e;
+            const bool fuse = limbs_fit && (pr->tune.large_form & (win.wide ? 4u : 2u));
+            if ((e = mark(e_b))) return e;
+            if (!fuse &&
+                (e = pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
+                                     ctx->win_off.as<uint32_t>(), rng, win.bound, &h.walk, ctx->win_r.p,
+                                     ctx->win_t0.p, win.wide, s, (int)pr->tune.kmod_lsb_limbs, h.klimbs.data())))
+                return e;
+            if ((e = mark(e_c))) return e;
+            e = pg::large_window(jd, win.lo, ctx->win_off.as<uint32_t>(), rng, win.bound, ctx->win_r.p,
+                                 ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint2>(), pr->ymask.as<uint2>(),
+                                 pg::LargeScratch{ctx->large_ctr.as<unsigned long long>(),
+                                                  ctx->heavy.as<pg::HeavyPrime>(), pg::heavy_capacity(),
+                                                  ctx->walks.as<pg::WalkEntry>(),
+                                                  ctx->walks.p ? pg::walk_capacity() : 0u},
+                                 s, fuse ? h.klimbs.data() : nullptr, (int)h.klimbs.size(),
+                                 pg::kmod_lsb((int)h.klimbs.size(), win.wide, (int)pr->tune.kmod_lsb_limbs));
+            if (e) return e;
+            if ((e = mark(e_d))) return e;
+            span(PGS_STAGE_PRIMES, e_a, e_b);
+            span(PGS_STAGE_KMOD, e_b, e_c);
+            span(PGS_STAGE_LARGE, e_c, e_d);
+            pr->launches += fuse ? 3 : 4;
+        }
+        return cudaSuccess;
+    };
+    if (!per_m) {
+        CK(large_phase(job));
+    } else {
+        // The per-m path (method1, combined_sieve.cpp:409-751): the reference
+        // keeps every large prime in a queue under the next m it divides and
+        // sieves m by m.  Here the phase runs twice, first counting each
+        // row's survivors, then, at offsets from their prefix sum, filing
+        // each survivor's column under its row; each row's marks then come
+        // from its own bucket.  Same bytes as method2.
+        unsigned long long *rc_ = nullptr, *ro = nullptr;
+        CK(pr->row_count.ensure(std::max<uint64_t>(rows, 1) * 8));
+        CK(pr->row_off.ensure((rows + 1) * 8));
+        rc_ = pr->row_count.as<unsigned long long>();
+        ro = pr->row_off.as<unsigned long long>();
+        pg::JobDev jd = job;
+        CK(cudaMemsetAsync(rc_, 0, rows * 8, s));
+        jd.mark_mode = pg::kMarkCount;
+        jd.row_count = rc_;
+        CK(large_phase(jd));
+        CK(pg::scan_u64((const uint64_t *)rc_, (uint64_t *)ro, (uint64_t *)(ro + rows), rows,
+                        pr->scan_tmp.as<uint64_t>(), s));
+        uint64_t total = 0;
+        CK(cudaMemcpyAsync(&total, ro + rows, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        CK(pr->bucket.ensure(std::max<uint64_t>(total, 1) * 4));
+        CK(cudaMemsetAsync(rc_, 0, rows * 8, s));
+        // the windows' prime counts accumulate: start them again
+        CK(cudaMemsetAsync(misc + 3, 0, 2 * pr->windows.size() * 8, s));
+        jd.mark_mode = pg::kMarkBucket;
+        jd.row_off = ro;
+        jd.bucket = pr->bucket.as<uint32_t>();
+        CK(large_phase(jd));
+        CK(pg::bucket_apply(jd, ro + rows, s));
+        pr->launches += 2;
     }
     // rows, text
     CK(mark(a));
@@ -519,6 +560,24 @@ int pgs_method2(pgs_ctx *ctx, const pgs_job *job, pgs_result *out) {
         std::lock_guard<std::mutex> g(ctx->mu);
         HostText ht;
         rc = run_job(ctx, pr, 1, &ht);
+        if (rc == PGS_OK) {
+            rc = fetch_job(ctx, pr, ctx->stream, out, &ht);
+            if (rc != PGS_OK) pinned_pool().put(ht.text, ht.cap);
+        }
+    }
+    pgs_prepared_free(pr);
+    return rc;
+}
+
+int pgs_method1(pgs_ctx *ctx, const pgs_job *job, pgs_result *out) {
+    if (!ctx || !job || !out) return PGS_EINVAL;
+    pgs_prepared *pr = nullptr;
+    int rc = pgs_prepare(ctx, job, &pr);
+    if (rc) return rc;
+    {
+        std::lock_guard<std::mutex> g(ctx->mu);
+        HostText ht;
+        rc = run_job(ctx, pr, 1, &ht, true);
         if (rc == PGS_OK) {
             rc = fetch_job(ctx, pr, ctx->stream, out, &ht);
             if (rc != PGS_OK) pinned_pool().put(ht.text, ht.cap);

@@ -230,15 +230,16 @@ struct pgs_prepared {
     uint64_t win_bound = 0;
     pgh::DevBuf klimbs, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0, mmask, ymask;
     pgh::DevBuf lists, counts, row_bytes, offsets, scan_tmp, misc, text;
+    pgh::DevBuf row_count, row_off, bucket;  // the per-m path (method1)
     std::vector<cudaEvent_t> events;
     std::vector<std::pair<int, std::pair<int, int>>> spans;  // stage, (ev a, ev b)
     double ms_setup = 0;
     uint64_t launches = 0;
     bool ran = false;
     std::vector<pgh::DevBuf *> all() {
-        return {&klimbs, &valid_mi, &dist,  &dq,       &dr,      &comp,     &sp,
-                &sr,     &sp_t0,    &lists, &counts,   &row_bytes, &offsets, &scan_tmp,
-                &misc,   &text,     &mmask, &ymask};
+        return {&klimbs, &valid_mi, &dist,  &dq,       &dr,        &comp,     &sp,
+                &sr,     &sp_t0,    &lists, &counts,   &row_bytes, &offsets,  &scan_tmp,
+                &misc,   &text,     &mmask, &ymask,    &row_count, &row_off,  &bucket};
     }
     char *stage = nullptr;  // pinned staging block of the table uploads
     size_t stage_cap = 0;

@@ -117,7 +117,21 @@ struct JobDev {
     // with a walk list; bits 1 and 2 = K mod p inside the large-prime kernel
     // for windows of 32-bit and of 64-bit primes
     uint32_t large_form;
+    // Where a large-prime survivor (row, col) goes.  kMarkComp: OR into comp
+    // (method2).  The per-m path (method1) runs the phase twice: kMarkCount
+    // counts each row's survivors in row_count, kMarkBucket appends col to
+    // the row's bucket at bucket[row_off[row] + k], k from row_count.
+    uint32_t mark_mode;
+    unsigned long long *row_count;
+    const unsigned long long *row_off;
+    uint32_t *bucket;
 };
+constexpr uint32_t kMarkComp = 0, kMarkCount = 1, kMarkBucket = 2;
+
+// The per-m path's rows: each row's large-prime marks from its bucket of
+// survivor columns (bucket[row_off[r] .. row_off[r + 1]) for row r, the last
+// end in *total) into its comp row, built in shared memory.
+cudaError_t bucket_apply(const JobDev &job, const unsigned long long *total, cudaStream_t stream);
 
 struct HeavyPrime;
 // Device scratch of the large-prime phase: two counters (group claims, heavy

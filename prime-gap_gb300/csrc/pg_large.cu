@@ -61,7 +61,14 @@ struct Marker {
             const uint32_t row = mv.y + __popc(mv.x & ((1u << (j & 31)) - 1u));
             const uint32_t ry = yv.y + __popc(yv.x & ((1u << (yi & 31)) - 1u));
             const uint32_t col = yi >= job.y_lo ? ry - job.half_cols : job.side_pad + job.half_cols - 1 - ry;
-            atomicOr(&job.comp[(uint64_t)row * job.pitch + (col >> 5)], 1u << (col & 31));
+            if (job.mark_mode == kMarkComp) {
+                atomicOr(&job.comp[(uint64_t)row * job.pitch + (col >> 5)], 1u << (col & 31));
+            } else if (job.mark_mode == kMarkCount) {
+                atomicAdd(&job.row_count[row], 1ull);
+            } else {
+                const unsigned long long k = atomicAdd(&job.row_count[row], 1ull);
+                job.bucket[job.row_off[row] + k] = col;
+            }
         }
     }
 };
@@ -504,6 +511,40 @@ __global__ void __launch_bounds__(kLargeThreads)
 
 uint32_t heavy_capacity() { return 1u << 20; }
 uint32_t walk_capacity() { return 1u << 24; }
+
+namespace {
+
+// One CTA per row of the per-m path: the row's survivor columns, in any
+// order and with repeats, set bits of its comp row in shared memory, which
+// then replaces the (zeroed) comp row.
+constexpr int kApplyThreads = 256;
+__global__ void __launch_bounds__(kApplyThreads)
+    bucket_apply_kernel(JobDev job, const unsigned long long *__restrict__ total) {
+    extern __shared__ uint32_t s_row[];
+    const uint32_t row = blockIdx.x;
+    for (uint32_t w = threadIdx.x; w < job.pitch; w += blockDim.x) s_row[w] = 0;
+    __syncthreads();
+    const unsigned long long b0 = job.row_off[row];
+    const unsigned long long b1 = row + 1 < job.rows ? job.row_off[row + 1] : *total;
+    for (unsigned long long k = b0 + threadIdx.x; k < b1; k += blockDim.x) {
+        const uint32_t col = job.bucket[k];
+        atomicOr(&s_row[col >> 5], 1u << (col & 31));
+    }
+    __syncthreads();
+    uint32_t *dst = job.comp + (uint64_t)row * job.pitch;
+    for (uint32_t w = threadIdx.x; w < job.pitch; w += blockDim.x) dst[w] = s_row[w];
+}
+
+}  // namespace
+
+cudaError_t bucket_apply(const JobDev &job, const unsigned long long *total, cudaStream_t stream) {
+    if (job.rows == 0) return cudaSuccess;
+    const size_t smem = (size_t)job.pitch * sizeof(uint32_t);
+    cudaError_t e = cudaFuncSetAttribute(bucket_apply_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e) return e;
+    bucket_apply_kernel<<<job.rows, kApplyThreads, smem, stream>>>(job, total);
+    return cudaGetLastError();
+}
 
 cudaError_t large_window(const JobDev &job, uint64_t base, const uint32_t *d_off,
                          const unsigned long long *d_range, uint64_t max_count, const void *d_a,

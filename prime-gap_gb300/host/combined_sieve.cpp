@@ -9,8 +9,10 @@
 // (combined_sieve.cpp:347-380).  Exit codes: 0 ok, 1 invalid arguments or
 // failed run (the reference's exit(1)).
 //
-// --method1 produces the same bytes (the reference checks the two methods
-// against each other, misc/tests.sh:62-67) under the .m1.txt name.
+// --method1 runs the per-m path (pgs_method1: each m's large-prime marks
+// from its own bucket, as the reference's prime_gap_search takes them from
+// its next-m queue) and writes the same bytes (the reference checks the two
+// methods against each other, misc/tests.sh:62-67) under the .m1.txt name.
 // set_defaults (combined_sieve.cpp:160-344) runs as in the reference: the d
 // optimizer for d % 4 == 0 (count_K_d statistics, gap_common.cpp:455-571,
 // then exit 0), the automatic sieve length and the automatic max_prime.
@@ -295,7 +297,7 @@ int main(int argc, char **argv) {
     pgs_job job{c.p, c.d, c.mstart, c.minc, c.sieve_length, c.max_prime,
                 c.compression == 3 ? 0 : c.compression, 0};
     pgs_result res;
-    rc = pgs_method2(ctx, &job, &res);
+    rc = c.method1 ? pgs_method1(ctx, &job, &res) : pgs_method2(ctx, &job, &res);
     if (rc != PGS_OK) {
         printf("combined_sieve failed (%d): %s\n", rc, pgs_last_error(ctx));
         pgs_destroy(ctx);

@@ -194,6 +194,7 @@ _SIGNATURES = {
     "pgs_set_stream": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
     "pgs_get_stream": (ctypes.c_void_p, [ctypes.c_void_p]),
     "pgs_method2": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.POINTER(Result)]),
+    "pgs_method1": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.POINTER(Result)]),
     "pgs_result_free": (None, [ctypes.POINTER(Result)]),
     "pgs_prepare": (ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(Job), ctypes.POINTER(ctypes.c_void_p)]),
     "pgs_run": (ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int]),
@@ -390,6 +391,19 @@ class Sieve:
         """Unknowns file bytes for one job (prime_gap_parallel + save)."""
         res = Result()
         self._check(self.lib.pgs_method2(self.h, ctypes.byref(job.c()), ctypes.byref(res)))
+        try:
+            data = ctypes.string_at(res.text, res.text_len)
+            if stats is not None:
+                stats.update(_result_stats(res))
+        finally:
+            self.lib.pgs_result_free(ctypes.byref(res))
+        return data
+
+    def method1(self, job: JobSpec, stats: dict | None = None) -> bytes:
+        """The same bytes by the per-m path (pgs_method1, the reference's
+        --method1 cross-check)."""
+        res = Result()
+        self._check(self.lib.pgs_method1(self.h, ctypes.byref(job.c()), ctypes.byref(res)))
         try:
             data = ctypes.string_at(res.text, res.text_len)
             if stats is not None:
