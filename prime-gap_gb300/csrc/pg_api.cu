@@ -425,30 +425,29 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
         // row's survivors, then, at offsets from their prefix sum, filing
         // each survivor's column under its row; each row's marks then come
         // from its own bucket.  Same bytes as method2.
-        unsigned long long *rc_ = nullptr, *ro = nullptr;
         CK(pr->row_count.ensure(std::max<uint64_t>(rows, 1) * 8));
         CK(pr->row_off.ensure((rows + 1) * 8));
-        rc_ = pr->row_count.as<unsigned long long>();
-        ro = pr->row_off.as<unsigned long long>();
+        unsigned long long *counts = pr->row_count.as<unsigned long long>();
+        unsigned long long *offs = pr->row_off.as<unsigned long long>();  // rows + 1: the total last
         pg::JobDev jd = job;
-        CK(cudaMemsetAsync(rc_, 0, rows * 8, s));
+        CK(cudaMemsetAsync(counts, 0, rows * 8, s));
         jd.mark_mode = pg::kMarkCount;
-        jd.row_count = rc_;
+        jd.row_count = counts;
         CK(large_phase(jd));
-        CK(pg::scan_u64((const uint64_t *)rc_, (uint64_t *)ro, (uint64_t *)(ro + rows), rows,
+        CK(pg::scan_u64((const uint64_t *)counts, (uint64_t *)offs, (uint64_t *)(offs + rows), rows,
                         pr->scan_tmp.as<uint64_t>(), s));
         uint64_t total = 0;
-        CK(cudaMemcpyAsync(&total, ro + rows, 8, cudaMemcpyDeviceToHost, s));
+        CK(cudaMemcpyAsync(&total, offs + rows, 8, cudaMemcpyDeviceToHost, s));
         CK(cudaStreamSynchronize(s));
         CK(pr->bucket.ensure(std::max<uint64_t>(total, 1) * 4));
-        CK(cudaMemsetAsync(rc_, 0, rows * 8, s));
+        CK(cudaMemsetAsync(counts, 0, rows * 8, s));  // now the fill position of each bucket
         // the windows' prime counts accumulate: start them again
         CK(cudaMemsetAsync(misc + 3, 0, 2 * pr->windows.size() * 8, s));
         jd.mark_mode = pg::kMarkBucket;
-        jd.row_off = ro;
+        jd.row_off = offs;
         jd.bucket = pr->bucket.as<uint32_t>();
         CK(large_phase(jd));
-        CK(pg::bucket_apply(jd, ro + rows, s));
+        CK(pg::bucket_apply(jd, offs + rows, s));
         pr->launches += 2;
     }
     // rows, text
