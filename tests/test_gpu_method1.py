@@ -58,3 +58,16 @@ def test_cli_method1_file(built, goldens, tmp_path):
     assert files == ["907_2190_1_200_s11000_l100M.m1.txt"], p.stdout
     data = (tmp_path / "unknowns" / files[0]).read_bytes()
     assert hashlib.md5(data).hexdigest() == goldens["fn1"]["md5"]
+
+
+@pytest.mark.parametrize("form", [1, 6, 7])
+def test_method1_other_large_forms(goldens, form):
+    """The per-m path through the other large-prime kernel forms (warps alone
+    with a walk list; K mod p inside the kernel), config 2 and a job past
+    2^32, against the reference's md5s."""
+    g64 = json.loads(MIX.read_text())["w64_503_210"]
+    with pgsieve.Sieve(0, load_tuning=False) as s:
+        for g in (goldens["config2"], g64):
+            job = _spec(g)
+            s.tuning_set(job, {"large_form": form})
+            assert hashlib.md5(s.method1(job)).hexdigest() == g["md5"], form
