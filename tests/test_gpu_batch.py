@@ -44,6 +44,25 @@ def test_batch_goldens(sieve, goldens):
             assert hashlib.md5(b.fetch(i)).hexdigest() == goldens[n]["md5"], n
 
 
+def test_batch_with_masks_in_global_memory(sieve, goldens):
+    """A batch where one job's masks do not fit the tile kernel's shared
+    memory (400,000 m of d = 105: the masks are read from global memory for
+    every job of the launch) next to golden jobs: every output equals the
+    same job alone on the plain path (itself checked against the oracle) or
+    the reference's md5."""
+    big = pgsieve.JobSpec(89, 105, 1000003, 400_000, 1000, 2_000_000, 1)
+    names = ["fn1", "small_d7_odd", "config1"]
+    jobs = [big] + [pgsieve.JobSpec(g["p"], g["d"], g["mstart"], g["minc"], g["sieve_length"], g["max_prime"],
+                                    g["compression"]) for g in (goldens[n] for n in names)]
+    want_big = hashlib.md5(sieve.method2(big)).hexdigest()
+    with sieve.batch(jobs, lanes=4) as b:
+        for graph in (False, True):
+            b.run(graph=graph)
+            assert hashlib.md5(b.fetch(0)).hexdigest() == want_big, graph
+            for i, n in enumerate(names, start=1):
+                assert hashlib.md5(b.fetch(i)).hexdigest() == goldens[n]["md5"], (n, graph)
+
+
 def test_batch_result_counts_match_plain(sieve):
     """Each batched job reports the rows, sieving primes and unknowns of the
     same job run alone (the bench's pairs come from these counts)."""
