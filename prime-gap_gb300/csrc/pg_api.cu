@@ -54,6 +54,10 @@ void pgs_destroy(pgs_ctx *ctx) {
     ctx->win_off.release();
     ctx->win_r.release();
     ctx->win_t0.release();
+    ctx->win_off2.release();
+    ctx->win_r2.release();
+    ctx->win_t02.release();
+    if (ctx->aux) cudaStreamDestroy(ctx->aux);
     ctx->large_ctr.release();
     ctx->heavy.release();
     ctx->walks.release();
@@ -176,6 +180,11 @@ int pgs_prepare(pgs_ctx *ctx, const pgs_job *job, pgs_prepared **out) {
     CK(ctx->win_off.ensure(pr->win_bound * 4 + 4));
     CK(ctx->win_r.ensure(pr->win_bound * 8 + 8));
     CK(ctx->win_t0.ensure(pr->win_bound * 8 + 8));
+    if (pr->windows.size() > 1) {
+        CK(ctx->win_off2.ensure(pr->win_bound * 4 + 4));
+        CK(ctx->win_r2.ensure(pr->win_bound * 8 + 8));
+        CK(ctx->win_t02.ensure(pr->win_bound * 8 + 8));
+    }
     CK(ctx->large_ctr.ensure(pg::kLargeCounters * sizeof(unsigned long long)));
     CK(ctx->heavy.ensure((size_t)pg::heavy_capacity() * pg::kHeavyPrimeBytes));
     CK(cudaStreamSynchronize(s));
@@ -335,7 +344,7 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
     pr->events.resize(2);
     pr->spans.clear();
     pr->launches = 0;
-    auto mark = [&](int &idx) -> cudaError_t {
+    auto mark_on = [&](int &idx, cudaStream_t st) -> cudaError_t {
         idx = -1;
         if (!record_stages) return cudaSuccess;
         cudaEvent_t e;
@@ -343,8 +352,9 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
         if (err) return err;
         pr->events.push_back(e);
         idx = (int)pr->events.size() - 1;
-        return cudaEventRecord(e, s);
+        return cudaEventRecord(e, st);
     };
+    auto mark = [&](int &idx) -> cudaError_t { return mark_on(idx, s); };
     int a = -1, b = -1, first = -1;
     auto span = [&](int stage, int ea, int eb) {
         if (record_stages) pr->spans.push_back({stage, {ea, eb}});
@@ -381,40 +391,118 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
     // K mod p of a window's primes inside the large-prime kernel: bit 1 of
     // the form for windows of 32-bit primes, bit 2 for 64-bit primes
     const bool limbs_fit = h.klimbs.size() <= (size_t)pg::kParamLimbs;
-    // large primes, window by window, marking through the job descriptor jd
+    // large primes, window by window, marking through the job descriptor jd.
+    // With two or more windows the primes and K mod p of window w + 1 are
+    // made on the auxiliary stream into the other buffer set while the large
+    // primes of window w run on the job's stream: their CTAs take the SM
+    // slots that the large-prime kernel's persistent CTAs give back as they
+    // run out of groups, so the window's tail is not idle.  (Reserving slots
+    // for them instead, two CTAs per SM, measured the same on config 2 and
+    // cost config 3 7.6 ms, whose fused 64-bit kernel has only four.)  The
+    // stage times of the later windows' primes and K mod p are not recorded:
+    // they run inside the large-prime spans.
+    const size_t nwin = pr->windows.size();
+    const bool overlap = nwin > 1;
+    if (overlap && !ctx->aux) {
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CK(cudaStreamCreateWithPriority(&ctx->aux, cudaStreamNonBlocking, greatest));
+    }
     auto large_phase = [&](const pg::JobDev &jd) -> cudaError_t {
-        for (size_t w = 0; w < pr->windows.size(); w++) {
+        if (nwin == 0) return cudaSuccess;  // every prime is a small one
+        cudaError_t e;
+        std::vector<cudaEvent_t> made(nwin, nullptr), used(nwin, nullptr);
+        auto cleanup = [&]() {
+            for (auto ev : made)
+                if (ev) cudaEventDestroy(ev);
+            for (auto ev : used)
+                if (ev) cudaEventDestroy(ev);
+        };
+        // window w's primes and K mod p, on stream `ps`, into buffer set w & 1
+        auto produce = [&](size_t w, cudaStream_t ps) -> cudaError_t {
             const Window &win = pr->windows[w];
             unsigned long long *rng = misc + 3 + 2 * w, *cnt = rng + 1;
-            int e_a, e_b, e_c, e_d;
-            cudaError_t e;
-            if ((e = mark(e_a))) return e;
-            if ((e = pg::sieve_window(ctx->base, win.lo, win.hi, ctx->win_off.as<uint32_t>(), win.bound, cnt, s)))
-                return e;
+            const bool second = overlap && (w & 1);
+            uint32_t *off = second ? ctx->win_off2.as<uint32_t>() : ctx->win_off.as<uint32_t>();
+            void *wr = second ? ctx->win_r2.p : ctx->win_r.p, *wt = second ? ctx->win_t02.p : ctx->win_t0.p;
+            cudaError_t err;
+            int e_a = -1, e_b = -1, e_c = -1;
+            const bool timed = ps == s;  // the first window only
+            if (timed && (err = mark_on(e_a, ps))) return err;
+            if ((err = pg::sieve_window(ctx->base, win.lo, win.hi, off, win.bound, cnt, ps))) return err;
+            if (timed && (err = mark_on(e_b, ps))) return err;
             const bool fuse = limbs_fit && (pr->tune.large_form & (win.wide ? 4u : 2u));
-            if ((e = mark(e_b))) return e;
             if (!fuse &&
-                (e = pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo,
-                                     ctx->win_off.as<uint32_t>(), rng, win.bound, &h.walk, ctx->win_r.p,
-                                     ctx->win_t0.p, win.wide, s, (int)pr->tune.kmod_lsb_limbs, h.klimbs.data())))
+                (err = pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), win.lo, off, rng, win.bound,
+                                       &h.walk, wr, wt, win.wide, ps, (int)pr->tune.kmod_lsb_limbs,
+                                       h.klimbs.data())))
+                return err;
+            if (timed) {
+                if ((err = mark_on(e_c, ps))) return err;
+                span(PGS_STAGE_PRIMES, e_a, e_b);
+                span(PGS_STAGE_KMOD, e_b, e_c);
+            }
+            pr->launches += fuse ? 1 : 2;
+            return cudaSuccess;
+        };
+        if ((e = produce(0, s))) return e;
+        cudaEvent_t first_made = nullptr;
+        if (overlap) {
+            // the second window starts once the first one's K mod p is done,
+            // so that it runs beside the first window's large primes
+            if ((e = cudaEventCreateWithFlags(&first_made, cudaEventDisableTiming))) return e;
+            if ((e = cudaEventRecord(first_made, s)) || (e = cudaStreamWaitEvent(ctx->aux, first_made, 0))) {
+                cudaEventDestroy(first_made);
                 return e;
-            if ((e = mark(e_c))) return e;
-            e = pg::large_window(jd, win.lo, ctx->win_off.as<uint32_t>(), rng, win.bound, ctx->win_r.p,
-                                 ctx->win_t0.p, rng, win.wide, false, pr->mmask.as<uint2>(), pr->ymask.as<uint2>(),
+            }
+            cudaEventDestroy(first_made);
+        }
+        for (size_t w = 0; w < nwin; w++) {
+            if (overlap && w + 1 < nwin) {
+                // the next window on the auxiliary stream, once its buffers are free
+                if (w >= 1 && (e = cudaStreamWaitEvent(ctx->aux, used[w - 1], 0))) break;
+                if ((e = produce(w + 1, ctx->aux))) break;
+                if ((e = cudaEventCreateWithFlags(&made[w + 1], cudaEventDisableTiming))) break;
+                if ((e = cudaEventRecord(made[w + 1], ctx->aux))) break;
+            }
+            if (w >= 1 && overlap && (e = cudaStreamWaitEvent(s, made[w], 0))) break;
+            const Window &win = pr->windows[w];
+            unsigned long long *rng = misc + 3 + 2 * w;
+            const bool second = overlap && (w & 1);
+            const bool fuse = limbs_fit && (pr->tune.large_form & (win.wide ? 4u : 2u));
+            int e_c, e_d;
+            if ((e = mark(e_c))) break;
+            e = pg::large_window(jd, win.lo, second ? ctx->win_off2.as<uint32_t>() : ctx->win_off.as<uint32_t>(), rng,
+                                 win.bound, second ? ctx->win_r2.p : ctx->win_r.p,
+                                 second ? ctx->win_t02.p : ctx->win_t0.p, rng, win.wide, false,
+                                 pr->mmask.as<uint2>(), pr->ymask.as<uint2>(),
                                  pg::LargeScratch{ctx->large_ctr.as<unsigned long long>(),
                                                   ctx->heavy.as<pg::HeavyPrime>(), pg::heavy_capacity(),
                                                   ctx->walks.as<pg::WalkEntry>(),
                                                   ctx->walks.p ? pg::walk_capacity() : 0u},
                                  s, fuse ? h.klimbs.data() : nullptr, (int)h.klimbs.size(),
                                  pg::kmod_lsb((int)h.klimbs.size(), win.wide, (int)pr->tune.kmod_lsb_limbs));
-            if (e) return e;
-            if ((e = mark(e_d))) return e;
-            span(PGS_STAGE_PRIMES, e_a, e_b);
-            span(PGS_STAGE_KMOD, e_b, e_c);
+            if (e) break;
+            if ((e = mark(e_d))) break;
             span(PGS_STAGE_LARGE, e_c, e_d);
-            pr->launches += fuse ? 3 : 4;
+            if (overlap) {
+                if ((e = cudaEventCreateWithFlags(&used[w], cudaEventDisableTiming))) break;
+                if ((e = cudaEventRecord(used[w], s))) break;
+            }
+            pr->launches += 1;
         }
-        return cudaSuccess;
+        // the job's stream waits for the auxiliary stream's last work (none
+        // left past the last window's wait, but an error may leave some)
+        if (overlap && e == cudaSuccess) {
+            cudaEvent_t tail;
+            if ((e = cudaEventCreateWithFlags(&tail, cudaEventDisableTiming)) == cudaSuccess) {
+                if ((e = cudaEventRecord(tail, ctx->aux)) == cudaSuccess) e = cudaStreamWaitEvent(s, tail, 0);
+                cudaEventDestroy(tail);
+            }
+        }
+        if (e != cudaSuccess && overlap) cudaStreamSynchronize(ctx->aux);
+        cleanup();
+        return e;
     };
     if (!per_m) {
         CK(large_phase(job));

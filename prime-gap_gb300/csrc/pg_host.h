@@ -200,6 +200,10 @@ struct pgs_ctx {
     std::string err;
     pg::BasePrimes base;
     pgh::DevBuf win_off, win_r, win_t0, large_ctr, heavy, walks;
+    // the next window's primes and K mod p, made on `aux` while the large
+    // primes of the current window run on the job's stream
+    pgh::DevBuf win_off2, win_r2, win_t02;
+    cudaStream_t aux = nullptr;
     pgh::DevicePool dpool;
     // batched / served paths (pg_batch.cu)
     PrimeTable *table = nullptr;
