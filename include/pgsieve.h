@@ -80,11 +80,12 @@ void pgs_destroy(pgs_ctx *ctx);
 /* Human-readable description of the last error on this context. */
 const char *pgs_last_error(pgs_ctx *ctx);
 /* Use an external CUDA stream (cudaStream_t as void*); NULL restores the
- * context's own stream.  A job with more than one prime window also runs
- * the next window's primes and K mod p on a second stream of the context,
- * which waits on this stream before its first launch and which this stream
- * waits on before the job's rows: the job's work stays ordered after what
- * came before it on this stream and before what comes after. */
+ * context's own stream.  A job also runs part of its work on a second
+ * stream of the context (the small primes that its rows read and, with more
+ * than one prime window, the next window's primes and K mod p), which waits
+ * on this stream before its first launch and which this stream waits on
+ * before the job's rows: the job's work stays ordered after what came
+ * before it on this stream and before what comes after. */
 int pgs_set_stream(pgs_ctx *ctx, void *stream);
 /* The stream the context launches on (cudaStream_t as void*). */
 void *pgs_get_stream(pgs_ctx *ctx);

@@ -334,7 +334,7 @@ int text_pipeline(pgs_ctx *ctx, pgs_prepared *pr, const pg::RowsDev &rd, uint32_
 
 // One run of a prepared job (context locked).  With `sink`, the rows and
 // text are pipelined with their copy to the host (text_pipeline).
-int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, bool per_m = false) {
+int run_job_on(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, bool per_m) {
     CK(cudaSetDevice(ctx->device));
     cudaStream_t s = ctx->stream;
     HostJob &h = pr->hj;
@@ -367,23 +367,43 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
     CK(cudaMemsetAsync(pr->comp.p, 0, rows * h.pitch * 4ull, s));
     CK(cudaMemsetAsync(pr->misc.p, 0, (3 + 2 * pr->windows.size()) * 8, s));
 
-    // small primes (P, S1] and the odd primes of d
+    // The auxiliary stream: it makes what only the rows read, and later
+    // windows' primes and K mod p, beside the job's stream, which it waits
+    // on here and which waits on it before the rows.
+    if (!ctx->aux) {
+        int least = 0, greatest = 0;
+        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        CK(cudaStreamCreateWithPriority(&ctx->aux, cudaStreamNonBlocking, greatest));
+    }
+    cudaStream_t aux = ctx->aux;
+    auto join = [&](cudaStream_t from, cudaStream_t to) -> cudaError_t {
+        cudaEvent_t ev;
+        cudaError_t err = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (err) return err;
+        if ((err = cudaEventRecord(ev, from)) == cudaSuccess) err = cudaStreamWaitEvent(to, ev, 0);
+        cudaEventDestroy(ev);
+        return err;
+    };
+    CK(join(s, aux));
+
+    // small primes (P, S1] and the odd primes of d, read by the rows only:
+    // on the auxiliary stream, beside the first window's primes and K mod p
     if (pr->sp_bound) {
-        CK(mark(a));
+        CK(mark_on(a, aux));
         CK(pg::sieve_window(ctx->base, pr->sp_lo, pr->sp_hi, pr->sp.as<uint32_t>(), pr->sp_bound,
-                            misc + 2, s));
-        CK(mark(b));
+                            misc + 2, aux));
+        CK(mark_on(b, aux));
         span(PGS_STAGE_PRIMES, a, b);
         CK(pg::kmod_window(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), pr->sp_lo,
                            pr->sp.as<uint32_t>(), misc + 1, pr->sp_bound, nullptr, pr->sr.p,
-                           nullptr, false, s, 0, h.klimbs.data()));
-        CK(mark(a));
+                           nullptr, false, aux, 0, h.klimbs.data()));
+        CK(mark_on(a, aux));
         span(PGS_STAGE_KMOD, b, a);
         pr->launches += 2;
     }
     if (!h.dq.empty()) {
         CK(pg::kmod_list32(pr->klimbs.as<uint32_t>(), (int)h.klimbs.size(), pr->dq.as<uint32_t>(),
-                           (uint32_t)h.dq.size(), pr->dr.as<uint32_t>(), s));
+                           (uint32_t)h.dq.size(), pr->dr.as<uint32_t>(), aux));
         pr->launches += 1;
     }
     // the warp-alone form's walk list, on first use
@@ -403,11 +423,6 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
     // they run inside the large-prime spans.
     const size_t nwin = pr->windows.size();
     const bool overlap = nwin > 1;
-    if (overlap && !ctx->aux) {
-        int least = 0, greatest = 0;
-        CK(cudaDeviceGetStreamPriorityRange(&least, &greatest));
-        CK(cudaStreamCreateWithPriority(&ctx->aux, cudaStreamNonBlocking, greatest));
-    }
     auto large_phase = [&](const pg::JobDev &jd) -> cudaError_t {
         if (nwin == 0) return cudaSuccess;  // every prime is a small one
         cudaError_t e;
@@ -491,16 +506,6 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
             }
             pr->launches += 1;
         }
-        // the job's stream waits for the auxiliary stream's last work (none
-        // left past the last window's wait, but an error may leave some)
-        if (overlap && e == cudaSuccess) {
-            cudaEvent_t tail;
-            if ((e = cudaEventCreateWithFlags(&tail, cudaEventDisableTiming)) == cudaSuccess) {
-                if ((e = cudaEventRecord(tail, ctx->aux)) == cudaSuccess) e = cudaStreamWaitEvent(s, tail, 0);
-                cudaEventDestroy(tail);
-            }
-        }
-        if (e != cudaSuccess && overlap) cudaStreamSynchronize(ctx->aux);
         cleanup();
         return e;
     };
@@ -538,7 +543,8 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
         CK(pg::bucket_apply(jd, offs + rows, s));
         pr->launches += 2;
     }
-    // rows, text
+    // rows, text, once the auxiliary stream's small primes are made
+    CK(join(aux, s));
     CK(mark(a));
     if (sink) {
         // rows and text interleave with the copy: one span for both
@@ -562,6 +568,13 @@ int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, b
     pr->launches += 5;
     pr->ran = true;
     return PGS_OK;
+}
+
+int run_job(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink, bool per_m = false) {
+    const int rc = run_job_on(ctx, pr, record_stages, sink, per_m);
+    // nothing of a failed run may still be running on the auxiliary stream
+    if (rc != PGS_OK && ctx->aux) cudaStreamSynchronize(ctx->aux);
+    return rc;
 }
 
 }  // namespace
