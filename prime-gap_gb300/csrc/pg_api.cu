@@ -504,7 +504,9 @@ int run_job_on(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink
                 if ((e = cudaEventCreateWithFlags(&used[w], cudaEventDisableTiming))) break;
                 if ((e = cudaEventRecord(used[w], s))) break;
             }
-            pr->launches += 1;
+            // the large-prime kernel and the heavy list's, and the walks' in
+            // the warp-alone form
+            pr->launches += (pr->tune.large_form & 1u) && ctx->walks.p ? 3 : 2;
         }
         cleanup();
         return e;
