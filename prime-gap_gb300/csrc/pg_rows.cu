@@ -70,16 +70,23 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
         s_h0[j * kMaxDPrimes + t] = ((x0 - x_par) >> 1) % q;
     }
     __syncthreads();
-    for (uint32_t idx = threadIdx.x; idx < nrows * nbw; idx += blockDim.x) {
-        uint32_t j = idx / nbw, w = idx % nbw;
-        uint32_t word = 0;
+    // Word w of row j has q's bits at b = (h0 - 32 w) mod q + k q (h0: the
+    // row's first multiple): one thread per word for all the CTA's rows, so
+    // 32 w mod q and q's word pattern are found once per (word, q) and each
+    // row costs a subtraction.
+    for (uint32_t w = threadIdx.x; w < nbw; w += blockDim.x) {
+        for (uint32_t j = 0; j < nrows; j++) sh[j * nbw + w] = 0;
         for (uint32_t t = 0; t < rd.nd; t++) {
-            uint32_t q = rd.dq[t];
-            uint32_t o = (s_h0[j * kMaxDPrimes + t] + q - (32u * w) % q) % q;
-            if (o < 32) word |= word_pattern(q) << o;
+            const uint32_t q = rd.dq[t];
+            const uint32_t pat = word_pattern(q), c = (32u * w) % q;
+            for (uint32_t j = 0; j < nrows; j++) {
+                const uint32_t h0 = s_h0[j * kMaxDPrimes + t];  // < q
+                const uint32_t o = h0 >= c ? h0 - c : h0 + (q - c);
+                if (o < 32) sh[j * nbw + w] |= pat << o;
+            }
         }
-        sh[j * nbw + w] = word;
-        if (rd.compression == 2) s_pat[j * nbw + w] = word;
+        if (rd.compression == 2)
+            for (uint32_t j = 0; j < nrows; j++) s_pat[j * nbw + w] = sh[j * nbw + w];
     }
     __syncthreads();
 
@@ -89,9 +96,13 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
     const uint32_t mi_first = s_mi[0];
     for (uint64_t i = threadIdx.x; i < ns; i += blockDim.x) {
         const uint32_t p = rd.sp_base + rd.sp[sp_begin + i], r = rd.sr[i];
-        uint64_t m = job.mstart + mi_first;
-        uint32_t mr = (uint32_t)(((m % p) * r) % p);
-        uint32_t x0 = (sl % p + p - mr) % p;
+        const uint64_t m = job.mstart + mi_first;
+        // (sl - m r) mod p, with 32-bit remainders where the operands fit
+        const uint32_t mm = (m >> 32) ? (uint32_t)(m % p) : (uint32_t)m % p;
+        const uint64_t prod = (uint64_t)mm * r;
+        const uint32_t mr = (prod >> 32) ? (uint32_t)(prod % p) : (uint32_t)prod % p;
+        const uint32_t sr = sl % p;
+        uint32_t x0 = sr >= mr ? sr - mr : sr + (p - mr);
         // row by row (the same row across the warp): step the residue over
         // the m values since the previous row, then strike this row; with d
         // even every valid m is odd, so the step is 2r mod p per two m
