@@ -417,8 +417,10 @@ int run_job_on(pgs_ctx *ctx, pgs_prepared *pr, int record_stages, HostText *sink
     // primes of window w run on the job's stream: their CTAs take the SM
     // slots that the large-prime kernel's persistent CTAs give back as they
     // run out of groups, so the window's tail is not idle.  (Reserving slots
-    // for them instead, two CTAs per SM, measured the same on config 2 and
-    // cost config 3 7.6 ms, whose fused 64-bit kernel has only four.)  The
+    // for them instead, two CTAs per SM, measured the same on the job of
+    // P = 1511, SL = 2e4, 1e5 m, primes to 2e9, and cost the job of P = 3001,
+    // SL = 4e4, 1e5 m, primes to 1e10 7.6 ms: its fused 64-bit kernel runs
+    // only four CTAs per SM.)  The
     // stage times of the later windows' primes and K mod p are not recorded:
     // they run inside the large-prime spans.
     const size_t nwin = pr->windows.size();

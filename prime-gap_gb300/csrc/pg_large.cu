@@ -364,9 +364,10 @@ __global__ void __launch_bounds__(kLargeThreads, sizeof(T) == 4 ? 8 : 1)
 // steps to walk_kernel (one warp per walk), more to heavy_kernel (one CTA per
 // prime).  A full list falls back to the next one, and finally to walking the
 // rotation in this thread.  Faster than the pooled form when walks are short
-// (small jobs: config 1's large stage 0.43 -> 0.35 ms), slower when many walks
-// of 25-100 steps leave each lane of walk_kernel only a few steps after its
-// closed-form start (config 2: 5.85 -> 8.64 ms); the tuner picks per class.
+// (small jobs: P = 503, SL = 5e3, 1e4 m, primes to 1e8: large stage 0.43 ->
+// 0.35 ms), slower when many walks of 25-100 steps leave each lane of
+// walk_kernel only a few steps after its closed-form start (P = 1511,
+// SL = 2e4, 1e5 m, primes to 2e9: 5.85 -> 8.64 ms); the tuner picks per class.
 template <typename T, int kIn, bool kShared>
 __global__ void __launch_bounds__(kLargeThreads)
     large_cf_kernel(const __grid_constant__ KLimbs<kIn >= kInLimbsLsb ? kParamLimbs : 1> kl, int nlimbs,
