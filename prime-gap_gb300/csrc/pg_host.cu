@@ -190,6 +190,12 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
         if (coprime[x] && ((x & 1) == h.x_par)) h.dist.push_back(dd);
     }
     h.H = (uint32_t)h.dist.size();
+    h.live.assign((h.nb + 31) / 32, 0);
+    for (uint32_t dd : h.dist)
+        for (uint32_t x : {SL - dd, SL + dd}) {
+            const uint32_t hx = (x - h.x_par) >> 1;
+            h.live[hx >> 5] |= 1u << (hx & 31);
+        }
     h.Hp = (h.H + 31) / 32 * 32;
     h.pitch = (2 * h.Hp / 32 + 3) / 4 * 4;
     if (h.pitch == 0) h.pitch = 4;
@@ -281,6 +287,7 @@ pg::RowsDev rows_dev(pgs_prepared *pr) {
     rd.nb = h.nb;
     rd.valid_mi = pr->valid_mi.as<uint32_t>();
     rd.dist = pr->dist.as<uint32_t>();
+    rd.live = pr->live.as<uint32_t>();
     rd.nd = (uint32_t)h.dq.size();
     rd.dq = pr->dq.as<uint32_t>();
     rd.dr = pr->dr.as<uint32_t>();
@@ -321,6 +328,7 @@ cudaError_t upload_tables(pgs_prepared *pr, cudaStream_t s) {
     } items[] = {{&pr->klimbs, h.klimbs.data(), h.klimbs.size() * 4},
                  {&pr->valid_mi, h.valid_mi.data(), h.valid_mi.size() * 4},
                  {&pr->dist, h.dist.data(), h.dist.size() * 4},
+                 {&pr->live, h.live.data(), h.live.size() * 4},
                  {&pr->dq, h.dq.data(), h.dq.size() * 4},
                  {&pr->mmask, h.mmask.data(), h.mmask.size() * 4},
                  {&pr->ymask, h.ymask.data(), h.ymask.size() * 4}};

@@ -29,6 +29,8 @@ struct HostJob {
     uint32_t kbits = 0;
     std::vector<uint32_t> valid_mi;
     std::vector<uint32_t> dist;
+    // the live offsets over the row bitmap's index (x - x_par) / 2, nb bits
+    std::vector<uint32_t> live;
     std::vector<uint32_t> dq;  // odd primes dividing d
     // valid-m bitmask over walk indices j and live-offset bitmask over walk
     // residues y (pg_host.cu), as {bits, set bits before the word} pairs
@@ -232,7 +234,7 @@ struct pgs_prepared {
     uint64_t large_primes = ~0ull;
     size_t footprint = 0;  // device bytes held by this job
     uint64_t win_bound = 0;
-    pgh::DevBuf klimbs, valid_mi, dist, dq, dr, comp, sp, sr, sp_t0, mmask, ymask;
+    pgh::DevBuf klimbs, valid_mi, dist, live, dq, dr, comp, sp, sr, sp_t0, mmask, ymask;
     pgh::DevBuf lists, counts, row_bytes, offsets, scan_tmp, misc, text;
     pgh::DevBuf row_count, row_off, bucket;  // the per-m path (method1)
     std::vector<cudaEvent_t> events;
@@ -241,9 +243,10 @@ struct pgs_prepared {
     uint64_t launches = 0;
     bool ran = false;
     std::vector<pgh::DevBuf *> all() {
-        return {&klimbs, &valid_mi, &dist,  &dq,       &dr,        &comp,     &sp,
-                &sr,     &sp_t0,    &lists, &counts,   &row_bytes, &offsets,  &scan_tmp,
-                &misc,   &text,     &mmask, &ymask,    &row_count, &row_off,  &bucket};
+        return {&klimbs, &valid_mi, &dist,  &live,     &dq,        &dr,       &comp,
+                &sp,     &sr,       &sp_t0, &lists,    &counts,    &row_bytes, &offsets,
+                &scan_tmp, &misc,   &text,  &mmask,    &ymask,     &row_count, &row_off,
+                &bucket};
     }
     char *stage = nullptr;  // pinned staging block of the table uploads
     size_t stage_cap = 0;

@@ -199,6 +199,7 @@ struct RowsDev {
     uint32_t nb;               // positions x in [0, 2SL] with x % 2 == x_par
     const uint32_t *valid_mi;  // rows entries
     const uint32_t *dist;      // H live distances, ascending
+    const uint32_t *live;      // nb bits: the live offsets over (x - x_par) / 2
     // odd primes dividing d (patterns) and their K mod q
     uint32_t nd;
     const uint32_t *dq;

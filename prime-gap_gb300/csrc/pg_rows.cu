@@ -122,7 +122,6 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
     // 3. merge with the large-prime bits and compact, one warp per row
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
     const uint32_t H = job.half_cols;
-    const uint32_t lt_mask = (1u << lane) - 1;
     if (rd.compression == 2) {
         // Bitcompressed rows (combined_sieve.cpp:1327-1385): over the offsets
         // in increasing X that are coprime to K and to every prime of d
@@ -179,46 +178,79 @@ __global__ void __launch_bounds__(kRowThreads) rows_kernel(RowsDev rd, uint32_t 
         }
         return;
     }
+    // Plain and RLE rows.  The large-prime marks (one bit per live offset,
+    // in distance order on each side) go into the row's bitmap over offset
+    // indexes, one lane per word of marks; then the live offsets left
+    // unmarked are read off that bitmap a word per lane, nearest to SL first
+    // on each side, each distance following from its index.
+    const uint32_t side_words = job.side_pad >> 5;
+    const uint32_t hs = (sl - x_par + 1) >> 1;  // indexes below hs: x < SL
     for (uint32_t j = warp; j < nrows; j += nwarps) {
         const uint32_t row = r0 + j;
         const uint32_t *grow = job.comp + (uint64_t)row * job.pitch;
+        uint32_t *bm = sh + j * nbw;
+        for (uint32_t cw = lane; cw < 2 * side_words; cw += 32) {
+            uint32_t bits = grow[cw];
+            const uint32_t side = cw >= side_words ? 1u : 0u;
+            const uint32_t h0 = 32 * (cw - side * side_words);
+            while (bits) {
+                const uint32_t h = h0 + __ffs(bits) - 1;
+                bits &= bits - 1;
+                if (h >= H) continue;  // columns past H are never marked
+                const uint32_t d = rd.dist[h];
+                const uint32_t hx = ((side ? sl + d : sl - d) - x_par) >> 1;
+                atomicOr(&bm[hx >> 5], 1u << (hx & 31));
+            }
+        }
+        __syncwarp();
         uint32_t *list = rd.lists + (uint64_t)row * 2 * H;
         uint64_t body = 0;
         uint32_t cnt_side[2];
         for (uint32_t side = 0; side < 2; side++) {
-            uint32_t cnt = 0;
-            uint32_t dsum = 0;
-            // digits of the distances: they ascend with h, so a round whose
-            // largest distance is below 10^D has D-digit distances only
-            // (D from the previous round); the others count per lane
-            uint32_t D = 1, T = 10;
-            for (uint32_t h0 = 0; h0 < H; h0 += 32) {
-                uint32_t h = h0 + lane;
-                bool unknown = false;
-                uint32_t d = 0;
-                if (h < H) {
-                    d = rd.dist[h];
-                    uint32_t x = side ? sl + d : sl - d;
-                    uint32_t hx = (x - x_par) >> 1;
-                    uint32_t sb = (sh[j * nbw + (hx >> 5)] >> (hx & 31)) & 1;
-                    uint32_t col = side * job.side_pad + h;
-                    uint32_t gb = (grow[col >> 5] >> (col & 31)) & 1;
-                    unknown = !(sb | gb);
-                }
-                uint32_t bal = __ballot_sync(0xFFFFFFFFu, unknown);
-                const uint32_t dmax = __reduce_max_sync(0xFFFFFFFFu, d);
-                uint32_t nd = D;
-                if (dmax >= T) {
-                    nd = ndigits(d);
-                    D = ndigits(dmax);
-                    for (T = 10; T <= dmax; T *= 10) {
+            // side 1: words from hs / 32 up; side 0: from (hs - 1) / 32 down
+            const uint32_t first = side ? hs >> 5 : (hs ? (hs - 1) >> 5 : 0);
+            const uint32_t nw = side ? nbw - (hs >> 5) : (hs ? ((hs - 1) >> 5) + 1 : 0);
+            uint32_t *out = list + side * H;
+            uint32_t cnt = 0, dsum = 0;
+            for (uint32_t k0 = 0; k0 < nw; k0 += 32) {
+                const uint32_t k = k0 + lane;
+                uint32_t u = 0, w = 0;
+                if (k < nw) {
+                    w = side ? first + k : first - k;
+                    u = rd.live[w] & ~bm[w];
+                    // the word holding hs has indexes of both sides
+                    const uint32_t lo = 32 * w;
+                    if (side) {
+                        if (lo < hs) u &= ~0u << (hs - lo);
+                    } else if (lo + 32 > hs) {
+                        u &= (1u << (hs - lo)) - 1;
                     }
                 }
-                if (unknown) {
-                    list[side * H + cnt + __popc(bal & lt_mask)] = d;
-                    dsum += nd;
+                const uint32_t c = __popc(u);
+                uint32_t incl = c;
+#pragma unroll
+                for (uint32_t off = 1; off < 32; off <<= 1) {
+                    const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, off);
+                    if ((uint32_t)lane >= off) incl += t;
                 }
-                cnt += __popc(bal);
+                uint32_t idx = cnt + incl - c;
+                // distances ascend within the word: D digits below T = 10^D
+                // (64-bit: the loop below ends for any 32-bit distance)
+                uint32_t D = 0;
+                uint64_t T = 1;
+                while (u) {
+                    const uint32_t b = side ? __ffs(u) - 1 : 31 - __clz(u);
+                    u ^= 1u << b;
+                    const uint32_t x = 2 * (32 * w + b) + x_par;
+                    const uint32_t d = side ? x - sl : sl - x;
+                    out[idx++] = d;
+                    while (d >= T) {
+                        D++;
+                        T *= 10;
+                    }
+                    dsum += D;
+                }
+                cnt += __shfl_sync(0xFFFFFFFFu, incl, 31);
             }
             dsum = __reduce_add_sync(0xFFFFFFFFu, dsum);
             cnt_side[side] = cnt;
