@@ -3,16 +3,17 @@
 //
 // Small primes replace method2_small_primes (combined_sieve.cpp:1450-1603):
 // for every m the multiples of each prime p <= 4*SL+2 (p > P, or p | d) are
-// struck from the offsets of m*K + X.  A CTA holds the bitmaps of kRows
+// struck from the offsets of m*K + X.  A CTA holds the bitmaps of up to 32
 // consecutive valid m in shared memory, over the offsets of the one parity
 // that can be prime (m*K + X odd).  Odd primes dividing d stamp a per-word
 // pattern that also initialises the bitmap; the other small primes are
 // marked by one thread each, walking the CTA's m values with the residue
 // update x0 <- x0 - r (mod p).
 //
-// The same CTA then reads each row's large-prime bits (written by pg_large.cu)
-// and compacts the surviving offsets, nearest first on each side, into a
-// per-row list; that replaces the coprime_prev/coprime_next walk of
+// The same CTA then ORs each row's large-prime bits (written by pg_large.cu,
+// one per live offset in distance order) into the row's bitmap and compacts
+// the live offsets left unmarked, nearest first on each side, into a per-row
+// list; that replaces the coprime_prev/coprime_next walk of
 // save_unknowns_method2 (combined_sieve.cpp:1289-1300, 1387-1438).
 // format_rows then writes the rows' text in parallel at offsets given by a
 // prefix sum of the per-row byte counts.
