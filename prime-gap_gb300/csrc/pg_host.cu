@@ -120,21 +120,28 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     h.x_par = d_even ? (SL & 1) : ((SL + 1) & 1);
     h.nb = h.x_par == 0 ? SL + 1 : SL;
 
-    // valid m (gap_common.cpp:307-342)
+    // valid m (gap_common.cpp:307-342).  The m and offset flags live in
+    // per-thread scratch that keeps its pages from one job to the next.
     const uint64_t minc = j.minc, ms = j.mstart;
-    std::vector<uint8_t> m_ok(minc, 1);
+    static thread_local std::vector<uint8_t> m_ok, coprime;
+    m_ok.assign(minc, 1);
     for (uint32_t q : pp) {
         if (D % q) continue;
         uint64_t first = (q - (ms % q)) % q;
         for (uint64_t mi = first; mi < minc; mi += q) m_ok[mi] = 0;
     }
     uint64_t valid = 0;
-    for (uint64_t mi = 0; mi < minc; mi++) valid += m_ok[mi];
+    {
+        const uint8_t *f = m_ok.data();
+        uint32_t acc = 0;  // minc < 2^31
+        for (uint64_t mi = 0; mi < minc; mi++) acc += f[mi];
+        valid = acc;
+    }
     if (valid == 0) return err = "no m coprime to d", PGS_EABORT;
 
     // offsets coprime to K (combined_sieve.cpp:1143-1169)
     const uint32_t interval = 2 * SL + 1;
-    std::vector<uint8_t> coprime(interval, 1);
+    coprime.assign(interval, 1);
     for (uint32_t q : pp) {
         if (D % q == 0) continue;
         for (uint32_t x = SL % q; x < interval; x += q) coprime[x] = 0;
@@ -181,13 +188,29 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     h.filename = fn;
     if (!tables) return PGS_OK;
 
-    h.valid_mi.reserve(valid);
-    for (uint64_t mi = 0; mi < minc; mi++)
-        if (m_ok[mi]) h.valid_mi.push_back((uint32_t)mi);
+    // lists written without branches: every index is stored, and the
+    // write position advances past the ones that stay
+    h.valid_mi.resize(valid + 1);
+    {
+        uint32_t *o = h.valid_mi.data();
+        uint64_t n = 0;
+        for (uint64_t mi = 0; mi < minc; mi++) {
+            o[n] = (uint32_t)mi;
+            n += m_ok[mi];
+        }
+    }
+    h.valid_mi.resize(valid);
     // live offsets: coprime to K and of the parity that makes m*K + X odd
-    for (uint32_t dd = 1; dd <= SL; dd++) {
-        uint32_t x = SL + dd;
-        if (coprime[x] && ((x & 1) == h.x_par)) h.dist.push_back(dd);
+    {
+        const uint32_t dd0 = ((SL + 1) & 1) == h.x_par ? 1 : 2;
+        h.dist.resize(SL / 2 + 2);
+        uint32_t *o = h.dist.data();
+        uint32_t n = 0;
+        for (uint32_t dd = dd0; dd <= SL; dd += 2) {
+            o[n] = dd;
+            n += coprime[SL + dd];
+        }
+        h.dist.resize(n);
     }
     h.H = (uint32_t)h.dist.size();
     h.live.assign((h.nb + 31) / 32, 0);
@@ -229,8 +252,17 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     // above SL.
     h.mmask.assign((w.jmax + 31) / 32, 0);
     uint64_t on_lattice = 0;
-    for (uint64_t j = 0; j < w.jmax; j++)
-        if (m_ok[w.mi_base + w.stride * j]) h.mmask[j >> 5] |= 1u << (j & 31), on_lattice++;
+    {
+        // a word at a time in a register (mi_base + stride * j < minc)
+        const uint8_t *f = m_ok.data() + w.mi_base;
+        for (uint64_t wi = 0; wi < h.mmask.size(); wi++) {
+            const uint64_t j0 = 32 * wi, jn = std::min<uint64_t>(32, w.jmax - j0);
+            uint32_t word = 0;
+            for (uint64_t b = 0; b < jn; b++) word |= (uint32_t)f[w.stride * (j0 + b)] << b;
+            h.mmask[wi] = word;
+            on_lattice += (uint64_t)__builtin_popcount(word);
+        }
+    }
     if (on_lattice != valid) return err = "valid m off the walk lattice", PGS_EABORT;
     h.ymask.assign((w.w + 31) / 32, 0);
     for (uint32_t dd : h.dist)
