@@ -124,6 +124,12 @@ int derive(const pgs_job &j, HostJob &h, std::string &err, bool tables) {
     // per-thread scratch that keeps its pages from one job to the next.
     const uint64_t minc = j.minc, ms = j.mstart;
     static thread_local std::vector<uint8_t> m_ok, coprime;
+    struct Trim {  // a huge job's flags are not kept past the call
+        ~Trim() {
+            for (std::vector<uint8_t> *v : {&m_ok, &coprime})
+                if (v->capacity() > (16u << 20)) std::vector<uint8_t>().swap(*v);
+        }
+    } trim;
     m_ok.assign(minc, 1);
     for (uint32_t q : pp) {
         if (D % q) continue;
