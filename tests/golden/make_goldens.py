@@ -59,6 +59,12 @@ JOBS = [
     ("small_rle_d210", 503, 210, 9999, 2000, 5000, 60, ["--rle"], None, "reference run"),
     ("small_bc_d30", 521, 30, 2024, 1500, 5000, 40, ["--bitcompressed"], None, "reference run"),
     ("edge_maxprime_1M", 503, 210, 1, 1000, 5000, 1, [], None, "reference run"),
+    # m past 2^32 (64-bit m in the walk starts, the row residues and the text),
+    # up to the reference's limit mstart + minc <= 1e10 + 1
+    ("big_m_cross_2e32", 503, 210, 4294965796, 3000, 5000, 100, [], None, "reference run"),
+    ("big_m_1e10_d7_odd", 509, 7, 9999997000, 3000, 3500, 10, [], None, "reference run"),
+    ("big_m_rle_d2190", 907, 2190, 6000000001, 2000, 11000, 100, ["--rle"], None, "reference run"),
+    ("big_m_bc_d30", 521, 30, 8589934000, 1500, 5000, 40, ["--bitcompressed"], None, "reference run"),
 ]
 LARGE_JOBS = [
     ("config2", 1511, 2190, 12345679, 100000, 20000, 2000, [], None, "reference run"),

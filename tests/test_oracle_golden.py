@@ -14,7 +14,9 @@ import pgo
 
 FAST = ["fn1", "fn1_rle", "fn1_bitcompressed", "fn2", "config1", "small_d1", "small_d2",
         "small_d30", "small_d2190", "small_d30030", "small_d7_odd", "small_d73_sl_odd",
-        "small_rle_d210", "small_bc_d30", "edge_maxprime_1M"]
+        "small_rle_d210", "small_bc_d30", "edge_maxprime_1M",
+        # m past 2^32, up to the reference's mstart + minc <= 1e10 + 1
+        "big_m_cross_2e32", "big_m_1e10_d7_odd", "big_m_rle_d2190", "big_m_bc_d30"]
 
 
 def _job(g):
